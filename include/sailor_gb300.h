@@ -1,0 +1,211 @@
+/*
+ * sailor_gb300.h -- C ABI of the GB300 (sm_103a) VoxelEncoding library.
+ *
+ * Plain pointers and sizes only; every pointer named d_* or documented as
+ * device memory must be a CUDA device (or managed) address.  Every entry
+ * point enqueues work on `stream` (NULL = legacy default stream) and returns
+ * a status code without synchronising; conditions only the device can see
+ * (capacity overflow) are reported through a caller-provided device status
+ * block (SgStatus) that the caller reads after synchronising.  No entry
+ * point calls exit(); the reference's CUDA_CHECK_ERRORS (include/cuda_helper.h:
+ * 31-40 of the SAILOR project) prints and exits instead.
+ *
+ * Each function names the reference interface it replaces (paths relative to
+ * the SAILOR project root).  Tensor layouts are the reference's.
+ */
+#ifndef SAILOR_GB300_H
+#define SAILOR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *sg_stream_t; /* == cudaStream_t */
+
+enum {
+  SG_OK = 0,
+  SG_ERR_INVALID_ARG = 1, /* null pointer, bad size, misaligned pointer */
+  SG_ERR_CUDA = 2,        /* a launch failed (cudaGetLastError)            */
+  SG_ERR_CAPACITY = 3,    /* output capacity exceeded (see SgStatus)      */
+  SG_ERR_UNSUPPORTED = 4  /* a configuration the library does not handle   */
+};
+
+/* Device-side status block written by kernels (atomicOr / atomicMax). */
+typedef struct SgStatus {
+  int flags;         /* bit 0: hit-list overflow, bit 1: tree capacity      */
+  int max_hits;      /* largest per-ray hit count seen (traversal)          */
+  int need_top;      /* required top-node capacity when bit 1 is set        */
+  int need_bottom;   /* required bottom-node capacity when bit 1 is set     */
+} SgStatus;
+
+#define SG_FLAG_HIT_OVERFLOW 1
+#define SG_FLAG_TREE_CAPACITY 2
+
+/* Two-level brick tree kept in device memory (replaces the AoS OcTree node
+ * array of include/octree.h:30-153 and MultiLayerOctree's buffers
+ * :274-302).  Node ids keep the reference's id space: fine voxels (level 0)
+ * are base_bot + j, top bricks (level 1) base_top + k. */
+typedef struct SgTree {
+  int B;          /* frames (batch)                                      */
+  int Dt;         /* top grid edge (bricks)                              */
+  int Db;         /* fine grid edge (voxels), Db = Dt * rate             */
+  int rate;       /* brick edge in voxels                                */
+  int base_top;   /* id of top node 0 (octree_nodes_index[1])            */
+  int base_bot;   /* id of bottom node 0 (octree_nodes_index[0])         */
+  int cap_top;    /* capacity of top_key/top_child_base                  */
+  int cap_bot;    /* capacity of bot_key/bot_parent                      */
+  int *brick_node;        /* [B*Dt^3] top node index k, or -1           */
+  uint32_t *brick_mask;   /* [B*Dt^3*mask_words] fine occupancy bits     */
+  int *top_key;           /* [cap_top] b*Dt^3 + brick linear index       */
+  int *top_child_base;    /* [cap_top] first child index j               */
+  int *bot_key;           /* [cap_bot] b*Db^3 + voxel linear index       */
+  int *bot_parent;        /* [cap_bot] parent node id                    */
+  int *counts;            /* [2] {#top nodes, #bottom nodes}             */
+  const float *voxel_size;/* [B]                                         */
+  const float *vol_bbox;  /* [B,3,2] (min,max) per axis                  */
+} SgTree;
+
+/* 32-bit words per brick in SgTree.brick_mask: max(1, rate^3 / 32). */
+int sg_mask_words(int rate);
+
+const char *sg_status_string(int status);
+int sg_version(void);
+
+/* ---- fusion ------------------------------------------------------------ */
+
+/* Data-driven cubic box.  Replaces inverse_mat3x3 + obtain_origin_bbox +
+ * obtain_resized_bbox as run by fusion_cuda_integrate
+ * (c_lib/VoxelEncoding/src/fusion_kernel.cu:51-184, 683-708).
+ * depth [B,N,H,W], K/R [B,N,3,3], T [B,N,3]; writes vol_origin [B,3,2],
+ * vol_bbox [B,3,2], voxel_size [B]. */
+int sg_auto_bbox(const float *depth, const float *K, const float *R,
+                 const float *T, int B, int N, int H, int W, int vol_dim,
+                 float th_bbox, float *vol_origin, float *vol_bbox,
+                 float *voxel_size, sg_stream_t stream);
+
+/* TSDF / weight / packed-colour fusion with occupancy.  Replaces
+ * integrate_cuda (fusion_kernel.cu:236-340) and the three torch::full
+ * pre-fills of fusion_cuda_integrate (:668-670): tsdf/weight/color are
+ * written, not read.  occ [B,Dx,Dy,Dz] is written (local id or -1);
+ * count [B] is incremented by the number of occupied voxels. */
+int sg_fuse_tsdf(const float *K, const float *RT, const float *color,
+                 const float *depth, int B, int N, int H, int W, int Dx,
+                 int Dy, int Dz, const float *vol_bbox,
+                 const float *voxel_size, float obs_weight,
+                 float trunc_weight, float th_low, float th_high,
+                 float *tsdf, float *weight, float *colorv, int *occ,
+                 int *count, sg_stream_t stream);
+
+/* ---- two-level tree -------------------------------------------------------- */
+
+/* Coarse occupancy: a coarse voxel holds its local id if any of its rate^3
+ * fine children is > -1, else -1; count [B] is incremented.  Replaces
+ * merge_non_empty_nodes / build_multi_res_occupied_volumes
+ * (octree_kernel.cu:242-303, 367-411). */
+int sg_brick_occupancy(const int *occ_fine, int B, int Df, int rate,
+                       int *occ_coarse, int *count, sg_stream_t stream);
+
+/* Scratch bytes sg_tree_build needs for a B x Dt^3 top grid. */
+size_t sg_tree_scratch_bytes(int B, int Dt);
+
+/* Node tables: top bricks that are occupied and have an occupied
+ * 26-neighbour, in ascending brick order, and their occupied fine voxels in
+ * ascending lexicographic order.  Rewrites occ_top / occ_bot entries of the
+ * nodes to node ids in place.  Replaces MultiLayerOctree::build_octree ->
+ * gen_root_octree_nodes (octree_kernel.cu:101-239, 656-697), whose node ids
+ * come from atomicAdd queues; here they are deterministic. */
+int sg_tree_build(SgTree *tree, int *occ_top, int *occ_bot, void *scratch,
+                  size_t scratch_bytes, SgStatus *status, sg_stream_t stream);
+
+/* Node table [n_nodes, 6] = (centre x, y, z, edge, valid, frame) per node
+ * id.  Replaces MultiLayerOctree::output_all_nodes_tensor
+ * (octree_kernel.cu:309-328, 699-717). */
+int sg_tree_nodes(const SgTree *tree, int n_nodes, float *out,
+                  sg_stream_t stream);
+
+/* ---- ray / tree intersection ---------------------------------------- */
+
+/* Per-ray DDA over the top grid with child slab tests.  Replaces
+ * MultiLayerOctree::voxel_traversal -> ray_voxel_traversal
+ * (intersection_kernel.cu:36-71, 128-439, 828-895).
+ * ori/dir [B,N,3].  Rows of width W: hit_idx/hit_t0/hit_t1 [B,N,W].
+ * padded != 0: entries past each ray's hits are set to -1 (the reference's
+ * layout); padded == 0: entries past the hits are left untouched.
+ * valid_len [B,N] and hit_count [B,N] (nullable) are written.  Rays with
+ * more than W hits keep the first W and set SG_FLAG_HIT_OVERFLOW;
+ * status->max_hits receives the largest count. */
+int sg_intersect(const SgTree *tree, const float *ori, const float *dir,
+                 int N, int W, int th_early_stop, int opt_num,
+                 int is_training, int padded, int *hit_idx, float *hit_t0,
+                 float *hit_t1, float *valid_len, int *hit_count,
+                 SgStatus *status, sg_stream_t stream);
+
+/* ---- sampling ------------------------------------------------------------ */
+
+/* Adaptive coarse sampling over padded hit rows.  Replaces
+ * ray_voxels_points_sampling_coarse -> ray_voxels_sampling_uniform_kernel
+ * (sampling_kernel.cu:1070-1177, 1251-1304).  rands/sampled_* [B,N,S];
+ * entries without a sample are -1. */
+int sg_sample_coarse(const SgTree *tree, const int *hit_idx,
+                     const float *hit_t0, const float *hit_t1, int N, int W,
+                     const float *rands, const float *valid_len, int S,
+                     int num_levels, int start_level, int *sampled_idx,
+                     float *sampled_z, sg_stream_t stream);
+
+/* Per-row ascending sort of R rows of S floats (S <= 256); equal keys keep
+ * their input order.  Replaces sort_samplings (sampling_kernel.cu:
+ * 1308-1329, torch::sort along dim 2 + int cast). */
+int sg_sort_samples(const float *z, int R, int S, float *sorted, int *idx,
+                    sg_stream_t stream);
+
+/* ---- compositing ------------------------------------------------------------ */
+
+/* Front-to-back compositing of R rays x S samples, C feature channels.
+ * mode 0: alpha = 1 - exp(-sigma * delta) (volume_rendering_training_
+ * forward_kernel, volume_rendering.cu:17-126); mode 1: alpha = sigma
+ * (volume_rendering_occ_training_forward_kernel :129-240).  sort_idx NULL:
+ * samples are already in order (volume_rendering_occ_kernel :666-745).
+ * out_feat [R,C], out_depth/out_ws/out_alpha [R]. */
+int sg_composite_fwd(const float *z, const int *sort_idx, const float *sigma,
+                     const float *feats, int R, int S, int C, float t_thres,
+                     int mode, float *out_feat, float *out_depth,
+                     float *out_ws, float *out_alpha, sg_stream_t stream);
+
+/* Adjoint of sg_composite_fwd.  exact == 0 reproduces the reference
+ * gradient formula of volume_rendering_training_backward_kernel
+ * (volume_rendering.cu:244-381) and its occupancy variant (:384-522);
+ * exact == 1 is the true derivative of the forward (transmittance and
+ * prefix sums recomputed per ray; the saved outputs are not read).
+ * grad_feats [R,S,C], grad_sigma [R,S] are fully written. */
+int sg_composite_bwd(const float *g_feat, const float *g_depth,
+                     const float *g_ws, const float *g_alpha,
+                     const float *o_feat, const float *o_depth,
+                     const float *o_ws, const float *o_alpha, const float *z,
+                     const int *sort_idx, const float *sigma,
+                     const float *feats, int R, int S, int C, float t_thres,
+                     int mode, int exact, float *grad_feats,
+                     float *grad_sigma, sg_stream_t stream);
+
+/* ---- trilinear gathers ------------------------------------------------------ */
+
+/* Node-corner trilinear aggregation.  Replaces
+ * MultiLayerOctree::trilinear_aggregate_features(_backward)
+ * (sampling_kernel.cu:162-327, 1384-1462).  ori/dir [B,N,3],
+ * z/idx [B,N,S], feats [B,C,N,S,8] -> out [B,C,N,S];
+ * backward: gout [B,C,N,S] -> gin [B,C,N,S,8] (fully written). */
+int sg_trilerp_nodes_fwd(const SgTree *tree, const float *ori,
+                         const float *dir, const float *z, const int *idx,
+                         const float *feats, int N, int S, int C, float *out,
+                         sg_stream_t stream);
+int sg_trilerp_nodes_bwd(const SgTree *tree, const float *ori,
+                         const float *dir, const float *z, const int *idx,
+                         const float *gout, int N, int S, int C, float *gin,
+                         sg_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SAILOR_GB300_H */

@@ -1,0 +1,338 @@
+"""NumPy front end of the C oracle (test infrastructure only).
+
+Each method restates one reference operation of SAILOR's VoxelEncoding path
+(the C source cites the reference file:line it follows) on host arrays.
+Inputs are converted to contiguous float32/int32; outputs are new arrays.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+FLAG_TIE, FLAG_ALIAS, FLAG_OVERFLOW = 1, 2, 4
+
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_vp = C.c_void_p
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        L = C.CDLL(path)
+        i, f, l = C.c_int, C.c_float, C.c_long
+        L.orc_inverse3x3.argtypes = [_f32p, i, _f32p]
+        L.orc_origin_bbox.argtypes = [_f32p, _f32p, _f32p, _f32p, i, i, i, i, f, _f32p]
+        L.orc_resized_bbox.argtypes = [_f32p, i, i, _f32p, _f32p]
+        L.orc_integrate.argtypes = [i, i, i, i, i, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p,
+                                    f, f, f, f, _f32p, _f32p, _f32p, _i32p, _i32p]
+        L.orc_integrate.restype = l
+        L.orc_merge.argtypes = [i, i, i, _i32p, _i32p, _i32p]
+        L.orc_build_tree.argtypes = [i, i, i, _i32p, _i32p, i, i, i, i,
+                                     _i32p, _i32p, _i32p, _i32p, _i32p, _i32p]
+        L.orc_build_tree.restype = i
+        L.orc_voxel_traversal.argtypes = [i, i, _f32p, _f32p, i, i, _i32p, i, i, i, i,
+                                          _i32p, _i32p, _i32p, _i32p, _f32p, _f32p,
+                                          i, i, i, i, _i32p, _f32p, _f32p, _f32p, _i32p, _i32p]
+        L.orc_voxel_traversal.restype = i
+        L.orc_sample_coarse.argtypes = [i, i, i, i, _i32p, _f32p, _f32p, _f32p, _f32p,
+                                        i, i, i, i, i, i, _f32p, _i32p, _f32p, _i32p]
+        L.orc_sort.argtypes = [i, i, _f32p, _f32p, _i32p]
+        L.orc_composite_fwd.argtypes = [i, i, i, _f32p, _vp, _f32p, _f32p, f, i,
+                                        _f64p, _f64p, _f64p, _f64p, _vp]
+        L.orc_composite_bwd_ref.argtypes = [i, i, i] + [_f32p] * 8 + [_f32p, _i32p, _f32p, _f32p,
+                                                                      f, i, _f64p, _f64p]
+        L.orc_trilerp_nodes.argtypes = [l, i, _f32p, _f32p, _i32p, _vp, _vp, _vp, _vp]
+        L.orc_grid_gather.argtypes = [l, i, i, _f32p, _vp, _f32p, _f32p, _f32p, _f64p]
+        L.orc_grid_scatter.argtypes = [l, i, i, i, _f32p, _vp, _f32p, _f32p, _f32p, _f64p]
+        L.orc_node_geometry.argtypes = [f, i, _f32p, _i32p, _f32p, _f32p]
+        L.orc_num_threads.restype = i
+        L.orc_set_threads.argtypes = [i]
+        _lib = L
+    return _lib
+
+
+def _f(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _i(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def num_threads():
+    return lib().orc_num_threads()
+
+
+def set_threads(n):
+    lib().orc_set_threads(int(n))
+
+
+# --------------------------------------------------------------------------
+# fusion (fusion_kernel.cu)
+# --------------------------------------------------------------------------
+def inverse3x3(M):
+    M = _f(M)
+    out = np.zeros_like(M)
+    lib().orc_inverse3x3(M.reshape(-1), M.size // 9, out.reshape(-1))
+    return out
+
+
+def auto_bbox(depths, K, R, T, D, th_bbox):
+    """fusion_cuda_integrate's bbox steps (fusion_kernel.cu:655-708)."""
+    B, N, H, W = depths.shape
+    Kinv = inverse3x3(K)
+    Rinv = inverse3x3(R)
+    vol_origin = np.empty((B, 3, 2), np.float32)
+    vol_origin[..., 0] = 99999.0
+    vol_origin[..., 1] = -99999.0
+    lib().orc_origin_bbox(_f(depths).reshape(-1), Kinv.reshape(-1), Rinv.reshape(-1),
+                          _f(T).reshape(-1), B, N, H, W, float(th_bbox), vol_origin.reshape(-1))
+    vol_bbox = np.empty((B, 3, 2), np.float32)
+    voxel_size = np.empty((B, 1), np.float32)
+    lib().orc_resized_bbox(vol_origin.reshape(-1), B, D, vol_bbox.reshape(-1), voxel_size.reshape(-1))
+    return vol_origin, vol_bbox, voxel_size
+
+
+def integrate(K, RT, colors, depths, D, vol_bbox, voxel_size, obs_weight=1.0,
+              trunc_weight=3.0, th_low=13.5, th_high=13.5):
+    """integrate_cuda (fusion_kernel.cu:236-340) over a given box."""
+    B, N, H, W = depths.shape
+    n = B * D ** 3
+    tsdf = np.empty(n, np.float32)
+    weight = np.empty(n, np.float32)
+    color = np.empty(n, np.float32)
+    occ = np.empty(n, np.int32)
+    count = np.zeros(B, np.int32)
+    ties = lib().orc_integrate(B, N, H, W, D, _f(vol_bbox).reshape(-1), _f(voxel_size).reshape(-1),
+                               _f(K).reshape(-1), _f(RT).reshape(-1), _f(colors).reshape(-1),
+                               _f(depths).reshape(-1), float(obs_weight), float(trunc_weight),
+                               float(th_low), float(th_high), tsdf, weight, color, occ, count)
+    shp = (B, D, D, D)
+    return dict(tsdf=tsdf.reshape(shp), weight=weight.reshape(shp), color=color.reshape(shp),
+                occ=occ.reshape(shp), count=count.reshape(B, 1), ties=int(ties))
+
+
+# --------------------------------------------------------------------------
+# tree (octree_kernel.cu)
+# --------------------------------------------------------------------------
+def merge(occ_fine, rate):
+    B, Df = occ_fine.shape[0], occ_fine.shape[1]
+    Dc = Df // rate
+    coarse = np.empty((B, Dc, Dc, Dc), np.int32)
+    count = np.zeros(B, np.int32)
+    lib().orc_merge(B, Dc, rate, _i(occ_fine).reshape(-1), coarse.reshape(-1), count)
+    return coarse, count.reshape(B, 1)
+
+
+def build_tree(occ_top, occ_bot, base_top=None, base_bot=0, cap_top=None, cap_bot=None):
+    """gen_root_octree_nodes with sequential node order; rewrites copies."""
+    occ_top = _i(occ_top).copy()
+    occ_bot = _i(occ_bot).copy()
+    B, Dt, Db = occ_top.shape[0], occ_top.shape[1], occ_bot.shape[1]
+    n_top_occ = int((occ_top > -1).sum())
+    n_bot_occ = int((occ_bot > -1).sum())
+    if base_top is None:
+        base_top = n_bot_occ
+    cap_top = n_top_occ if cap_top is None else cap_top
+    cap_bot = n_bot_occ if cap_bot is None else cap_bot
+    top_key = np.full(max(cap_top, 1), -1, np.int32)
+    top_cb = np.zeros(max(cap_top, 1), np.int32)
+    top_nc = np.zeros(max(cap_top, 1), np.int32)
+    bot_key = np.full(max(cap_bot, 1), -1, np.int32)
+    bot_par = np.full(max(cap_bot, 1), -1, np.int32)
+    q = np.zeros(2, np.int32)
+    rc = lib().orc_build_tree(B, Dt, Db, occ_top.reshape(-1), occ_bot.reshape(-1), base_top, base_bot,
+                              cap_top, cap_bot, top_key, top_cb, top_nc, bot_key, bot_par, q)
+    if rc != 0:
+        raise RuntimeError("oracle tree build: capacity exceeded")
+    nt, nb = int(q[0]), int(q[1])
+    return dict(occ_top=occ_top, occ_bot=occ_bot, base_top=base_top, base_bot=base_bot,
+                ntop=nt, nbot=nb, top_key=top_key[:max(nt, 1)].copy(), top_child_base=top_cb[:max(nt, 1)].copy(),
+                top_nchild=top_nc[:max(nt, 1)].copy(), bot_key=bot_key[:max(nb, 1)].copy(),
+                bot_parent=bot_par[:max(nb, 1)].copy(), Dt=Dt, Db=Db, B=B)
+
+
+def node_geometry(vs, size, bbox_min3, idx3):
+    c = np.zeros(3, np.float32)
+    nvs = np.zeros(1, np.float32)
+    lib().orc_node_geometry(float(vs), int(size), _f(bbox_min3), _i(idx3), c, nvs)
+    return c, float(nvs[0])
+
+
+def node_keys(tree, gids):
+    """Canonical (level, b, x, y, z) per node id (level 1 = top brick)."""
+    gids = np.asarray(gids)
+    out = np.full(gids.shape + (5,), -1, np.int64)
+    Dt, Db = tree["Dt"], tree["Db"]
+    top = gids >= tree["base_top"]
+    k = gids[top] - tree["base_top"]
+    key = tree["top_key"][k].astype(np.int64)
+    vt = Dt ** 3
+    out[top, 0] = 1
+    out[top, 1] = key // vt
+    l = key % vt
+    out[top, 2], out[top, 3], out[top, 4] = l // (Dt * Dt), (l // Dt) % Dt, l % Dt
+    bot = (gids >= 0) & ~top
+    key = tree["bot_key"][gids[bot] - tree["base_bot"]].astype(np.int64)
+    vb = Db ** 3
+    out[bot, 0] = 0
+    out[bot, 1] = key // vb
+    l = key % vb
+    out[bot, 2], out[bot, 3], out[bot, 4] = l // (Db * Db), (l // Db) % Db, l % Db
+    return out
+
+
+# --------------------------------------------------------------------------
+# intersection (intersection_kernel.cu) and sampling (sampling_kernel.cu)
+# --------------------------------------------------------------------------
+def voxel_traversal(tree, ori, dirs, voxel_size, vol_bbox, W=1024, th_early_stop=-1,
+                    opt_num=-1, is_training=False):
+    B, N = ori.shape[0], ori.shape[1]
+    idx = np.full((B, N, W), -1, np.int32)
+    t0 = np.full((B, N, W), -1, np.float32)
+    t1 = np.full((B, N, W), -1, np.float32)
+    vlen = np.zeros((B, N), np.float32)
+    nhit = np.zeros((B, N), np.int32)
+    flags = np.zeros((B, N), np.int32)
+    mx = lib().orc_voxel_traversal(
+        B, N, _f(ori).reshape(-1), _f(dirs).reshape(-1), tree["Dt"], tree["Db"],
+        tree["occ_top"].reshape(-1), tree["base_top"], tree["base_bot"], tree["ntop"], tree["nbot"],
+        tree["top_key"], tree["top_child_base"], tree["top_nchild"], tree["bot_key"],
+        _f(voxel_size).reshape(-1), _f(vol_bbox).reshape(-1), W, th_early_stop, opt_num,
+        int(bool(is_training)), idx.reshape(-1), t0.reshape(-1), t1.reshape(-1), vlen.reshape(-1),
+        nhit.reshape(-1), flags.reshape(-1))
+    return dict(idx=idx, t0=t0, t1=t1, valid_len=vlen[..., None], nhit=nhit, flags=flags, max_hits=int(mx))
+
+
+def sample_coarse(tree, hits, rands, voxel_size, S, num_levels=2, start_level=0):
+    idx, t0, t1 = hits["idx"], hits["t0"], hits["t1"]
+    B, N, W = idx.shape
+    sidx = np.full((B, N, S), -1, np.int32)
+    sz = np.full((B, N, S), -1, np.float32)
+    flags = _i(hits["flags"]).copy()
+    lib().orc_sample_coarse(B, N, W, S, _i(idx).reshape(-1), _f(t0).reshape(-1), _f(t1).reshape(-1),
+                            _f(rands).reshape(-1), _f(hits["valid_len"]).reshape(-1),
+                            int(hits["max_hits"]), num_levels, start_level, tree["Dt"], tree["Db"],
+                            tree["base_top"], _f(voxel_size).reshape(-1), sidx.reshape(-1),
+                            sz.reshape(-1), flags.reshape(-1))
+    return sidx, sz, flags
+
+
+def sort(z):
+    z = _f(z)
+    S = z.shape[-1]
+    R = z.size // S
+    out = np.empty_like(z)
+    idx = np.empty(z.shape, np.int32)
+    lib().orc_sort(R, S, z.reshape(-1), out.reshape(-1), idx.reshape(-1))
+    return out, idx
+
+
+# --------------------------------------------------------------------------
+# compositing (volume_rendering.cu)
+# --------------------------------------------------------------------------
+def composite_fwd(z, sort_idx, sigma, feats, t_thres=1e-4, occ_mode=False):
+    z = _f(z)
+    S = z.shape[-1]
+    R = z.size // S
+    Cf = feats.shape[-1]
+    sig = _f(sigma).reshape(-1)
+    ft = _f(feats).reshape(-1)
+    sidx = None if sort_idx is None else _i(sort_idx)
+    of = np.zeros(R * Cf, np.float64)
+    od = np.zeros(R, np.float64)
+    ow = np.zeros(R, np.float64)
+    oa = np.zeros(R, np.float64)
+    flags = np.zeros(R, np.int32)
+    lib().orc_composite_fwd(R, S, Cf, z.reshape(-1), None if sidx is None else sidx.ctypes.data, sig, ft,
+                            float(t_thres), int(bool(occ_mode)), of, od, ow, oa, flags.ctypes.data)
+    lead = z.shape[:-1]
+    return (of.reshape(lead + (Cf,)), od.reshape(lead + (1,)), ow.reshape(lead + (1,)),
+            oa.reshape(lead + (1,)), flags.reshape(lead))
+
+
+def composite_bwd_ref(g_feat, g_depth, g_ws, g_alpha, o_feat, o_depth, o_ws, o_alpha,
+                      z, sort_idx, sigma, feats, t_thres=1e-4, occ_mode=False):
+    z = _f(z)
+    S = z.shape[-1]
+    R = z.size // S
+    Cf = feats.shape[-1]
+    gf = np.zeros(R * S * Cf, np.float64)
+    gs = np.zeros(R * S, np.float64)
+    lib().orc_composite_bwd_ref(R, S, Cf, *[_f(a).reshape(-1) for a in (g_feat, g_depth, g_ws, g_alpha,
+                                                                         o_feat, o_depth, o_ws, o_alpha)],
+                                z.reshape(-1), _i(sort_idx).reshape(-1), _f(sigma).reshape(-1),
+                                _f(feats).reshape(-1), float(t_thres), int(bool(occ_mode)), gf, gs)
+    lead = z.shape
+    return gf.reshape(lead + (Cf,)), gs.reshape(lead + (1,))
+
+
+# --------------------------------------------------------------------------
+# trilinear gathers (sampling_kernel.cu:162-327 and the dense-grid extension)
+# --------------------------------------------------------------------------
+def trilerp_nodes(pts, corners, valid, feats=None, gout=None):
+    """pts [M,3], corners [M,8,3], valid [M]; feats [C,M,8]; gout [C,M]."""
+    pts, corners, valid = _f(pts), _f(corners), _i(valid)
+    M = pts.shape[0]
+    Cf = (feats if feats is not None else gout).shape[0]
+    out = np.zeros((Cf, M), np.float64) if feats is not None else None
+    gin = np.zeros((Cf, M, 8), np.float64) if gout is not None else None
+    fe = _f(feats) if feats is not None else None
+    go = _f(gout) if gout is not None else None
+    lib().orc_trilerp_nodes(M, Cf, pts.reshape(-1), corners.reshape(-1), valid,
+                            None if fe is None else fe.ctypes.data, None if go is None else go.ctypes.data,
+                            None if out is None else out.ctypes.data, None if gin is None else gin.ctypes.data)
+    return out, gin
+
+
+def grid_gather(pts, grid, bbox_min, voxel_size, batch=None):
+    """pts [P,3]; grid [B,D,D,D,C]; bbox_min [B,3]; voxel_size [B]."""
+    pts, grid = _f(pts), _f(grid)
+    P, D, Cf = pts.shape[0], grid.shape[1], grid.shape[-1]
+    out = np.zeros((P, Cf), np.float64)
+    bt = None if batch is None else _i(batch)
+    lib().orc_grid_gather(P, Cf, D, pts.reshape(-1), None if bt is None else bt.ctypes.data,
+                          _f(bbox_min).reshape(-1), _f(voxel_size).reshape(-1), grid.reshape(-1), out)
+    return out
+
+
+def grid_scatter(pts, gout, B, D, bbox_min, voxel_size, batch=None):
+    pts, gout = _f(pts), _f(gout)
+    P, Cf = pts.shape[0], gout.shape[-1]
+    gg = np.zeros((B, D, D, D, Cf), np.float64)
+    bt = None if batch is None else _i(batch)
+    lib().orc_grid_scatter(P, Cf, D, B, pts.reshape(-1), None if bt is None else bt.ctypes.data,
+                           _f(bbox_min).reshape(-1), _f(voxel_size).reshape(-1), gout.reshape(-1),
+                           gg.reshape(-1))
+    return gg
+
+
+# --------------------------------------------------------------------------
+# whole chain, as SRONet's forward_build + forward_ray_intersect call it
+# --------------------------------------------------------------------------
+def chain(scene, D, rate, S, ori, dirs, rands, W=1024, obs_weight=1.0, trunc_weight=3.0,
+          th_low=13.5, th_high=13.5, th_bbox=0.025, explicit_box=True):
+    """Fusion -> merge -> tree -> traversal -> sampling -> sort, on host."""
+    K, RT, colors, depths = scene["K"], scene["RT"], scene["colors"], scene["depths"]
+    if explicit_box:
+        vol_bbox, voxel_size = scene["vol_bbox"], scene["voxel_size"]
+    else:
+        R = RT[..., :3]
+        T = RT[..., 3]
+        _, vol_bbox, voxel_size = auto_bbox(depths, K, R, T, D, th_bbox)
+    fz = integrate(K, RT, colors, depths, D, vol_bbox, voxel_size, obs_weight, trunc_weight, th_low, th_high)
+    top, cnt_top = merge(fz["occ"], rate)
+    tree = build_tree(top, fz["occ"])
+    hits = voxel_traversal(tree, ori, dirs, voxel_size, vol_bbox, W=W)
+    sidx, sz, flags = sample_coarse(tree, hits, rands, voxel_size, S)
+    sorted_z, sort_idx = sort(sz)
+    return dict(fusion=fz, top=top, cnt_top=cnt_top, tree=tree, hits=hits, sampled_idx=sidx,
+                sampled_z=sz, flags=flags, sorted_z=sorted_z, sort_idx=sort_idx,
+                vol_bbox=vol_bbox, voxel_size=voxel_size)

@@ -1,0 +1,84 @@
+"""ctypes binding of libsailor_gb300.so (the C ABI in include/sailor_gb300.h).
+
+The library is required: importing this module raises ImportError when the
+shared object is missing or lacks an entry point, so no operation of the
+package can run without the CUDA kernels.
+"""
+import ctypes as C
+import os
+
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsailor_gb300.so")
+
+SG_FLAG_HIT_OVERFLOW = 1
+SG_FLAG_TREE_CAPACITY = 2
+
+EXPORTS = (
+    "sg_mask_words", "sg_status_string", "sg_version", "sg_auto_bbox", "sg_fuse_tsdf",
+    "sg_brick_occupancy", "sg_tree_scratch_bytes", "sg_tree_build", "sg_tree_nodes", "sg_intersect",
+    "sg_sample_coarse", "sg_sort_samples", "sg_composite_fwd", "sg_composite_bwd",
+    "sg_trilerp_nodes_fwd", "sg_trilerp_nodes_bwd",
+)
+
+
+class SgTree(C.Structure):
+    _fields_ = [("B", C.c_int), ("Dt", C.c_int), ("Db", C.c_int), ("rate", C.c_int),
+                ("base_top", C.c_int), ("base_bot", C.c_int), ("cap_top", C.c_int), ("cap_bot", C.c_int),
+                ("brick_node", C.c_void_p), ("brick_mask", C.c_void_p), ("top_key", C.c_void_p),
+                ("top_child_base", C.c_void_p), ("bot_key", C.c_void_p), ("bot_parent", C.c_void_p),
+                ("counts", C.c_void_p), ("voxel_size", C.c_void_p), ("vol_bbox", C.c_void_p)]
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            f"{LIB_PATH} is missing: build it with `python -c \"import __graft_entry__ as g; g.build()\"` "
+            "(the package has no CPU implementation)")
+    lib = C.CDLL(LIB_PATH)
+    missing = [n for n in EXPORTS if not hasattr(lib, n)]
+    if missing:
+        raise ImportError(f"{LIB_PATH} lacks entry points: {missing}")
+    i, f, p, sz = C.c_int, C.c_float, C.c_void_p, C.c_size_t
+    lib.sg_status_string.restype = C.c_char_p
+    lib.sg_status_string.argtypes = [i]
+    lib.sg_mask_words.argtypes = [i]
+    lib.sg_auto_bbox.argtypes = [p, p, p, p, i, i, i, i, i, f, p, p, p, p]
+    lib.sg_fuse_tsdf.argtypes = [p, p, p, p, i, i, i, i, i, i, i, p, p, f, f, f, f, p, p, p, p, p, p]
+    lib.sg_brick_occupancy.argtypes = [p, i, i, i, p, p, p]
+    lib.sg_tree_scratch_bytes.argtypes = [i, i]
+    lib.sg_tree_scratch_bytes.restype = sz
+    lib.sg_tree_build.argtypes = [C.POINTER(SgTree), p, p, p, sz, p, p]
+    lib.sg_tree_nodes.argtypes = [C.POINTER(SgTree), i, p, p]
+    lib.sg_intersect.argtypes = [C.POINTER(SgTree), p, p, i, i, i, i, i, i, p, p, p, p, p, p, p]
+    lib.sg_sample_coarse.argtypes = [C.POINTER(SgTree), p, p, p, i, i, p, p, i, i, i, p, p, p]
+    lib.sg_sort_samples.argtypes = [p, i, i, p, p, p]
+    lib.sg_composite_fwd.argtypes = [p, p, p, p, i, i, i, f, i, p, p, p, p, p]
+    lib.sg_composite_bwd.argtypes = [p] * 12 + [i, i, i, f, i, i, p, p, p]
+    lib.sg_trilerp_nodes_fwd.argtypes = [C.POINTER(SgTree), p, p, p, p, p, i, i, i, p, p]
+    lib.sg_trilerp_nodes_bwd.argtypes = [C.POINTER(SgTree), p, p, p, p, p, i, i, i, p, p]
+    return lib
+
+
+lib = _load()
+
+
+def check(rc, what=""):
+    if rc != 0:
+        raise RuntimeError(f"sailor_gb300 {what}: {lib.sg_status_string(rc).decode()} (status {rc})")
+
+
+def ptr(t):
+    """Device address of a tensor (None -> NULL)."""
+    if t is None:
+        return None
+    return C.c_void_p(t.data_ptr())
+
+
+def stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def mask_words(rate):
+    return lib.sg_mask_words(int(rate))

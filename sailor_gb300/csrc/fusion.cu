@@ -1,0 +1,309 @@
+// fusion.cu -- data-driven bounding box and TSDF fusion on sm_103a.
+//
+// Replaces fusion_kernel.cu (SAILOR c_lib/VoxelEncoding/src):
+//   inverse_mat3x3 :105, obtain_origin_bbox :137, obtain_resized_bbox :51,
+//   integrate_cuda :236 and the host wrapper fusion_cuda_integrate :600.
+//
+// fuse_tsdf: one thread per 4 consecutive z voxels of one x-y row, one CTA
+// row of the grid per frame (blockIdx.y).  Cameras (K, [R|T] of every view)
+// sit in shared memory; tsdf/weight/colour live in registers across the view
+// loop and are stored once with 16-byte vector stores (the reference pre-
+// fills three full volumes with torch::full and then read-modify-writes them
+// once per view).  Occupancy counts are warp-aggregated before one atomic
+// per warp.  HBM traffic is the 16 bytes/voxel of the four outputs plus the
+// depth/colour images (L2-resident gathers).
+#include "common.cuh"
+
+namespace sg {
+
+constexpr int kMaxViews = 32;
+
+// ---------------------------------------------------------------------------
+// bounding box
+// ---------------------------------------------------------------------------
+__global__ void bbox_init_kernel(float *vol_origin, int B) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < B * 3) {
+    vol_origin[2 * i] = 99999.0f;       // fusion_kernel.cu:655
+    vol_origin[2 * i + 1] = -99999.0f;  // fusion_kernel.cu:656
+  }
+}
+
+// float atomics for min / max that are exact (order-independent results)
+__device__ __forceinline__ void atomic_min_f(float *a, float v) {
+  if (v >= 0.0f) atomicMin((int *)a, __float_as_int(v));
+  else atomicMax((unsigned *)a, __float_as_uint(v));
+}
+__device__ __forceinline__ void atomic_max_f(float *a, float v) {
+  if (v >= 0.0f) atomicMax((int *)a, __float_as_int(v));
+  else atomicMin((unsigned *)a, __float_as_uint(v));
+}
+
+// Grid: (pixel tiles, B).  Each CTA inverts K and R of its frame's views
+// into shared memory (the reference runs a separate inverse kernel), then
+// back-projects its pixels and reduces the six extrema before one atomic
+// each.
+__global__ void __launch_bounds__(256) origin_bbox_kernel(
+    const float *__restrict__ depth, const float *__restrict__ K, const float *__restrict__ R,
+    const float *__restrict__ T, int N, int H, int W, float thres, float *vol_origin) {
+  __shared__ float s_ki[kMaxViews][9], s_ri[kMaxViews][9], s_t[kMaxViews][3];
+  __shared__ float s_red[6][8];
+  int b = blockIdx.y;
+  for (int v = threadIdx.x; v < N; v += blockDim.x) {
+    inverse3x3(K + (size_t)(b * N + v) * 9, s_ki[v]);
+    inverse3x3(R + (size_t)(b * N + v) * 9, s_ri[v]);
+    for (int a = 0; a < 3; a++) s_t[v][a] = T[(size_t)(b * N + v) * 3 + a];
+  }
+  __syncthreads();
+  float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+  long npix = (long)N * H * W;
+  const float *dm = depth + (size_t)b * npix;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += (long)gridDim.x * blockDim.x) {
+    float d = __ldg(dm + i);
+    if (d < 0.1f || d > 5.0f) continue;
+    int v = (int)(i / ((long)H * W));
+    long p = i - (long)v * H * W;
+    int y = (int)(p / W), x = (int)(p - (long)y * W);
+    const float *ki = s_ki[v], *ri = s_ri[v];
+    float px = (float)x, py = (float)y;
+    float cx = (__fmaf_rn(ki[0], px, ki[1] * py) + ki[2]) * d;
+    float cy = (__fmaf_rn(ki[3], px, ki[4] * py) + ki[5]) * d;
+    float cz = (__fmaf_rn(ki[6], px, ki[7] * py) + ki[8]) * d;
+    cx -= s_t[v][0];
+    cy -= s_t[v][1];
+    cz -= s_t[v][2];
+    float q[3] = {dot3c(ri[0], ri[1], ri[2], cx, cy, cz), dot3c(ri[3], ri[4], ri[5], cx, cy, cz),
+                  dot3c(ri[6], ri[7], ri[8], cx, cy, cz)};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      mn[a] = fminf(mn[a], q[a] - thres);
+      mx[a] = fmaxf(mx[a], q[a] + thres);
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mn[a] = fminf(mn[a], __shfl_xor_sync(SG_FULL, mn[a], o));
+      mx[a] = fmaxf(mx[a], __shfl_xor_sync(SG_FULL, mx[a], o));
+    }
+  }
+  int w = threadIdx.x >> 5;
+  if (lane_id() == 0) {
+    for (int a = 0; a < 3; a++) {
+      s_red[2 * a][w] = mn[a];
+      s_red[2 * a + 1][w] = mx[a];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    int k = threadIdx.x;
+    int nw = blockDim.x >> 5;
+    float r = s_red[k][0];
+    for (int j = 1; j < nw; j++) r = (k & 1) ? fmaxf(r, s_red[k][j]) : fminf(r, s_red[k][j]);
+    if ((k & 1) == 0) {
+      if (r < 3.0e38f) atomic_min_f(&vol_origin[b * 6 + k], r);
+    } else {
+      if (r > -3.0e38f) atomic_max_f(&vol_origin[b * 6 + k], r);
+    }
+  }
+}
+
+// obtain_resized_bbox (fusion_kernel.cu:51-103)
+__global__ void resized_bbox_kernel(const float *vol_origin, int B, int D, float *vol_bbox,
+                                    float *voxel_size) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= B) return;
+  const float *o = vol_origin + 6 * i;
+  float x_min = o[0], x_max = o[1], y_min = o[2], y_max = o[3], z_min = o[4], z_max = o[5];
+  float x_len = x_max - x_min, y_len = y_max - y_min, z_len = z_max - z_min;
+  float max_len = fmaxf(x_len, fmaxf(y_len, z_len));
+  float xc = (x_min + x_max) / 2.0f, yc = (y_min + y_max) / 2.0f, zc = (z_min + z_max) / 2.0f;
+  voxel_size[i] = max_len / (float)(D - 1);
+  float h = max_len / 2.0f;
+  if (max_len == x_len) {
+    y_min = yc - h; y_max = yc + h; z_min = zc - h; z_max = zc + h;
+  } else if (max_len == y_len) {
+    x_min = xc - h; x_max = xc + h; z_min = zc - h; z_max = zc + h;
+  } else {
+    x_min = xc - h; x_max = xc + h; y_min = yc - h; y_max = yc + h;
+  }
+  float *bb = vol_bbox + 6 * i;
+  bb[0] = x_min; bb[1] = x_max; bb[2] = y_min; bb[3] = y_max; bb[4] = z_min; bb[5] = z_max;
+}
+
+// ---------------------------------------------------------------------------
+// TSDF fusion
+// ---------------------------------------------------------------------------
+struct FuseParams {
+  const float *K, *RT, *color, *depth, *vol_bbox, *voxel_size;
+  float *tsdf, *weight, *colorv;
+  int *occ, *count;
+  int N, H, W, Dx, Dy, Dz;
+  float obs_weight, trunc_weight, th_low, th_high;
+};
+
+// Integrate one view into the running state of one voxel (the body of the
+// view loop of integrate_cuda, fusion_kernel.cu:279-332).
+__device__ __forceinline__ void integrate_view(const float *__restrict__ Kk, const float *__restrict__ P,
+                                               float ax, float ay, float az, float pz,
+                                               const float *__restrict__ dimg,
+                                               const float *__restrict__ cimg, int H, int W,
+                                               float trunc, float obs, float &ts, float &w,
+                                               float &col) {
+  // cam = [R|T] p: fma(P2, pz, fma(P0, px, P1*py)) + P3 with the inner
+  // fma shared by the four voxels of the thread (ax/ay/az)
+  float cx = __fmaf_rn(P[2], pz, ax) + P[3];
+  float cy = __fmaf_rn(P[6], pz, ay) + P[7];
+  float cz = __fmaf_rn(P[10], pz, az) + P[11];
+  float ux = dot3c(Kk[0], Kk[1], Kk[2], cx, cy, cz);
+  float uy = dot3c(Kk[3], Kk[4], Kk[5], cx, cy, cz);
+  float uz = dot3c(Kk[6], Kk[7], Kk[8], cx, cy, cz);
+  ux = ux / uz;
+  uy = uy / uz;
+  int pxi = (int)roundf(ux), pyi = (int)roundf(uy);
+  if (pxi < 0 || pxi >= W || pyi < 0 || pyi >= H || cz < 0) return;
+  size_t pidx = (size_t)pyi * W + pxi;
+  float dv = __ldg(dimg + pidx);
+  if (dv < 0.1f || dv > 4.0f) return;
+  float diff = dv - cz;
+  if (diff < -trunc) return;
+  float dist = fminf(1.0f, diff / trunc);
+  float w_old = w, w_new = w_old + obs;
+  w = w_new;
+  // (tsdf*w_old + obs*dist)/w_new: nvcc fuses the second product
+  ts = __fmaf_rn(obs, dist, ts * w_old) / w_new;
+  // packed colour b*65536 + g*256 + r: integer-valued floats, exact steps
+  float old_b = floorf(col / 65536.0f);
+  float old_g = floorf((col - old_b * 256.0f * 256.0f) / 256.0f);
+  float old_r = col - old_b * 256.0f * 256.0f - old_g * 256.0f;
+  float nc = __ldg(cimg + pidx);
+  float nb = floorf(nc / 65536.0f);
+  float ng = floorf((nc - nb * 256.0f * 256.0f) / 256.0f);
+  float nr = nc - nb * 256.0f * 256.0f - ng * 256.0f;
+  nb = fminf(roundf(__fmaf_rn(old_b, w_old, obs * nb) / w_new), 255.0f);
+  ng = fminf(roundf(__fmaf_rn(old_g, w_old, obs * ng) / w_new), 255.0f);
+  nr = fminf(roundf(__fmaf_rn(old_r, w_old, obs * nr) / w_new), 255.0f);
+  col = nb * 256.0f * 256.0f + ng * 256.0f + nr;
+}
+
+template <int VPT>
+__global__ void __launch_bounds__(128) fuse_tsdf_kernel(FuseParams p) {
+  __shared__ float s_K[kMaxViews][9];
+  __shared__ float s_P[kMaxViews][12];
+  const int b = blockIdx.y;
+  for (int i = threadIdx.x; i < p.N * 21; i += blockDim.x) {
+    int v = i / 21, k = i - v * 21;
+    if (k < 9) s_K[v][k] = p.K[(size_t)(b * p.N + v) * 9 + k];
+    else s_P[v][k - 9] = p.RT[(size_t)(b * p.N + v) * 12 + (k - 9)];
+  }
+  __syncthreads();
+  const long vol = (long)p.Dx * p.Dy * p.Dz;
+  const long groups = vol / VPT;
+  const float vs = p.voxel_size[b];
+  const float trunc = vs * p.trunc_weight;
+  const float bx = p.vol_bbox[b * 6 + 0], by = p.vol_bbox[b * 6 + 2], bz = p.vol_bbox[b * 6 + 4];
+  const float hi_th = trunc * p.th_high, lo_th = -trunc * p.th_low;
+  const size_t img = (size_t)p.H * p.W;
+  int cnt = 0;
+  for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < groups; g += (long)gridDim.x * blockDim.x) {
+    long v0 = g * VPT;
+    int x = (int)(v0 / ((long)p.Dy * p.Dz));
+    long rem = v0 - (long)x * p.Dy * p.Dz;
+    int y = (int)(rem / p.Dz);
+    int z0 = (int)(rem - (long)y * p.Dz);
+    float px = __fmaf_rn((float)x, vs, bx);
+    float py = __fmaf_rn((float)y, vs, by);
+    float pz[VPT], ts[VPT], w[VPT], col[VPT];
+#pragma unroll
+    for (int j = 0; j < VPT; j++) {
+      pz[j] = __fmaf_rn((float)(z0 + j), vs, bz);
+      ts[j] = 1.0f;
+      w[j] = 0.0f;
+      col[j] = 0.0f;
+    }
+    for (int k = 0; k < p.N; k++) {
+      const float *P = s_P[k];
+      const float *Kk = s_K[k];
+      float ax = __fmaf_rn(P[0], px, P[1] * py);
+      float ay = __fmaf_rn(P[4], px, P[5] * py);
+      float az = __fmaf_rn(P[8], px, P[9] * py);
+      const float *dimg = p.depth + ((size_t)b * p.N + k) * img;
+      const float *cimg = p.color + ((size_t)b * p.N + k) * img;
+#pragma unroll
+      for (int j = 0; j < VPT; j++)
+        integrate_view(Kk, P, ax, ay, az, pz[j], dimg, cimg, p.H, p.W, trunc, p.obs_weight, ts[j],
+                       w[j], col[j]);
+    }
+    int oc[VPT];
+#pragma unroll
+    for (int j = 0; j < VPT; j++) {
+      bool o = ts[j] < hi_th && ts[j] > lo_th;
+      oc[j] = o ? (int)(v0 + j) : -1;
+      cnt += o;
+    }
+    size_t o = (size_t)b * vol + v0;
+    if (VPT == 4) {
+      *reinterpret_cast<float4 *>(p.tsdf + o) = make_float4(ts[0], ts[1], ts[2], ts[3]);
+      *reinterpret_cast<float4 *>(p.weight + o) = make_float4(w[0], w[1], w[2], w[3]);
+      *reinterpret_cast<float4 *>(p.colorv + o) = make_float4(col[0], col[1], col[2], col[3]);
+      *reinterpret_cast<int4 *>(p.occ + o) = make_int4(oc[0], oc[1], oc[2], oc[3]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < VPT; j++) {
+        p.tsdf[o + j] = ts[j];
+        p.weight[o + j] = w[j];
+        p.colorv[o + j] = col[j];
+        p.occ[o + j] = oc[j];
+      }
+    }
+  }
+  cnt = warp_sum(cnt);
+  if (lane_id() == 0 && cnt) atomicAdd(p.count + b, cnt);
+}
+
+}  // namespace sg
+
+using namespace sg;
+
+extern "C" int sg_auto_bbox(const float *depth, const float *K, const float *R, const float *T, int B,
+                            int N, int H, int W, int vol_dim, float th_bbox, float *vol_origin,
+                            float *vol_bbox, float *voxel_size, sg_stream_t stream) {
+  if (!depth || !K || !R || !T || !vol_origin || !vol_bbox || !voxel_size) return SG_ERR_INVALID_ARG;
+  if (B <= 0 || N <= 0 || N > kMaxViews || H <= 0 || W <= 0 || vol_dim < 2) return SG_ERR_INVALID_ARG;
+  bbox_init_kernel<<<ceil_div(B * 3, 128), 128, 0, stream>>>(vol_origin, B);
+  long npix = (long)N * H * W;
+  int gx = ceil_div(npix, 256 * 8);
+  if (gx > 4096) gx = 4096;
+  origin_bbox_kernel<<<dim3(gx, B), 256, 0, stream>>>(depth, K, R, T, N, H, W, th_bbox, vol_origin);
+  resized_bbox_kernel<<<ceil_div(B, 128), 128, 0, stream>>>(vol_origin, B, vol_dim, vol_bbox, voxel_size);
+  SG_LAUNCH_CHECK();
+  return SG_OK;
+}
+
+extern "C" int sg_fuse_tsdf(const float *K, const float *RT, const float *color, const float *depth, int B,
+                            int N, int H, int W, int Dx, int Dy, int Dz, const float *vol_bbox,
+                            const float *voxel_size, float obs_weight, float trunc_weight, float th_low,
+                            float th_high, float *tsdf, float *weight, float *colorv, int *occ,
+                            int *count, sg_stream_t stream) {
+  if (!K || !RT || !color || !depth || !vol_bbox || !voxel_size || !tsdf || !weight || !colorv || !occ ||
+      !count)
+    return SG_ERR_INVALID_ARG;
+  if (B <= 0 || N <= 0 || N > kMaxViews || H <= 0 || W <= 0 || Dx <= 0 || Dy <= 0 || Dz <= 0)
+    return SG_ERR_INVALID_ARG;
+  FuseParams p{K, RT, color, depth, vol_bbox, voxel_size, tsdf, weight, colorv, occ, count,
+               N, H, W, Dx, Dy, Dz, obs_weight, trunc_weight, th_low, th_high};
+  long vol = (long)Dx * Dy * Dz;
+  bool vec = (Dz % 4 == 0) && ((((uintptr_t)tsdf) | ((uintptr_t)weight) | ((uintptr_t)colorv) |
+                                 ((uintptr_t)occ)) % 16 == 0);
+  if (vec) {
+    long groups = vol / 4;
+    int gx = ceil_div(groups, 128);
+    fuse_tsdf_kernel<4><<<dim3(gx, B), 128, 0, stream>>>(p);
+  } else {
+    int gx = ceil_div(vol, 128);
+    fuse_tsdf_kernel<1><<<dim3(gx, B), 128, 0, stream>>>(p);
+  }
+  SG_LAUNCH_CHECK();
+  return SG_OK;
+}

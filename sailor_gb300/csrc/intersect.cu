@@ -1,0 +1,230 @@
+// intersect.cu -- ray / two-level tree intersection on sm_103a.
+//
+// Replaces intersection_kernel.cu (SAILOR c_lib/VoxelEncoding/src):
+//   RayVoxelIntersection :36-71, RayVoxelIntersectionNodeListNew :128-284,
+//   ray_voxel_traversal :286-439, MultiLayerOctree::voxel_traversal :828-895.
+//
+// One thread per ray walks the top grid with the reference's Amanatides-Woo
+// DDA (same float operations, so the same cells in the same order).  At a
+// kept brick the thread reads the brick's node index from the dense brick
+// map and iterates the set bits of the brick's fine-occupancy mask in
+// ascending order -- the reference's lexicographic children order -- slab-
+// testing each occupied child with geometry recomputed from its index (the
+// reference copies a ~1.1 KB node per test).  Hits are appended to the
+// ray's row; the reference's -1 padding of the row tail is written by a
+// second, warp-per-row kernel with coalesced 16-byte stores.
+//
+// Isolated occupied bricks (no occupied neighbour, hence not nodes) are
+// treated as empty.  The reference instead looks up node index == the
+// brick's local id there, i.e. an unrelated node.
+#include "common.cuh"
+
+namespace sg {
+
+struct IsectParams {
+  SgTree t;
+  const float *ori, *dir;
+  int N, W, th_early_stop, opt_num, is_training;
+  int *hit_idx;
+  float *hit_t0, *hit_t1, *valid_len;
+  int *hit_count;
+  SgStatus *st;
+};
+
+__global__ void __launch_bounds__(128) intersect_kernel(IsectParams p) {
+  const SgTree &t = p.t;
+  const long R = (long)t.B * p.N;
+  const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  int cnt = 0;
+  bool over = false;
+  if (r < R) {
+    const int b = (int)(r / p.N);
+    const float *bb = t.vol_bbox + 6 * b;
+    const float bmin[3] = {bb[0], bb[2], bb[4]};
+    const float xc = (bb[0] + bb[1]) / 2.0f, yc = (bb[2] + bb[3]) / 2.0f, zc = (bb[4] + bb[5]) / 2.0f;
+    const float vs = t.voxel_size[b];
+    const float vs_top = vs * (float)(t.Db / t.Dt);
+    const float bst[3] = {bb[0] - vs / 2.0f, bb[2] - vs / 2.0f, bb[4] - vs / 2.0f};
+    const float o[3] = {p.ori[r * 3 + 0], p.ori[r * 3 + 1], p.ori[r * 3 + 2]};
+    const float d[3] = {p.dir[r * 3 + 0], p.dir[r * 3 + 1], p.dir[r * 3 + 2]};
+    const float inv[3] = {__fdividef(1.0f, d[0]), __fdividef(1.0f, d[1]), __fdividef(1.0f, d[2])};
+    const LevelGeom gt = level_geom(vs, t.Db / t.Dt);
+    const LevelGeom gb = level_geom(vs, 1);
+    const int mw = sg_mask_words_dev(t.rate);
+    const int r2 = t.rate * t.rate;
+    const long vt = (long)t.Dt * t.Dt * t.Dt;
+    int *oi = p.hit_idx + (size_t)r * p.W;
+    float *o0 = p.hit_t0 + (size_t)r * p.W, *o1 = p.hit_t1 + (size_t)r * p.W;
+    float vlen = 0.0f;
+    float T0, T1;
+    if (slab(o, inv, xc, yc, zc, vs_top * (float)t.Dt, T0, T1) && !(T0 < 0.0f || T1 < 0.0f)) {
+      float so[3];
+      int st[3];
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        float sp = __fmaf_rn(T0, d[a], o[a]);
+        so[a] = sp - bst[a];
+        int s = (int)(so[a] / vs_top);
+        s = s < 0 ? 0 : s;
+        st[a] = s < t.Dt ? s : t.Dt - 1;
+      }
+      float step[3], tm[3], td[3];
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        step[a] = (d[a] >= 0) ? 1.0f : -1.0f;
+        float nb = (step[a] > 0) ? ((float)st[a] + step[a]) * vs_top : (float)st[a] * vs_top;
+        tm[a] = (d[a] != 0) ? (nb - so[a]) / d[a] : 9999999.0f;
+        td[a] = (d[a] != 0) ? vs_top / d[a] * step[a] : 9999999.0f;
+      }
+      const int J = 4 * t.Dt;
+      bool pre_empty = false, has_valid = false;
+      int nsucc = 0, nint = 0;
+      for (int j = 0; j < J; j++) {
+        int rid = -1;
+        long brick = (long)b * vt + ((long)st[0] * t.Dt + st[1]) * t.Dt + st[2];
+        int k = t.brick_node[brick];
+        if (k >= 0) {
+          float p0, p1;
+          if (slab(o, inv, node_coord(gt, bmin[0], st[0]), node_coord(gt, bmin[1], st[1]),
+                   node_coord(gt, bmin[2], st[2]), gt.vs, p0, p1) &&
+              !(p0 < 0.0f || p1 < 0.0f)) {
+            if (!p.is_training) {
+              const uint32_t *mask = t.brick_mask + (size_t)brick * mw;
+              const int cb = t.base_bot + t.top_child_base[k];
+              int rank = 0;
+              for (int w = 0; w < mw; w++) {
+                uint32_t bits = __ldg(mask + w);
+                while (bits) {
+                  int bit = __ffs(bits) - 1;
+                  bits &= bits - 1;
+                  int c = w * 32 + bit;
+                  int a = c / r2, c2 = (c / t.rate) % t.rate, e = c % t.rate;
+                  float c0, c1;
+                  if (slab(o, inv, node_coord(gb, bmin[0], st[0] * t.rate + a),
+                           node_coord(gb, bmin[1], st[1] * t.rate + c2),
+                           node_coord(gb, bmin[2], st[2] * t.rate + e), gb.vs, c0, c1) &&
+                      !(c0 < 0.0f || c1 < 0.0f)) {
+                    if (cnt < p.W) {
+                      oi[cnt] = cb + rank;
+                      o0[cnt] = c0;
+                      o1[cnt] = c1;
+                    } else {
+                      over = true;
+                    }
+                    vlen = vlen + (c1 - c0) * 4.0f;
+                    cnt++;
+                  }
+                  rank++;
+                }
+              }
+            }
+            if (cnt < p.W) {
+              oi[cnt] = t.base_top + k;
+              o0[cnt] = p0;
+              o1[cnt] = p1;
+            } else {
+              over = true;
+            }
+            vlen = vlen + (p1 - p0);
+            cnt++;
+            rid = cnt - 1;
+          }
+        }
+        if (p.th_early_stop > -1) {
+          if (rid == -1) {
+            if (pre_empty && has_valid) nsucc++;
+            pre_empty = true;
+          } else {
+            nsucc = 0;
+            pre_empty = false;
+            has_valid = true;
+          }
+          if ((nsucc + 1) >= p.th_early_stop) break;
+        }
+        if (p.opt_num > -1) {
+          if (rid + 1 > 0) nint++;
+          if (nint >= p.opt_num) break;
+        }
+        int ax;
+        if (tm[0] < tm[1]) ax = (tm[0] < tm[2]) ? 0 : 2;
+        else ax = (tm[1] < tm[2]) ? 1 : 2;
+        st[ax] = (int)((float)st[ax] + step[ax]);
+        tm[ax] += td[ax];
+        if (st[0] < 0 || st[0] >= t.Dt || st[1] < 0 || st[1] >= t.Dt || st[2] < 0 || st[2] >= t.Dt) break;
+      }
+    }
+    p.valid_len[r] = vlen;
+    if (p.hit_count) p.hit_count[r] = cnt;
+  }
+  // warp-aggregated status updates
+  int m = cnt;
+#pragma unroll
+  for (int o2 = 16; o2 > 0; o2 >>= 1) m = max(m, __shfl_xor_sync(SG_FULL, m, o2));
+  bool anyover = __any_sync(SG_FULL, over);
+  if (lane_id() == 0 && p.st) {
+    if (m > 0) atomicMax(&p.st->max_hits, m);
+    if (anyover) atomicOr(&p.st->flags, SG_FLAG_HIT_OVERFLOW);
+  }
+}
+
+// -1 padding of row tails [count, W): warp per row
+__global__ void pad_rows_kernel(long R, int W, const int *__restrict__ count, int *idx, float *t0,
+                                float *t1) {
+  const int lane = lane_id();
+  for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < R;
+       r += ((long)gridDim.x * blockDim.x) >> 5) {
+    int c = min(count[r], W);
+    size_t base = (size_t)r * W;
+    // scalar head up to a 4-element boundary, then 16-byte stores
+    int head = c;
+    while (head < W && ((base + head) & 3)) {
+      if (lane == 0) {
+        idx[base + head] = -1;
+        t0[base + head] = -1.0f;
+        t1[base + head] = -1.0f;
+      }
+      head++;
+    }
+    int nvec = (W - head) / 4;
+    int4 mi = make_int4(-1, -1, -1, -1);
+    float4 mf = make_float4(-1.f, -1.f, -1.f, -1.f);
+    for (int q = lane; q < nvec; q += 32) {
+      size_t o = base + head + 4 * q;
+      *reinterpret_cast<int4 *>(idx + o) = mi;
+      *reinterpret_cast<float4 *>(t0 + o) = mf;
+      *reinterpret_cast<float4 *>(t1 + o) = mf;
+    }
+    for (int q = head + 4 * nvec + lane; q < W; q += 32) {
+      idx[base + q] = -1;
+      t0[base + q] = -1.0f;
+      t1[base + q] = -1.0f;
+    }
+  }
+}
+
+}  // namespace sg
+
+using namespace sg;
+
+extern "C" int sg_intersect(const SgTree *tree, const float *ori, const float *dir, int N, int W,
+                            int th_early_stop, int opt_num, int is_training, int padded, int *hit_idx,
+                            float *hit_t0, float *hit_t1, float *valid_len, int *hit_count,
+                            SgStatus *status, sg_stream_t stream) {
+  if (!tree || !ori || !dir || !hit_idx || !hit_t0 || !hit_t1 || !valid_len) return SG_ERR_INVALID_ARG;
+  if (N <= 0 || W <= 0 || tree->B <= 0 || tree->Dt <= 0 || tree->Db != tree->Dt * tree->rate)
+    return SG_ERR_INVALID_ARG;
+  if (padded && !hit_count) return SG_ERR_INVALID_ARG;
+  if (padded && (((uintptr_t)hit_idx) | ((uintptr_t)hit_t0) | ((uintptr_t)hit_t1)) % 16 != 0)
+    return SG_ERR_INVALID_ARG;
+  IsectParams p{*tree, ori, dir, N, W, th_early_stop, opt_num, is_training,
+                hit_idx, hit_t0, hit_t1, valid_len, hit_count, status};
+  long R = (long)tree->B * N;
+  intersect_kernel<<<ceil_div(R, 128), 128, 0, stream>>>(p);
+  if (padded) {
+    int g = ceil_div(R * 32, 256);
+    if (g > 152 * 64) g = 152 * 64;
+    pad_rows_kernel<<<g, 256, 0, stream>>>(R, W, hit_count, hit_idx, hit_t0, hit_t1);
+  }
+  SG_LAUNCH_CHECK();
+  return SG_OK;
+}

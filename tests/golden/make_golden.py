@@ -1,0 +1,173 @@
+"""Generate golden vectors by running the reference's own CUDA kernels.
+
+Run on a GPU machine after ``oracle/build.py`` has compiled the reference
+cubins into ``oracle/_ref/`` (they are compiled from the SAILOR sources where
+they lie; this script only loads the cubins):
+
+    python tests/golden/make_golden.py --out <dir>
+
+It writes ``ref_chain_explicit.npz``, ``ref_chain_auto.npz`` and
+``ref_composite.npz``.  Each holds the seeded inputs
+and the reference outputs of fusion, coarse occupancy, the two-level tree
+(as canonical node keys, since the reference's node ids depend on atomic
+ordering), the voxel traversal, the coarse sampling, the sort, compositing
+forward/backward.  The reference's trilinear_aggregate_features kernels are
+not run: they step through their [B,C,N,S,8] input and gradient tensors
+with a per-sample stride of MAX_LEAVES = 64 (sampling_kernel.cu:210-213,
+272-275; octree.h:13) and so read and write past those tensors.  The committed
+copies under tests/golden/ pin the CPU oracle in the CPU test suite.
+"""
+import argparse
+import math
+import os
+import sys
+
+import numpy as np
+import torch
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import ref_cubin as rc  # noqa: E402
+from sailor_gb300 import synthetic as syn  # noqa: E402
+
+RES, D, RATE, VIEWS, PRIMS, TRES, S = 96, 64, 4, 4, 12, 48, 32
+
+
+def canonical(table, Dt, ids):
+    """node id -> (level, b, x, y, z); level 1 = top brick, -2 = not a node."""
+    ids = np.asarray(ids)
+    out = np.full(ids.shape + (5,), -1, np.int32)
+    m = ids >= 0
+    g = ids[m]
+    top_depth = int(round(math.log2(Dt)))
+    valid = table["valid"][g] == 1
+    lvl = np.where(table["depth"][g] == top_depth, 1, 0)
+    lvl = np.where(valid, lvl, -2)
+    out[m, 0] = lvl
+    out[m, 1] = table["batch"][g]
+    out[m, 2:] = table["xyz"][g]
+    return out
+
+
+def chain(scene, ori, dirs, rands_list, explicit, trunc_weight, th_bbox=0.025):
+    res = {}
+    f = rc.integrate(scene["K"], scene["RT"], scene["colors"], scene["depths"], D, 1.0, th_bbox,
+                     trunc_weight, 13.5, 13.5,
+                     vol_bbox=scene["vol_bbox"] if explicit else None,
+                     voxel_size=scene["voxel_size"] if explicit else None)
+    for k in ("tsdf", "weight", "color", "occ", "count", "vol_origin", "vol_bbox", "voxel_size"):
+        res["fusion_" + k] = f[k].cpu().numpy()
+    if not explicit:
+        res["Kinv"], res["Rinv"] = f["Kinv"].cpu().numpy(), f["Rinv"].cpu().numpy()
+    occ0, cnt0 = f["occ"], f["count"]
+    occ1, cnt1 = rc.build_multi_res_volumes(occ0, cnt0, RATE)
+    res["merge_occ"], res["merge_count"] = occ1.cpu().numpy(), cnt1.cpu().numpy()
+    tree = rc.Octree(occ0, occ1, cnt0, cnt1, f["voxel_size"], f["vol_bbox"], RATE)
+    table = tree.node_table()
+    res["tree_queue"] = tree.queue.cpu().numpy()
+    res["tree_totals"] = np.array(tree.totals, np.int32)
+    n = tree.n_nodes
+    res["tree_node_keys"] = canonical(table, tree.Dt, np.arange(n))
+    res["tree_node_children"] = canonical(table, tree.Dt, table["children"])  # [n,64,5]
+    res["tree_node_centre"] = table["centre"]
+    res["tree_node_vs"] = table["voxel_size"]
+    res["tree_node_valid"] = table["valid"].astype(np.int32)
+    res["tree_occ_top"] = occ1.cpu().numpy()
+    res["tree_occ_bot"] = occ0.cpu().numpy()
+    W = 4 * tree.Dt * (RATE ** 3 + 1)
+    idx, t0, t1, vl, q = tree.voxel_traversal(ori, dirs, W)
+    mh = tree.max_hits
+    res["trav_max_hits"] = np.array(mh, np.int32)
+    res["trav_count"] = q.cpu().numpy()[..., 0]
+    wk = max(mh, 1)
+    res["trav_keys"] = canonical(table, tree.Dt, idx[..., :wk].cpu().numpy())
+    res["trav_t0"] = t0[..., :wk].cpu().numpy()
+    res["trav_t1"] = t1[..., :wk].cpu().numpy()
+    res["trav_valid_len"] = vl.cpu().numpy()
+    for j, rands in enumerate(rands_list):
+        si, sd = tree.sample_coarse(idx, t0, t1, rands, vl, S)
+        res[f"samp{j}_keys"] = canonical(table, tree.Dt, si.cpu().numpy())
+        res[f"samp{j}_z"] = sd.cpu().numpy()
+        srt, sidx = rc.sort_samplings(sd)
+        res[f"samp{j}_sorted"] = srt.cpu().numpy()
+        res[f"samp{j}_sort_idx"] = sidx.cpu().numpy()
+        if j == 0:
+            res["_si"], res["_sd"] = si, sd
+    # training-mode traversal (parents only) and early-stop variants
+    idx2, t02, t12, vl2, q2 = tree.voxel_traversal(ori, dirs, W, is_training=True)
+    res["trav_train_keys"] = canonical(table, tree.Dt, idx2[..., :max(tree.max_hits, 1)].cpu().numpy())
+    res["trav_train_t0"] = t02[..., :max(tree.max_hits, 1)].cpu().numpy()
+    res["trav_train_valid_len"] = vl2.cpu().numpy()
+    idx3, _, _, _, q3 = tree.voxel_traversal(ori, dirs, W, th_early_stop=3, opt_num=6)
+    res["trav_stop_keys"] = canonical(table, tree.Dt, idx3[..., :max(tree.max_hits, 1)].cpu().numpy())
+    res["trav_stop_count"] = q3.cpu().numpy()[..., 0]
+    return res, tree
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", required=True)
+    args = ap.parse_args()
+    os.makedirs(args.out, exist_ok=True)
+    assert rc.available(), "reference cubins or GPU missing"
+    scene = syn.make_scene(seed=11, n_views=VIEWS, res=RES, n_prims=PRIMS, D=D, trunc=0.03)
+    ori, dirs = syn.target_rays(seed=11, res=TRES)
+    rng = np.random.default_rng(5)
+    rands = [np.full((1, ori.shape[1], S), 0.5, np.float32),
+             rng.random((1, ori.shape[1], S), dtype=np.float32)]
+    inputs = dict(K=scene["K"], RT=scene["RT"], depths=scene["depths"], colors=scene["colors"],
+                  vol_bbox=scene["vol_bbox"], voxel_size=scene["voxel_size"], ori=ori, dirs=dirs,
+                  rands0=rands[0], rands1=rands[1])
+    meta = dict(D=D, rate=RATE, S=S, res=RES, trunc_weight=scene["trunc_weight"])
+    for name, explicit, tw in (("explicit", True, scene["trunc_weight"]), ("auto", False, 3.0)):
+        res, tree = chain(scene, ori, dirs, rands, explicit, tw)
+        res.pop("_si"), res.pop("_sd")
+        out = dict(inputs)
+        out.update(res)
+        out.update({"meta_" + k: np.array(v) for k, v in meta.items()})
+        out["meta_trunc_weight"] = np.array(tw, np.float32)
+        np.savez_compressed(os.path.join(args.out, f"ref_chain_{name}.npz"), **out)
+        print(name, "max_hits", res["trav_max_hits"], "nodes", res["tree_queue"], flush=True)
+
+    # compositing: random sorted/unsorted samples with -1 padding
+    R, Sc = 2048, 48
+    z = rng.uniform(1.5, 3.5, (1, R, Sc)).astype(np.float32)
+    npad = rng.integers(0, Sc, R)
+    npad[:64] = Sc  # fully invalid rays
+    npad[64:128] = 0
+    for r in range(R):
+        z[0, r, Sc - npad[r]:] = -1.0
+    sigma = rng.gamma(0.8, 20.0, (1, R, Sc, 1)).astype(np.float32)
+    occv = (1.0 / (1.0 + np.exp(-rng.normal(0, 3, (1, R, Sc, 1))))).astype(np.float32)
+    feats = rng.random((1, R, Sc, 3), dtype=np.float32)
+    zt = rc._dev(z, torch.float32)
+    srt, sidx = rc.sort_samplings(zt)
+    g = [rc._dev(rng.normal(size=s).astype(np.float32), torch.float32)
+         for s in ((1, R, 3), (1, R, 1), (1, R, 1), (1, R, 1))]
+    comp = dict(z=z, sigma=sigma, occ=occv, feats=feats, sort_idx=sidx.cpu().numpy(),
+                sorted_z=srt.cpu().numpy(), g_feat=g[0].cpu().numpy(), g_depth=g[1].cpu().numpy(),
+                g_ws=g[2].cpu().numpy(), g_alpha=g[3].cpu().numpy())
+    for occ in (False, True):
+        tag = "occ" if occ else "den"
+        sg = rc._dev(occv if occ else sigma, torch.float32)
+        ft = rc._dev(feats, torch.float32)
+        outs = rc.volume_rendering_forward(zt, sidx, sg, ft, 1e-4, occ)
+        gf, gs = rc.volume_rendering_backward(g, outs, zt, sidx, sg, ft, 1e-4, occ)
+        for k, v in zip(("feat", "depth", "ws", "alpha"), outs):
+            comp[f"{tag}_fwd_{k}"] = v.cpu().numpy()
+        comp[f"{tag}_bwd_feat"], comp[f"{tag}_bwd_sigma"] = gf.cpu().numpy(), gs.cpu().numpy()
+    # pre-sorted occupancy rendering on the sorted depths
+    occ_sorted = np.take_along_axis(occv[..., 0], sidx.cpu().numpy().astype(np.int64), 2)[..., None]
+    feats_sorted = np.take_along_axis(feats, sidx.cpu().numpy().astype(np.int64)[..., None], 2)
+    outs = rc.volume_rendering_occ_forward(srt, rc._dev(occ_sorted, torch.float32),
+                                           rc._dev(feats_sorted, torch.float32), 1e-4)
+    comp["presorted_occ"], comp["presorted_feats"] = occ_sorted, feats_sorted
+    for k, v in zip(("feat", "depth", "ws", "alpha"), outs):
+        comp[f"presorted_fwd_{k}"] = v.cpu().numpy()
+    np.savez_compressed(os.path.join(args.out, "ref_composite.npz"), **comp)
+    print("done", flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,75 @@
+"""CPU checks of the C ABI boundary: the library loads and exports every
+function include/sailor_gb300.h declares; host-side argument validation
+raises before any kernel launch.  No compute call is made without a GPU."""
+import ctypes as C
+import os
+import re
+
+import pytest
+import torch
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _header_functions():
+    src = open(os.path.join(ROOT, "include", "sailor_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(sg_[a-z0-9_]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from sailor_gb300 import build
+    path = build.build_library()
+    return C.CDLL(path)
+
+
+def test_header_symbols_exported(lib):
+    names = _header_functions()
+    assert len(names) >= 15
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_binding_covers_header():
+    from sailor_gb300 import _native as N
+    assert set(_header_functions()) <= set(N.EXPORTS)
+
+
+def test_status_strings_and_constants(lib):
+    lib.sg_status_string.restype = C.c_char_p
+    for code in range(5):
+        assert lib.sg_status_string(code)
+    assert lib.sg_status_string(0) == b"ok"
+    assert lib.sg_mask_words(2) == 1 and lib.sg_mask_words(4) == 2 and lib.sg_mask_words(8) == 16
+    lib.sg_tree_scratch_bytes.restype = C.c_size_t
+    assert lib.sg_tree_scratch_bytes(1, 32) >= 2 * 4 * 32 ** 3
+
+
+def test_null_arguments_rejected(lib):
+    """Entry points validate pointers and sizes before launching."""
+    from sailor_gb300 import _native as N
+    L = N.lib
+    assert L.sg_fuse_tsdf(*([None] * 4), 1, 1, 8, 8, 8, 8, 8, None, None, 1.0, 3.0, 13.5, 13.5,
+                          *([None] * 5), None) == 1
+    assert L.sg_sort_samples(None, 1, 8, None, None, None) == 1
+    assert L.sg_composite_fwd(None, None, None, None, 1, 8, 3, 1e-4, 0, None, None, None, None, None) == 1
+    assert L.sg_brick_occupancy(None, 1, 8, 4, None, None, None) == 1
+
+
+def test_cpu_tensors_rejected():
+    from sailor_gb300.dist import VoxelEncoding as VE
+    z = torch.zeros(1, 4, 8)
+    with pytest.raises(RuntimeError, match="cuda"):
+        VE.volume_rendering_occ_forward(z, torch.zeros(1, 4, 8, 1), torch.zeros(1, 4, 8, 3), 0, 1e-4)
+    with pytest.raises(RuntimeError, match="cuda"):
+        VE.build_multi_res_volumes([torch.zeros(1, 8, 8, 8, dtype=torch.int32)], [torch.zeros(1, 1)], 2, 4, 0)
+
+
+def test_unsupported_tree_levels():
+    from sailor_gb300.dist import VoxelEncoding as VE
+    o = VE.MultiLayerOctree(3, 1, 2, 0)
+    with pytest.raises(RuntimeError, match="two-level"):
+        o.init_octree([None] * 3, [0, 0, 0], [None] * 3, [0, 0, 0], None, None)
+    with pytest.raises(NotImplementedError):
+        o.octree_traversal()
