@@ -155,6 +155,20 @@ int sg_sample_coarse(const SgTree *tree, const int *hit_idx,
                      int num_levels, int start_level, int *sampled_idx,
                      float *sampled_z, sg_stream_t stream);
 
+/* Fused sampling + per-ray sort (no reference counterpart as one call: it
+ * is ray_voxels_points_sampling_coarse followed by sort_samplings,
+ * sampling_kernel.cu:1251-1329, producing only the sorted outputs).
+ * hit_count NULL: rows are -1 terminated; else the first hit_count[r]
+ * entries of row r are its hits.  rands NULL: all jitters = rand_const.
+ * sorted_z / sorted_idx [B,N,S] (S <= 128): sample depths ascending (-1
+ * padding first) and the node id of each. */
+int sg_sample_sorted(const SgTree *tree, const int *hit_idx,
+                     const float *hit_t0, const float *hit_t1,
+                     const int *hit_count, int N, int W, const float *rands,
+                     float rand_const, const float *valid_len, int S,
+                     int num_levels, int start_level, float *sorted_z,
+                     int *sorted_idx, sg_stream_t stream);
+
 /* Per-row ascending sort of R rows of S floats (S <= 256); equal keys keep
  * their input order.  Replaces sort_samplings (sampling_kernel.cu:
  * 1308-1329, torch::sort along dim 2 + int cast). */
@@ -190,6 +204,17 @@ int sg_composite_bwd(const float *g_feat, const float *g_depth,
                      float *grad_sigma, sg_stream_t stream);
 
 /* ---- trilinear gathers ------------------------------------------------------ */
+
+/* Dense-grid trilinear gather at sample points (no reference counterpart:
+ * the dense-grid extension of trilinear_aggregate_features,
+ * sampling_kernel.cu:162-234).  Point of sample (b, n, s) = ori[b,n] +
+ * z[b,n,s] * dir[b,n]; grid [B,D,D,D,C] channel-last over each frame's
+ * vol_bbox / voxel_size; out [B,N,S,C] (0 where z < 0).  mode 1 (C == 1):
+ * out = sigmoid(-g * scale / s) / s, a density from a normalised TSDF. */
+int sg_grid_gather(const float *ori, const float *dir, const float *z, int B,
+                   int N, int S, const float *grid, int D, int C,
+                   const float *vol_bbox, const float *voxel_size, int mode,
+                   float scale, float s, float *out, sg_stream_t stream);
 
 /* Node-corner trilinear aggregation.  Replaces
  * MultiLayerOctree::trilinear_aggregate_features(_backward)

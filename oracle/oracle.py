@@ -33,6 +33,9 @@ def lib():
         L.orc_integrate.argtypes = [i, i, i, i, i, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p,
                                     f, f, f, f, _f32p, _f32p, _f32p, _i32p, _i32p]
         L.orc_integrate.restype = l
+        L.orc_integrate_slab.argtypes = [i, i, i, i, i, i, i, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p,
+                                         f, f, f, f, _f32p, _f32p, _f32p, _i32p, _i32p]
+        L.orc_integrate_slab.restype = l
         L.orc_merge.argtypes = [i, i, i, _i32p, _i32p, _i32p]
         L.orc_build_tree.argtypes = [i, i, i, _i32p, _i32p, i, i, i, i,
                                      _i32p, _i32p, _i32p, _i32p, _i32p, _i32p]
@@ -117,6 +120,24 @@ def integrate(K, RT, colors, depths, D, vol_bbox, voxel_size, obs_weight=1.0,
     shp = (B, D, D, D)
     return dict(tsdf=tsdf.reshape(shp), weight=weight.reshape(shp), color=color.reshape(shp),
                 occ=occ.reshape(shp), count=count.reshape(B, 1), ties=int(ties))
+
+
+def integrate_slab(K, RT, colors, depths, D, vol_bbox, voxel_size, x_begin, x_end, obs_weight=1.0,
+                   trunc_weight=3.0, th_low=13.5, th_high=13.5):
+    """integrate over the x-slab [x_begin, x_end) only (outputs sized for the slab)."""
+    B, N, H, W = depths.shape
+    n = B * D ** 3
+    tsdf = np.empty(n, np.float32)
+    weight = np.empty(n, np.float32)
+    color = np.empty(n, np.float32)
+    occ = np.empty(n, np.int32)
+    count = np.zeros(B, np.int32)
+    lib().orc_integrate_slab(B, N, H, W, D, int(x_begin), int(x_end), _f(vol_bbox).reshape(-1),
+                             _f(voxel_size).reshape(-1), _f(K).reshape(-1), _f(RT).reshape(-1),
+                             _f(colors).reshape(-1), _f(depths).reshape(-1), float(obs_weight),
+                             float(trunc_weight), float(th_low), float(th_high), tsdf, weight, color, occ, count)
+    shp = (B, D, D, D)
+    return dict(tsdf=tsdf.reshape(shp), occ=occ.reshape(shp), count=count)
 
 
 # --------------------------------------------------------------------------

@@ -173,12 +173,15 @@ void orc_resized_bbox(const float *vol_origin, int B, int D, float *vol_bbox,
 /* Voxel order x-major, z fastest (:265-268).  tsdf/weight/colour start at    */
 /* 1/0/0 (:668-670).  Returns the number of pixel-rounding near-ties seen.    */
 /* ------------------------------------------------------------------------ */
-long orc_integrate(int B, int N, int H, int W, int D, const float *vol_bbox,
-                   const float *voxel_size, const float *K, const float *RT,
-                   const float *color_im, const float *depth_im,
-                   float obs_weight, float trunc_weight, float th_low,
-                   float th_high, float *tsdf, float *weight, float *colorv,
-                   int *occ, int *count) {
+/* x-slab [x_begin, x_end) of the grid (the whole grid: 0, D); used to time
+ * a bounded sample of the fusion on the host */
+long orc_integrate_slab(int B, int N, int H, int W, int D, int x_begin, int x_end,
+                        const float *vol_bbox, const float *voxel_size,
+                        const float *K, const float *RT, const float *color_im,
+                        const float *depth_im, float obs_weight,
+                        float trunc_weight, float th_low, float th_high,
+                        float *tsdf, float *weight, float *colorv, int *occ,
+                        int *count) {
   long ties = 0;
   size_t vol = (size_t)D * D * D;
   for (int b = 0; b < B; b++) {
@@ -186,8 +189,9 @@ long orc_integrate(int B, int N, int H, int W, int D, const float *vol_bbox,
     float vs = voxel_size[b];
     float trunc = vs * trunc_weight;
     float bx = vol_bbox[b * 6 + 0], by = vol_bbox[b * 6 + 2], bz = vol_bbox[b * 6 + 4];
+    long v_begin = (long)x_begin * D * D, v_end = (long)x_end * D * D;
 #pragma omp parallel for reduction(+ : cnt, ties) schedule(static)
-    for (long v = 0; v < (long)vol; v++) {
+    for (long v = v_begin; v < v_end; v++) {
       int x = (int)(v / ((long)D * D));
       int y = (int)((v - (long)x * D * D) / D);
       int z = (int)(v - (long)x * D * D - (long)y * D);
@@ -248,6 +252,17 @@ long orc_integrate(int B, int N, int H, int W, int D, const float *vol_bbox,
     count[b] = (int)cnt;
   }
   return ties;
+}
+
+long orc_integrate(int B, int N, int H, int W, int D, const float *vol_bbox,
+                   const float *voxel_size, const float *K, const float *RT,
+                   const float *color_im, const float *depth_im,
+                   float obs_weight, float trunc_weight, float th_low,
+                   float th_high, float *tsdf, float *weight, float *colorv,
+                   int *occ, int *count) {
+  return orc_integrate_slab(B, N, H, W, D, 0, D, vol_bbox, voxel_size, K, RT,
+                            color_im, depth_im, obs_weight, trunc_weight, th_low,
+                            th_high, tsdf, weight, colorv, occ, count);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -594,10 +609,17 @@ void orc_sample_coarse(int B, int N, int W, int S, const int *hit_idx,
       float nvs = (id >= base_top) ? voxel_size[b] * (float)(Db / Dt) : voxel_size[b];
       float rate = start_vs / nvs;
       float q = (mx - mn) * rate * (float)S / vl;
-      /* within ~16 ulp of an integer boundary of the (int) cast; exact  */
-      /* integers come from exact cancellation (one hit: q == S) and are  */
-      /* reproduced by any implementation with the same operation order  */
-      if (q >= 0.5f && q != roundf(q) && fabsf(q - roundf(q)) <= 2e-6f * fabsf(q)) flags[r] |= FLAG_TIE;
+      /* q near an integer boundary of the (int) cast, within the error that */
+      /* a few-ulp difference in t0/t1 (the GPU's approximate reciprocal)   */
+      /* induces: |dq|/q <= 2*et/len + nh*2*et*4/vl, et = 8 ulp of t1.       */
+      /* Exact integers come from exact cancellation (one hit: q == S) and  */
+      /* are reproduced by any implementation with the same operation order */
+      {
+        float et = 8.0f * ldexpf(fabsf(mx), -23);
+        float rel = 2.0f * et / fmaxf(mx - mn, 1e-30f) + (float)(i + 1) * 8.0f * et / fmaxf(vl, 1e-30f);
+        if (q >= 0.5f && q != roundf(q) && fabsf(q - roundf(q)) <= rel * fabsf(q) + 1e-6f * fabsf(q))
+          flags[r] |= FLAG_TIE;
+      }
       int n = (int)q;
       n = n >= 1 ? n : 1;
       int left = S - has;

@@ -19,7 +19,7 @@ EXPORTS = (
     "sg_mask_words", "sg_status_string", "sg_version", "sg_auto_bbox", "sg_fuse_tsdf",
     "sg_brick_occupancy", "sg_tree_scratch_bytes", "sg_tree_build", "sg_tree_nodes", "sg_intersect",
     "sg_sample_coarse", "sg_sort_samples", "sg_composite_fwd", "sg_composite_bwd",
-    "sg_trilerp_nodes_fwd", "sg_trilerp_nodes_bwd",
+    "sg_trilerp_nodes_fwd", "sg_trilerp_nodes_bwd", "sg_sample_sorted", "sg_grid_gather",
 )
 
 
@@ -56,6 +56,8 @@ def _load():
     lib.sg_sort_samples.argtypes = [p, i, i, p, p, p]
     lib.sg_composite_fwd.argtypes = [p, p, p, p, i, i, i, f, i, p, p, p, p, p]
     lib.sg_composite_bwd.argtypes = [p] * 12 + [i, i, i, f, i, i, p, p, p]
+    lib.sg_sample_sorted.argtypes = [C.POINTER(SgTree), p, p, p, p, i, i, p, f, p, i, i, i, p, p, p]
+    lib.sg_grid_gather.argtypes = [p, p, p, i, i, i, p, i, i, p, p, i, f, f, p, p]
     lib.sg_trilerp_nodes_fwd.argtypes = [C.POINTER(SgTree), p, p, p, p, p, i, i, i, p, p]
     lib.sg_trilerp_nodes_bwd.argtypes = [C.POINTER(SgTree), p, p, p, p, p, i, i, i, p, p]
     return lib

@@ -188,9 +188,141 @@ __global__ void __launch_bounds__(256) sort_rows_kernel(const float *__restrict_
   }
 }
 
+// ---------------------------------------------------------------------------
+// fused sampling + per-ray sort (pipeline path)
+// ---------------------------------------------------------------------------
+// Same per-ray sampling as sample_coarse_kernel, but the samples of a ray go
+// to shared memory, are sorted there by (depth, position) with the register
+// bitonic network, and only the sorted depths and node ids are written: one
+// coalesced 8-byte-per-sample write instead of the reference's two
+// write-then-sort passes.  Hit rows may be compact (hit_count given: the
+// first hit_count[r] entries are the hits) or -1 terminated (hit_count
+// NULL).  rands NULL: every jitter is rand_const (the inference setting).
+template <int E>
+__global__ void __launch_bounds__(256) sample_sorted_kernel(SampleParams p, const int *__restrict__ hit_count,
+                                                            float rand_const, float *out_z, int *out_idx) {
+  __shared__ float s_z[8][32 * E];
+  __shared__ int s_i[8][32 * E];
+  const int lane = lane_id();
+  const int w8 = threadIdx.x >> 5;
+  const long R = (long)p.t.B * p.N;
+  const int S = p.S;
+  for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < R;
+       r += ((long)gridDim.x * blockDim.x) >> 5) {
+    const int b = (int)(r / p.N);
+    const int *hi = p.hit_idx + (size_t)r * p.W;
+    const float *h0 = p.hit_t0 + (size_t)r * p.W, *h1 = p.hit_t1 + (size_t)r * p.W;
+    const float *rd = p.rands ? p.rands + (size_t)r * S : nullptr;
+    const int nh = hit_count ? min(hit_count[r], p.W) : p.W;
+    float *sz = s_z[w8];
+    int *si = s_i[w8];
+    int done = 0;
+    if (nh > 0 && __ldg(hi) >= 0) {
+      const float vl = p.valid_len[r];
+      const float vs = p.t.voxel_size[b];
+      const float start_vs = vs * ldexpf(1.0f, 2 * (p.num_levels - p.start_level - 1));
+      const float vs_top = vs * (float)(p.t.Db / p.t.Dt);
+      int has = 0, nvalid = 0;
+      bool stop = false;
+      for (int c0 = 0; c0 < nh && !stop; c0 += 32) {
+        int i = c0 + lane;
+        int id = -1;
+        float mn = -1.0f, mx = -1.0f;
+        if (i < nh) {
+          id = __ldg(hi + i);
+          mn = __ldg(h0 + i);
+          mx = __ldg(h1 + i);
+        }
+        bool ok = i < nh && !(id < 0 || mn < 0 || mx < 0);
+        unsigned bad = __ballot_sync(SG_FULL, !ok);
+        int first_bad = bad ? __ffs(bad) - 1 : 32;
+        ok = ok && lane < first_bad;
+        if (bad) stop = true;
+        int n = 0;
+        if (ok) {
+          float nvs = (id >= p.t.base_top) ? vs_top : vs;
+          float rate = start_vs / nvs;
+          n = (int)((mx - mn) * rate * (float)S / vl);
+          n = n >= 1 ? n : 1;
+          n = n < S ? n : S;
+        }
+        int incl = warp_incl_scan(n);
+        int start = has + incl - n;
+        int ne = S - start;
+        ne = ne < 0 ? 0 : (ne < n ? ne : n);
+        if (ne > 0) {
+          float off = (mx - mn) / (float)(ne + 1);
+          for (int j = 0; j < ne; j++) {
+            int q = start + j;
+            sz[q] = sample_z(mn, off, j, rd ? __ldg(rd + q) : rand_const);
+            si[q] = id;
+          }
+        }
+        int tot = __shfl_sync(SG_FULL, incl, 31);
+        has = min(has + tot, S);
+        nvalid += __popc(__ballot_sync(SG_FULL, ok));
+      }
+      int left = S - has;
+      int cnt = left < nvalid ? left : nvalid;
+      for (int i = lane; i < cnt; i += 32) {
+        int id = __ldg(hi + i);
+        float mn = __ldg(h0 + i), mx = __ldg(h1 + i);
+        float off = (mx - mn) * 0.5f;
+        float base = mn + off;
+        int q = has + i;
+        sz[q] = sum3_rn(base, -(off * 0.5f), off * (rd ? __ldg(rd + q) : rand_const));
+        si[q] = id;
+      }
+      done = has + cnt;
+    }
+    for (int q = done + lane; q < S; q += 32) {
+      sz[q] = -1.0f;
+      si[q] = -1;
+    }
+    __syncwarp();
+    unsigned long long key[E];
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      int i = e * 32 + lane;
+      key[e] = (i < S) ? (((unsigned long long)ordered_bits(sz[i]) << 32) | (unsigned)i) : ~0ull;
+    }
+    bitonic_warp<E>(key);
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      int i = e * 32 + lane;
+      if (i < S) {
+        int pos = (int)(key[e] & 0xffffffffu);
+        out_z[(size_t)r * S + i] = from_ordered((uint32_t)(key[e] >> 32));
+        out_idx[(size_t)r * S + i] = si[pos];
+      }
+    }
+    __syncwarp();
+  }
+}
+
 }  // namespace sg
 
 using namespace sg;
+
+extern "C" int sg_sample_sorted(const SgTree *tree, const int *hit_idx, const float *hit_t0,
+                                const float *hit_t1, const int *hit_count, int N, int W, const float *rands,
+                                float rand_const, const float *valid_len, int S, int num_levels,
+                                int start_level, float *sorted_z, int *sorted_idx, sg_stream_t stream) {
+  if (!tree || !hit_idx || !hit_t0 || !hit_t1 || !valid_len || !sorted_z || !sorted_idx)
+    return SG_ERR_INVALID_ARG;
+  if (N <= 0 || W <= 0 || S <= 0 || tree->B <= 0) return SG_ERR_INVALID_ARG;
+  SampleParams p{*tree, hit_idx, hit_t0, hit_t1, rands, valid_len, N, W, S, num_levels, start_level,
+                 nullptr, nullptr};
+  long R = (long)tree->B * N;
+  int g = ceil_div(R * 32, 256);
+  if (g > 152 * 64) g = 152 * 64;
+  if (S <= 32) sample_sorted_kernel<1><<<g, 256, 0, stream>>>(p, hit_count, rand_const, sorted_z, sorted_idx);
+  else if (S <= 64) sample_sorted_kernel<2><<<g, 256, 0, stream>>>(p, hit_count, rand_const, sorted_z, sorted_idx);
+  else if (S <= 128) sample_sorted_kernel<4><<<g, 256, 0, stream>>>(p, hit_count, rand_const, sorted_z, sorted_idx);
+  else return SG_ERR_UNSUPPORTED;
+  SG_LAUNCH_CHECK();
+  return SG_OK;
+}
 
 extern "C" int sg_sample_coarse(const SgTree *tree, const int *hit_idx, const float *hit_t0,
                                 const float *hit_t1, int N, int W, const float *rands,
