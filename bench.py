@@ -41,6 +41,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="small configuration (256^3, 512^2) for profiling")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--unfused", action="store_true",
+                    help="render with four kernels (sample+sort, two field gathers, composite) instead of one")
     return ap.parse_args()
 
 
@@ -66,6 +69,10 @@ def algorithmic_bytes(cfg, n_hits, n_rays, S, n_pix):
         fusion=16 * V + 8 * n_pix,                      # 4 output volumes + depth/colour images
         tree=4 * V + 4 * Vt,                            # fine occupancy read + coarse write
         intersect=24 * n_rays + 12 * n_hits + 8 * n_rays,
+        # fused render: hit rows + per-ray count/valid length + ray ori/dir in,
+        # 24 B/ray out (field-grid taps are cache-resident and not counted)
+        render=12 * n_hits + 8 * n_rays + 24 * n_rays + 24 * n_rays,
+        # unfused render stages
         sample=12 * n_hits + 8 * n_rays + 8 * n_rays * S,
         gather=2 * 4 * n_rays * S + 4 * n_rays * S + 12 * n_rays * S,
         composite=20 * n_rays * S + 24 * n_rays,
@@ -228,10 +235,19 @@ def main():
     trunc_m = float(sc["voxel_size"][0, 0]) * sc["trunc_weight"]
     pipe = FramePipeline(1, cfg["D"], cfg["rate"], n_rays, cfg["S"], W_hits=1024, device=dev)
 
+    fused = not args.unfused
+
     def step():
         pipe.build(K, RT, col, dep, bb, vs, sc["trunc_weight"])
-        return pipe.render(o, d, cg, cbb, cvs, trunc_m)
+        return pipe.render(o, d, cg, cbb, cvs, trunc_m, fused=fused)
 
+    tuned = None
+    if not args.no_autotune:
+        from sailor_gb300 import autotune
+        step()
+        tuned = autotune.tune_pipeline(
+            pipe, lambda: pipe.build(K, RT, col, dep, bb, vs, sc["trunc_weight"]),
+            lambda: pipe.render(o, d, cg, cbb, cvs, trunc_m, fused=fused), cache=False, verbose=True)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -286,7 +302,7 @@ def main():
         for k in host:
             dev_in[k].copy_(host[k], non_blocking=True)
         pipe.build(dev_in["K"], dev_in["RT"], dev_in["col"], dev_in["dep"], bb, vs, sc["trunc_weight"])
-        rgb, dep_, ws, al = pipe.render(dev_in["o"], dev_in["d"], cg, cbb, cvs, trunc_m)
+        rgb, dep_, ws, al = pipe.render(dev_in["o"], dev_in["d"], cg, cbb, cvs, trunc_m, fused=fused)
         img = torch.cat([rgb.view(-1, 3), dep_.view(-1, 1), ws.view(-1, 1), al.view(-1, 1)], 1)
         out_host.copy_(img, non_blocking=True)
 
@@ -326,16 +342,16 @@ def main():
                                  "1024^2 target, S=96" if not args.small else
                         "small: 4x512^2 views, 256^3 TSDF, 8^3 bricks, 512^2 target, S=64",
                         frames_per_rank=1, rays_per_step=n_rays, l2="per-step working set > 10 GB >> L2",
-                        parallelism=f"replicas x{world}"),
+                        parallelism=f"replicas x{world}", fused_render=fused, launch_shapes=tuned),
             stages_ms=stages, tsdf_gvox_s=vox / (stages.get("fusion", float("nan")) / 1000.0) / 1e9,
-            render_rays_s=n_rays / (sum(stages.get(k, 0) for k in ("intersect", "sample", "gather", "composite"))
-                                    / 1000.0),
+            render_rays_s=n_rays / (sum(stages.get(k, 0) for k in ("intersect", "render", "sample", "gather",
+                                                                    "composite")) / 1000.0),
             hits_per_ray=n_hits / n_rays,
             roofline=dict(bound="hbm", kernel=dom, achieved=achieved, peak=pk["hbm_gbs"], unit="GB/s",
                           frac=achieved / pk["hbm_gbs"], traffic=traffic, peak_kind=pk_kind,
                           algorithmic_bytes=ab[dom]),
             e2e=dict(value=e2e_value, unit=UNIT, h2d_bytes_per_step=h2d, d2h_bytes_per_step=d2h),
-            gpu_launches=12 * args.steps,
+            gpu_launches=(9 if fused else 12) * args.steps,
             clocks=clk.summary(),
         )
         if not args.no_cpu_baseline and world >= 1:

@@ -74,6 +74,21 @@ int sg_mask_words(int rate);
 const char *sg_status_string(int status);
 int sg_version(void);
 
+/* Launch-shape knobs read by the kernels' host wrappers (process-wide).
+ * Values are validated; sg_tune_set returns SG_ERR_INVALID_ARG for a value
+ * a knob does not accept.  Set by the autotuner (sailor_gb300/autotune.py);
+ * no reference counterpart (the reference sizes every launch with
+ * cudaOccupancyMaxPotentialBlockSize). */
+enum {
+  SG_TUNE_FUSE_VPT = 0,      /* voxels per thread in sg_fuse_tsdf: 1, 2, 4 */
+  SG_TUNE_FUSE_BLOCK = 1,    /* threads per CTA in sg_fuse_tsdf: 32..256   */
+  SG_TUNE_ISECT_BLOCK = 2,   /* threads per CTA in sg_intersect: 32..512   */
+  SG_TUNE_RENDER_WARPS = 3,  /* CTAs per SM (x152) in warp-per-ray kernels */
+  SG_TUNE_COUNT = 4
+};
+int sg_tune_set(int knob, int value);
+int sg_tune_get(int knob);
+
 /* ---- fusion ------------------------------------------------------------ */
 
 /* Data-driven cubic box.  Replaces inverse_mat3x3 + obtain_origin_bbox +
@@ -229,6 +244,30 @@ int sg_trilerp_nodes_bwd(const SgTree *tree, const float *ori,
                          const float *dir, const float *z, const int *idx,
                          const float *gout, int N, int S, int C, float *gin,
                          sg_stream_t stream);
+
+/* ---- fused render ------------------------------------------------------------ */
+
+/* One pass per ray: coarse sampling over the hit row (compact: hit_count
+ * given; or -1 terminated), per-ray sort, density from the normalised TSDF
+ * grid tsdf [B,D,D,D] (sigma = sigmoid(-t * sdf_scale / sdf_s) / sdf_s),
+ * colour from color_grid [B,Dc,Dc,Dc,3] over color_bbox / color_vs, and
+ * density compositing (t_thres early termination) into out_rgb [B,N,3],
+ * out_depth/out_ws/out_alpha [B,N].  out_z/out_node [B,N,S] (both NULL or
+ * both set) receive the sorted samples.  No reference counterpart as one
+ * call: it is ray_voxels_points_sampling_coarse + sort_samplings
+ * (sampling_kernel.cu:1251-1329) + the field queries + 
+ * volume_rendering_training_forward (volume_rendering.cu:17-126). */
+int sg_render_fused(const SgTree *tree, const int *hit_idx,
+                    const float *hit_t0, const float *hit_t1,
+                    const int *hit_count, int N, int W, const float *rands,
+                    float rand_const, const float *valid_len, int S,
+                    int num_levels, int start_level, const float *ori,
+                    const float *dir, const float *tsdf, int D,
+                    float sdf_scale, float sdf_s, const float *color_grid,
+                    int Dc, const float *color_bbox, const float *color_vs,
+                    float t_thres, float *out_rgb, float *out_depth,
+                    float *out_ws, float *out_alpha, float *out_z,
+                    int *out_node, sg_stream_t stream);
 
 #ifdef __cplusplus
 }

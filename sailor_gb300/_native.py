@@ -20,6 +20,7 @@ EXPORTS = (
     "sg_brick_occupancy", "sg_tree_scratch_bytes", "sg_tree_build", "sg_tree_nodes", "sg_intersect",
     "sg_sample_coarse", "sg_sort_samples", "sg_composite_fwd", "sg_composite_bwd",
     "sg_trilerp_nodes_fwd", "sg_trilerp_nodes_bwd", "sg_sample_sorted", "sg_grid_gather",
+    "sg_render_fused", "sg_tune_set", "sg_tune_get",
 )
 
 
@@ -58,6 +59,10 @@ def _load():
     lib.sg_composite_bwd.argtypes = [p] * 12 + [i, i, i, f, i, i, p, p, p]
     lib.sg_sample_sorted.argtypes = [C.POINTER(SgTree), p, p, p, p, i, i, p, f, p, i, i, i, p, p, p]
     lib.sg_grid_gather.argtypes = [p, p, p, i, i, i, p, i, i, p, p, i, f, f, p, p]
+    lib.sg_render_fused.argtypes = [C.POINTER(SgTree), p, p, p, p, i, i, p, f, p, i, i, i, p, p, p, i, f, f, p, i,
+                                    p, p, f, p, p, p, p, p, p, p]
+    lib.sg_tune_set.argtypes = [i, i]
+    lib.sg_tune_get.argtypes = [i]
     lib.sg_trilerp_nodes_fwd.argtypes = [C.POINTER(SgTree), p, p, p, p, p, i, i, i, p, p]
     lib.sg_trilerp_nodes_bwd.argtypes = [C.POINTER(SgTree), p, p, p, p, p, i, i, i, p, p]
     return lib

@@ -13,3 +13,35 @@ extern "C" const char *sg_status_string(int status) {
 }
 
 extern "C" int sg_version(void) { return 100; }
+
+// ---------------------------------------------------------------------------
+// launch-shape knobs
+// ---------------------------------------------------------------------------
+namespace sg {
+static int g_tune[SG_TUNE_COUNT] = {4, 128, 64, 64};
+
+int tune(int knob) { return (knob >= 0 && knob < SG_TUNE_COUNT) ? g_tune[knob] : 0; }
+}  // namespace sg
+
+extern "C" int sg_tune_set(int knob, int value) {
+  switch (knob) {
+    case SG_TUNE_FUSE_VPT:
+      if (value != 1 && value != 2 && value != 4) return SG_ERR_INVALID_ARG;
+      break;
+    case SG_TUNE_FUSE_BLOCK:
+      if (value < 32 || value > 256 || value % 32) return SG_ERR_INVALID_ARG;
+      break;
+    case SG_TUNE_ISECT_BLOCK:
+      if (value < 32 || value > 512 || value % 32) return SG_ERR_INVALID_ARG;
+      break;
+    case SG_TUNE_RENDER_WARPS:
+      if (value < 1 || value > 64) return SG_ERR_INVALID_ARG;
+      break;
+    default:
+      return SG_ERR_INVALID_ARG;
+  }
+  sg::g_tune[knob] = value;
+  return SG_OK;
+}
+
+extern "C" int sg_tune_get(int knob) { return sg::tune(knob); }

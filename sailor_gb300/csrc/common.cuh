@@ -184,6 +184,9 @@ __device__ __forceinline__ void status_or(SgStatus *st, int f) {
   if (st) atomicOr(&st->flags, f);
 }
 
+// launch-shape knobs (sg_tune_set / sg_tune_get, capi.cu)
+int tune(int knob);
+
 }  // namespace sg
 
 // launch-error check used by every entry point

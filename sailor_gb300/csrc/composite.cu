@@ -21,7 +21,7 @@
 // reference's gradient formula; exact == 1 is the true derivative of the
 // forward (the reference adds g_ws*(1-ws) four extra times and drops the
 // sample that triggers early termination).
-#include "common.cuh"
+#include "ray_core.cuh"
 
 namespace sg {
 
@@ -54,7 +54,7 @@ struct RayState {
 };
 
 template <int E>
-__device__ __forceinline__ bool load_ray(const CompParams &p, long r, float *s_z, RayState<E> &st) {
+__device__ __forceinline__ bool load_ray(const CompParams &p, long r, float *s_z, float *s_f, RayState<E> &st) {
   const int lane = lane_id();
   const size_t rb = (size_t)r * p.S;
   const int S = p.S;
@@ -78,79 +78,18 @@ __device__ __forceinline__ bool load_ray(const CompParams &p, long r, float *s_z
     s_z[i] = st.z[e];
   }
   __syncwarp();
-  // alpha per position
-  if (p.mode == 0) {
-    unsigned gtz[E];
-#pragma unroll
-    for (int e = 0; e < E; e++) gtz[e] = __ballot_sync(SG_FULL, st.z[e] > 0.0f);
-#pragma unroll
-    for (int e = 0; e < E; e++) {
-      int i = e * 32 + lane;
-      st.al[e] = 0.0f;
-      if ((st.valid >> e) & 1u) {
-        float delta;
-        if (i == S - 1) {
-          delta = 1e10f;
-        } else {
-          // next position with z > 0, else the last position (:87-94)
-          int m = S - 1;
-          unsigned above = (lane == 31) ? 0u : (gtz[e] & (~0u << (lane + 1)));
-          if (above) {
-            m = e * 32 + __ffs(above) - 1;
-          } else {
-#pragma unroll
-            for (int e2 = 0; e2 < E; e2++)
-              if (e2 > e && gtz[e2] && m == S - 1) {
-                int mm = e2 * 32 + __ffs(gtz[e2]) - 1;
-                m = mm;
-                break;
-              }
-          }
-          delta = s_z[m] - st.z[e];
-        }
-        st.al[e] = 1.0f - __expf(-st.sg[e] * delta);
-      }
-    }
-  } else {
-#pragma unroll
-    for (int e = 0; e < E; e++) st.al[e] = ((st.valid >> e) & 1u) ? st.sg[e] : 0.0f;
-  }
-  // transmittance, strictly sequential over positions
-  float T = 1.0f;
-  bool stopped = false;
-  st.proc = 0;
-  st.post = 0;
-#pragma unroll
-  for (int e = 0; e < E; e++) {
-    st.tb[e] = 0.0f;
-    unsigned vmask = __ballot_sync(SG_FULL, (st.valid >> e) & 1u);
-    float f = ((st.valid >> e) & 1u) ? (1.0f - st.al[e]) : 1.0f;
-    if (!stopped) {
-      for (int l = 0; l < 32; l++) {
-        float fl = __shfl_sync(SG_FULL, f, l);
-        if (lane == l) {
-          st.tb[e] = T;
-          st.proc |= 1u << e;
-        }
-        if ((vmask >> l) & 1u) {
-          T = T * fl;
-          if (T < p.t_thres) {
-            stopped = true;
-            break;
-          }
-        }
-        if (lane == l) st.post |= 1u << e;
-      }
-    }
-  }
+  ray_alpha<E>(st.z, st.sg, st.valid, S, p.mode, s_z, st.al);
+  ray_transmittance<E>(st.al, st.valid, S, p.t_thres, s_f, st.tb, st.proc, st.post);
   return true;
 }
 
 template <int E, int CT>
 __global__ void __launch_bounds__(256) composite_fwd_kernel(CompParams p) {
   __shared__ float s_zall[8][32 * E];
+  __shared__ __align__(16) float s_fall[8][32 * E];
   const int lane = lane_id();
   float *s_z = s_zall[threadIdx.x >> 5];
+  float *s_f = s_fall[threadIdx.x >> 5];
   const int C = CT > 0 ? CT : p.C;
   for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < p.R;
        r += ((long)gridDim.x * blockDim.x) >> 5) {
@@ -159,7 +98,7 @@ __global__ void __launch_bounds__(256) composite_fwd_kernel(CompParams p) {
 #pragma unroll
     for (int c = 0; c < (CT > 0 ? CT : kMaxC); c++) acc[c] = 0.0f;
     float d = 0.0f, ws = 0.0f, aa = 0.0f;
-    bool ok = load_ray<E>(p, r, s_z, st);
+    bool ok = load_ray<E>(p, r, s_z, s_f, st);
     if (ok) {
       const size_t rb = (size_t)r * p.S;
 #pragma unroll
@@ -201,14 +140,16 @@ __global__ void __launch_bounds__(256) composite_fwd_kernel(CompParams p) {
 template <int E, int CT>
 __global__ void __launch_bounds__(256) composite_bwd_kernel(CompParams p) {
   __shared__ float s_zall[8][32 * E];
+  __shared__ __align__(16) float s_fall[8][32 * E];
   const int lane = lane_id();
   float *s_z = s_zall[threadIdx.x >> 5];
+  float *s_f = s_fall[threadIdx.x >> 5];
   constexpr int CM = CT > 0 ? CT : kMaxC;
   const int C = CT > 0 ? CT : p.C;
   for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < p.R;
        r += ((long)gridDim.x * blockDim.x) >> 5) {
     RayState<E> st;
-    bool ok = load_ray<E>(p, r, s_z, st);
+    bool ok = load_ray<E>(p, r, s_z, s_f, st);
     const size_t rb = (size_t)r * p.S;
     if (!ok) {
       // invalid ray: no gradient (the reference leaves its zero fill)

@@ -17,7 +17,7 @@
 // sigma = sigmoid(-t * scale / s) / s  (scale = truncation margin in metres,
 // s = the density's length scale), so the gather is fused with the field
 // transform that feeds compositing.
-#include "common.cuh"
+#include "ray_core.cuh"
 
 namespace sg {
 
@@ -33,51 +33,27 @@ struct GatherParams {
   float *out;
 };
 
-template <int CT>
+template <int C>
 __global__ void __launch_bounds__(256) grid_gather_kernel(GatherParams p) {
   const long n = p.R * p.S;
-  const int C = CT > 0 ? CT : p.C;
   for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
     const long r = k / p.S;
     const int b = (int)(r / p.N);
     const float zz = __ldg(p.z + k);
-    float acc[CT > 0 ? CT : 16];
+    float acc[C];
 #pragma unroll
-    for (int c = 0; c < (CT > 0 ? CT : 16); c++) acc[c] = 0.0f;
+    for (int c = 0; c < C; c++) acc[c] = 0.0f;
     if (zz >= 0.0f) {
       const float *bb = p.vol_bbox + 6 * b;
-      const float vs = __ldg(p.voxel_size + b);
-      float u[3];
-      int i0[3];
-      float f[3];
+      const float bmin[3] = {bb[0], bb[2], bb[4]};
+      float pt[3];
 #pragma unroll
-      for (int a = 0; a < 3; a++) {
-        float pa = __fmaf_rn(__ldg(p.dir + r * 3 + a), zz, __ldg(p.ori + r * 3 + a));
-        u[a] = (pa - bb[2 * a]) / vs;
-        float fl = floorf(u[a]);
-        i0[a] = (int)fl;
-        f[a] = u[a] - fl;
-      }
-      const size_t base = (size_t)b * p.D * p.D * p.D;
-#pragma unroll
-      for (int cr = 0; cr < 8; cr++) {
-        const int dx = (cr >> 2) & 1, dy = (cr >> 1) & 1, dz = cr & 1;
-        const int ix = i0[0] + dx, iy = i0[1] + dy, iz = i0[2] + dz;
-        if (ix < 0 || iy < 0 || iz < 0 || ix >= p.D || iy >= p.D || iz >= p.D) continue;
-        const float w = (dx ? f[0] : 1.0f - f[0]) * (dy ? f[1] : 1.0f - f[1]) * (dz ? f[2] : 1.0f - f[2]);
-        const float *g = p.grid + (base + ((size_t)ix * p.D + iy) * p.D + iz) * C;
-#pragma unroll
-        for (int c = 0; c < (CT > 0 ? CT : 16); c++)
-          if (c < C) acc[c] = __fmaf_rn(w, __ldg(g + c), acc[c]);
-      }
-      if (p.mode == 1) {
-        float v = acc[0] * p.scale / p.s;
-        acc[0] = (1.0f / (1.0f + __expf(v))) / p.s;  // sigmoid(-v) / s
-      }
+      for (int a = 0; a < 3; a++) pt[a] = __fmaf_rn(__ldg(p.dir + r * 3 + a), zz, __ldg(p.ori + r * 3 + a));
+      grid_tap<C>(p.grid + (size_t)b * p.D * p.D * p.D * C, p.D, bmin, __ldg(p.voxel_size + b), pt, acc);
+      if (p.mode == 1) acc[0] = tsdf_density(acc[0], p.scale, p.s);
     }
 #pragma unroll
-    for (int c = 0; c < (CT > 0 ? CT : 16); c++)
-      if (c < C) p.out[k * C + c] = acc[c];
+    for (int c = 0; c < C; c++) p.out[k * C + c] = acc[c];
   }
 }
 
@@ -95,9 +71,14 @@ extern "C" int sg_grid_gather(const float *ori, const float *dir, const float *z
   long n = (long)B * N * S;
   int g = ceil_div(n, 256);
   if (g > 152 * 64) g = 152 * 64;
-  if (C == 1) grid_gather_kernel<1><<<g, 256, 0, stream>>>(p);
-  else if (C == 3) grid_gather_kernel<3><<<g, 256, 0, stream>>>(p);
-  else grid_gather_kernel<0><<<g, 256, 0, stream>>>(p);
+  switch (C) {
+    case 1: grid_gather_kernel<1><<<g, 256, 0, stream>>>(p); break;
+    case 3: grid_gather_kernel<3><<<g, 256, 0, stream>>>(p); break;
+    case 4: grid_gather_kernel<4><<<g, 256, 0, stream>>>(p); break;
+    case 8: grid_gather_kernel<8><<<g, 256, 0, stream>>>(p); break;
+    case 16: grid_gather_kernel<16><<<g, 256, 0, stream>>>(p); break;
+    default: return SG_ERR_UNSUPPORTED;
+  }
   SG_LAUNCH_CHECK();
   return SG_OK;
 }

@@ -188,7 +188,7 @@ __device__ __forceinline__ void integrate_view(const float *__restrict__ Kk, con
 }
 
 template <int VPT>
-__global__ void __launch_bounds__(128) fuse_tsdf_kernel(FuseParams p) {
+__global__ void __launch_bounds__(256) fuse_tsdf_kernel(FuseParams p) {
   __shared__ float s_K[kMaxViews][9];
   __shared__ float s_P[kMaxViews][12];
   const int b = blockIdx.y;
@@ -243,11 +243,16 @@ __global__ void __launch_bounds__(128) fuse_tsdf_kernel(FuseParams p) {
       cnt += o;
     }
     size_t o = (size_t)b * vol + v0;
-    if (VPT == 4) {
+    if constexpr (VPT == 4) {
       *reinterpret_cast<float4 *>(p.tsdf + o) = make_float4(ts[0], ts[1], ts[2], ts[3]);
       *reinterpret_cast<float4 *>(p.weight + o) = make_float4(w[0], w[1], w[2], w[3]);
       *reinterpret_cast<float4 *>(p.colorv + o) = make_float4(col[0], col[1], col[2], col[3]);
       *reinterpret_cast<int4 *>(p.occ + o) = make_int4(oc[0], oc[1], oc[2], oc[3]);
+    } else if constexpr (VPT == 2) {
+      *reinterpret_cast<float2 *>(p.tsdf + o) = make_float2(ts[0], ts[1]);
+      *reinterpret_cast<float2 *>(p.weight + o) = make_float2(w[0], w[1]);
+      *reinterpret_cast<float2 *>(p.colorv + o) = make_float2(col[0], col[1]);
+      *reinterpret_cast<int2 *>(p.occ + o) = make_int2(oc[0], oc[1]);
     } else {
 #pragma unroll
       for (int j = 0; j < VPT; j++) {
@@ -294,16 +299,14 @@ extern "C" int sg_fuse_tsdf(const float *K, const float *RT, const float *color,
   FuseParams p{K, RT, color, depth, vol_bbox, voxel_size, tsdf, weight, colorv, occ, count,
                N, H, W, Dx, Dy, Dz, obs_weight, trunc_weight, th_low, th_high};
   long vol = (long)Dx * Dy * Dz;
-  bool vec = (Dz % 4 == 0) && ((((uintptr_t)tsdf) | ((uintptr_t)weight) | ((uintptr_t)colorv) |
-                                 ((uintptr_t)occ)) % 16 == 0);
-  if (vec) {
-    long groups = vol / 4;
-    int gx = ceil_div(groups, 128);
-    fuse_tsdf_kernel<4><<<dim3(gx, B), 128, 0, stream>>>(p);
-  } else {
-    int gx = ceil_div(vol, 128);
-    fuse_tsdf_kernel<1><<<dim3(gx, B), 128, 0, stream>>>(p);
-  }
+  int vpt = tune(SG_TUNE_FUSE_VPT);
+  const int blk = tune(SG_TUNE_FUSE_BLOCK);
+  const uintptr_t ptrs = ((uintptr_t)tsdf) | ((uintptr_t)weight) | ((uintptr_t)colorv) | ((uintptr_t)occ);
+  while (vpt > 1 && (Dz % vpt != 0 || ptrs % (4 * vpt) != 0)) vpt >>= 1;
+  const int gx = ceil_div(vol / vpt, blk);
+  if (vpt == 4) fuse_tsdf_kernel<4><<<dim3(gx, B), blk, 0, stream>>>(p);
+  else if (vpt == 2) fuse_tsdf_kernel<2><<<dim3(gx, B), blk, 0, stream>>>(p);
+  else fuse_tsdf_kernel<1><<<dim3(gx, B), blk, 0, stream>>>(p);
   SG_LAUNCH_CHECK();
   return SG_OK;
 }

@@ -31,7 +31,7 @@ struct IsectParams {
   SgStatus *st;
 };
 
-__global__ void __launch_bounds__(128) intersect_kernel(IsectParams p) {
+__global__ void __launch_bounds__(512) intersect_kernel(IsectParams p) {
   const SgTree &t = p.t;
   const long R = (long)t.B * p.N;
   const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -51,7 +51,6 @@ __global__ void __launch_bounds__(128) intersect_kernel(IsectParams p) {
     const LevelGeom gt = level_geom(vs, t.Db / t.Dt);
     const LevelGeom gb = level_geom(vs, 1);
     const int mw = sg_mask_words_dev(t.rate);
-    const int r2 = t.rate * t.rate;
     const long vt = (long)t.Dt * t.Dt * t.Dt;
     int *oi = p.hit_idx + (size_t)r * p.W;
     float *o0 = p.hit_t0 + (size_t)r * p.W, *o1 = p.hit_t1 + (size_t)r * p.W;
@@ -89,32 +88,68 @@ __global__ void __launch_bounds__(128) intersect_kernel(IsectParams p) {
                    node_coord(gt, bmin[2], st[2]), gt.vs, p0, p1) &&
               !(p0 < 0.0f || p1 < 0.0f)) {
             if (!p.is_training) {
+              // Children in lexicographic (x, y, z) order.  Only cells the
+              // ray can touch are visited: per x-slab of the brick, the y/z
+              // cell ranges of the ray segment inside the parent interval,
+              // widened by kMargin voxels (float error of the reference slab
+              // test is ~1e-6 of a voxel).  Each occupied candidate then
+              // gets the reference slab test, so the hit set and its order
+              // equal the reference's full scan over all children.
               const uint32_t *mask = t.brick_mask + (size_t)brick * mw;
               const int cb = t.base_bot + t.top_child_base[k];
-              int rank = 0;
-              for (int w = 0; w < mw; w++) {
-                uint32_t bits = __ldg(mask + w);
-                while (bits) {
-                  int bit = __ffs(bits) - 1;
-                  bits &= bits - 1;
-                  int c = w * 32 + bit;
-                  int a = c / r2, c2 = (c / t.rate) % t.rate, e = c % t.rate;
-                  float c0, c1;
-                  if (slab(o, inv, node_coord(gb, bmin[0], st[0] * t.rate + a),
-                           node_coord(gb, bmin[1], st[1] * t.rate + c2),
-                           node_coord(gb, bmin[2], st[2] * t.rate + e), gb.vs, c0, c1) &&
-                      !(c0 < 0.0f || c1 < 0.0f)) {
-                    if (cnt < p.W) {
-                      oi[cnt] = cb + rank;
-                      o0[cnt] = c0;
-                      o1[cnt] = c1;
-                    } else {
-                      over = true;
+              const int r = t.rate;
+              const float e0 = node_coord(gb, bmin[0], st[0] * r) - gb.vs * 0.5f;
+              const float e1 = node_coord(gb, bmin[1], st[1] * r) - gb.vs * 0.5f;
+              const float e2 = node_coord(gb, bmin[2], st[2] * r) - gb.vs * 0.5f;
+              const float ivs = 1.0f / gb.vs;
+              const float u0 = (o[0] - e0) * ivs, u1 = (o[1] - e1) * ivs, u2 = (o[2] - e2) * ivs;
+              const float du0 = d[0] * ivs, du1 = d[1] * ivs, du2 = d[2] * ivs;
+              const float tm_ = 1e-4f * (p1 - p0) + 1e-5f * fabsf(p1) + 1e-6f;
+              const float tlo = p0 - tm_, thi = p1 + tm_;
+              constexpr float kMargin = 0.02f;
+              for (int a = 0; a < r; a++) {
+                float ta, tb;
+                if (du0 != 0.0f) {
+                  float q1 = ((float)a - kMargin - u0) / du0, q2 = ((float)a + 1.0f + kMargin - u0) / du0;
+                  ta = fminf(q1, q2);
+                  tb = fmaxf(q1, q2);
+                } else {
+                  if (u0 < (float)a - kMargin || u0 > (float)a + 1.0f + kMargin) continue;
+                  ta = tlo;
+                  tb = thi;
+                }
+                ta = fmaxf(ta, tlo);
+                tb = fminf(tb, thi);
+                if (ta > tb) continue;
+                float ya = u1 + ta * du1, yb = u1 + tb * du1;
+                float za = u2 + ta * du2, zb = u2 + tb * du2;
+                int y0 = max(0, (int)floorf(fminf(ya, yb) - kMargin));
+                int y1 = min(r - 1, (int)floorf(fmaxf(ya, yb) + kMargin));
+                int z0 = max(0, (int)floorf(fminf(za, zb) - kMargin));
+                int z1 = min(r - 1, (int)floorf(fmaxf(za, zb) + kMargin));
+                for (int y = y0; y <= y1; y++) {
+                  for (int z = z0; z <= z1; z++) {
+                    const int c = (a * r + y) * r + z;
+                    const uint32_t word = __ldg(mask + (c >> 5));
+                    if (!((word >> (c & 31)) & 1u)) continue;
+                    float c0, c1;
+                    if (slab(o, inv, node_coord(gb, bmin[0], st[0] * r + a),
+                             node_coord(gb, bmin[1], st[1] * r + y), node_coord(gb, bmin[2], st[2] * r + z),
+                             gb.vs, c0, c1) &&
+                        !(c0 < 0.0f || c1 < 0.0f)) {
+                      int rank = __popc(word & ((1u << (c & 31)) - 1u));
+                      for (int w = 0; w < (c >> 5); w++) rank += __popc(__ldg(mask + w));
+                      if (cnt < p.W) {
+                        oi[cnt] = cb + rank;
+                        o0[cnt] = c0;
+                        o1[cnt] = c1;
+                      } else {
+                        over = true;
+                      }
+                      vlen = vlen + (c1 - c0) * 4.0f;
+                      cnt++;
                     }
-                    vlen = vlen + (c1 - c0) * 4.0f;
-                    cnt++;
                   }
-                  rank++;
                 }
               }
             }
@@ -219,7 +254,8 @@ extern "C" int sg_intersect(const SgTree *tree, const float *ori, const float *d
   IsectParams p{*tree, ori, dir, N, W, th_early_stop, opt_num, is_training,
                 hit_idx, hit_t0, hit_t1, valid_len, hit_count, status};
   long R = (long)tree->B * N;
-  intersect_kernel<<<ceil_div(R, 128), 128, 0, stream>>>(p);
+  const int blk = tune(SG_TUNE_ISECT_BLOCK);
+  intersect_kernel<<<ceil_div(R, blk), blk, 0, stream>>>(p);
   if (padded) {
     int g = ceil_div(R * 32, 256);
     if (g > 152 * 64) g = 152 * 64;

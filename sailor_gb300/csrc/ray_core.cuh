@@ -1,0 +1,362 @@
+// ray_core.cuh -- per-ray building blocks shared by the sampling, compositing
+// and fused render kernels (one warp per ray, lane l owns positions l, l+32..).
+#pragma once
+
+#include <type_traits>
+
+#include "common.cuh"
+
+namespace sg {
+
+// ---------------------------------------------------------------------------
+// sampling (ray_voxels_sampling_uniform_kernel, sampling_kernel.cu:1070-1177)
+// ---------------------------------------------------------------------------
+struct SampleParams {
+  SgTree t;
+  const int *hit_idx;
+  const float *hit_t0, *hit_t1, *rands, *valid_len;
+  int N, W, S, num_levels, start_level;
+  int *sampled_idx;
+  float *sampled_z;
+};
+
+// Warp-private shared scratch of the sampler.
+struct SampleScratch {
+  int start[32];
+  float mn[32], off[32];
+  int id[32];
+};
+
+// depth of the j-th sample (0-based) of a hit with n samples:
+// base = min + off*(j+1); z = base - off/2 + off*rand   (sampling_kernel.cu:1142-1148)
+__device__ __forceinline__ float sample_z(float mn, float off, int j, float rnd) {
+  float base = __fmaf_rn(off, (float)(j + 1), mn);
+  return sum3_rn(base, -(off * 0.5f), off * rnd);
+}
+
+// Samples of ray r into shared sz/si[0, S) in the reference's output order,
+// -1 where there is none.  The hit row holds nh entries (compact rows) or is
+// -1 terminated (nh = W).  Per chunk of 32 hits, lanes compute the hits'
+// sample counts exactly as the reference's serial loop, a warp scan turns
+// the serial "samples left" capping into output ranges, and the chunk's
+// samples are generated position-parallel: the owner of position q is the
+// last hit whose range starts at or before q (starts are non-decreasing and
+// strictly increasing over hits that get samples).  Returns #samples.
+__device__ __forceinline__ int warp_sample_ray(const SampleParams &p, long r, int nh, float rand_const,
+                                               float *sz, int *si, SampleScratch &sc) {
+  const int lane = lane_id();
+  const int S = p.S;
+  const int b = (int)(r / p.N);
+  const int *hi = p.hit_idx + (size_t)r * p.W;
+  const float *h0 = p.hit_t0 + (size_t)r * p.W, *h1 = p.hit_t1 + (size_t)r * p.W;
+  const float *rd = p.rands ? p.rands + (size_t)r * S : nullptr;
+  int done = 0;
+  if (nh > 0 && __ldg(hi) >= 0) {
+    const float vl = p.valid_len[r];
+    const float vs = p.t.voxel_size[b];
+    const float start_vs = vs * ldexpf(1.0f, 2 * (p.num_levels - p.start_level - 1));
+    const float vs_top = vs * (float)(p.t.Db / p.t.Dt);
+    int has = 0, nvalid = 0;
+    bool stop = false;
+    for (int c0 = 0; c0 < nh && !stop && has < S; c0 += 32) {
+      const int i = c0 + lane;
+      int id = -1;
+      float mn = -1.0f, mx = -1.0f;
+      if (i < nh) {
+        id = __ldg(hi + i);
+        mn = __ldg(h0 + i);
+        mx = __ldg(h1 + i);
+      }
+      bool ok = i < nh && !(id < 0 || mn < 0 || mx < 0);
+      const unsigned bad = __ballot_sync(SG_FULL, !ok);
+      const int first_bad = bad ? __ffs(bad) - 1 : 32;
+      ok = ok && lane < first_bad;
+      if (bad) stop = true;
+      int n = 0;
+      if (ok) {
+        const float nvs = (id >= p.t.base_top) ? vs_top : vs;
+        const float rate = start_vs / nvs;
+        n = (int)((mx - mn) * rate * (float)S / vl);
+        n = n >= 1 ? n : 1;
+        n = n < S ? n : S;
+      }
+      const int incl = warp_incl_scan(n);
+      const int start = has + incl - n;
+      int ne = S - start;
+      ne = ne < 0 ? 0 : (ne < n ? ne : n);
+      sc.start[lane] = start;
+      sc.mn[lane] = mn;
+      sc.off[lane] = (mx - mn) / (float)(ne + 1);
+      sc.id[lane] = id;
+      __syncwarp();
+      const int end = min(has + __shfl_sync(SG_FULL, incl, 31), S);
+      for (int q = has + lane; q < end; q += 32) {
+        int lo = 0, up = 31;
+        while (lo < up) {
+          const int mid = (lo + up + 1) >> 1;
+          if (sc.start[mid] <= q) lo = mid;
+          else up = mid - 1;
+        }
+        sz[q] = sample_z(sc.mn[lo], sc.off[lo], q - sc.start[lo], rd ? __ldg(rd + q) : rand_const);
+        si[q] = sc.id[lo];
+      }
+      __syncwarp();
+      has = end;
+      nvalid += __popc(__ballot_sync(SG_FULL, ok));
+    }
+    // leftover: one more sample in each of the first hits (:1156-1174)
+    const int left = S - has;
+    const int cnt = left < nvalid ? left : nvalid;
+    for (int i = lane; i < cnt; i += 32) {
+      const int id = __ldg(hi + i);
+      const float mn = __ldg(h0 + i), mx = __ldg(h1 + i);
+      const float off = (mx - mn) * 0.5f;
+      const float base = mn + off;
+      const int q = has + i;
+      sz[q] = sum3_rn(base, -(off * 0.5f), off * (rd ? __ldg(rd + q) : rand_const));
+      si[q] = id;
+    }
+    done = has + cnt;
+  }
+  for (int q = done + lane; q < S; q += 32) {
+    sz[q] = -1.0f;
+    si[q] = -1;
+  }
+  __syncwarp();
+  return done;
+}
+
+// ---------------------------------------------------------------------------
+// per-ray sort: register bitonic network on (depth, position) keys
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t ordered_bits(float f) {
+  uint32_t u = __float_as_uint(f);
+  return u ^ ((u >> 31) ? 0xffffffffu : 0x80000000u);
+}
+__device__ __forceinline__ float from_ordered(uint32_t k) {
+  return __uint_as_float((k >> 31) ? (k ^ 0x80000000u) : ~k);
+}
+
+// E keys per lane, element i = e*32 + lane, P = 32*E (power of two)
+template <int E>
+__device__ __forceinline__ void bitonic_warp(unsigned long long (&key)[E]) {
+  const int lane = lane_id();
+  constexpr int P = 32 * E;
+#pragma unroll
+  for (int k = 2; k <= P; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      if (j >= 32) {
+        const int m = j >> 5;
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+          if ((e & m) == 0) {
+            const int i = e * 32 + lane;
+            const bool asc = (i & k) == 0;
+            unsigned long long a = key[e], c = key[e ^ m];
+            bool sw = asc ? (a > c) : (a < c);
+            key[e] = sw ? c : a;
+            key[e ^ m] = sw ? a : c;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+          const int i = e * 32 + lane;
+          const bool asc = (i & k) == 0;
+          unsigned long long other = __shfl_xor_sync(SG_FULL, key[e], j);
+          const bool lower = (lane & j) == 0;
+          unsigned long long mn = key[e] < other ? key[e] : other;
+          unsigned long long mx = key[e] < other ? other : key[e];
+          key[e] = (lower == asc) ? mn : mx;
+        }
+      }
+    }
+  }
+}
+
+// Sort the samples of a ray in shared memory.  sz[0, done) hold the
+// samples, sz[done, S) the -1 padding (warp_sample_ray's layout).  On
+// return sz[i] / spos[i] hold the depth and original position of sorted
+// position i: the padding first (stable: positions done, done+1, ...), then
+// the samples ascending by (depth, position).  Only the samples are sorted,
+// with the smallest register bitonic network that holds them.
+__device__ __forceinline__ void warp_sort_samples(float *sz, int *spos, int S, int done) {
+  const int lane = lane_id();
+  const int npad = S - done;
+  for (int q = lane; q < npad; q += 32) spos[q] = done + q;
+  if (done > 0) {
+    auto run = [&](auto tag) {
+      constexpr int E = decltype(tag)::value;
+      unsigned long long key[E];
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        const int i = e * 32 + lane;
+        key[e] = (i < done) ? (((unsigned long long)ordered_bits(sz[i]) << 32) | (unsigned)i) : ~0ull;
+      }
+      __syncwarp();
+      bitonic_warp<E>(key);
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        const int j = e * 32 + lane;
+        if (j < done) {
+          sz[npad + j] = from_ordered((uint32_t)(key[e] >> 32));
+          spos[npad + j] = (int)(key[e] & 0xffffffffu);
+        }
+      }
+    };
+    if (done <= 32) run(std::integral_constant<int, 1>());
+    else if (done <= 64) run(std::integral_constant<int, 2>());
+    else if (done <= 128) run(std::integral_constant<int, 4>());
+    else run(std::integral_constant<int, 8>());
+  }
+  __syncwarp();
+  for (int q = lane; q < npad; q += 32) sz[q] = -1.0f;
+  __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// compositing (volume_rendering.cu:17-240)
+// ---------------------------------------------------------------------------
+// alpha per sorted position.  mode 0: 1 - exp(-sigma * delta) with delta to
+// the next position holding z > 0 (else the last position; 1e10 for the
+// last position itself, :87-97); mode 1: alpha = sigma.  s_z: depths by
+// sorted position.  Invalid positions (z < 0) get alpha 0.
+template <int E>
+__device__ __forceinline__ void ray_alpha(const float (&z)[E], const float (&sg)[E], unsigned valid, int S,
+                                          int mode, const float *s_z, float (&al)[E]) {
+  const int lane = lane_id();
+  if (mode == 0) {
+    unsigned gtz[E];
+#pragma unroll
+    for (int e = 0; e < E; e++) gtz[e] = __ballot_sync(SG_FULL, z[e] > 0.0f);
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      const int i = e * 32 + lane;
+      al[e] = 0.0f;
+      if ((valid >> e) & 1u) {
+        float delta;
+        if (i == S - 1) {
+          delta = 1e10f;
+        } else {
+          int m = S - 1;
+          const unsigned above = (lane == 31) ? 0u : (gtz[e] & (~0u << (lane + 1)));
+          if (above) {
+            m = e * 32 + __ffs(above) - 1;
+          } else {
+#pragma unroll
+            for (int e2 = 0; e2 < E; e2++)
+              if (e2 > e && gtz[e2] && m == S - 1) m = e2 * 32 + __ffs(gtz[e2]) - 1;
+          }
+          delta = s_z[m] - z[e];
+        }
+        al[e] = 1.0f - __expf(-sg[e] * delta);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int e = 0; e < E; e++) al[e] = ((valid >> e) & 1u) ? sg[e] : 0.0f;
+  }
+}
+
+// Transmittance before each position, carried strictly sequentially over
+// positions (bit-identical to the reference's serial T *= 1 - alpha, so is
+// the early-termination decision T < t_thres, which the reference takes
+// after each valid sample).  proc: position reached; post: transmittance
+// after the position still >= t_thres.
+//
+// Every lane runs the same chain (warp-uniform), four positions per step
+// from a shared-memory factor array; the factors are overwritten in place
+// by the transmittance before each position, which the owning lanes read
+// back.  Positions before the first valid one are padding (factor 1) and
+// are skipped.  s_f: 32*E floats of warp-private shared scratch.
+template <int E>
+__device__ __forceinline__ void ray_transmittance(const float (&al)[E], unsigned valid, int S, float t_thres,
+                                                  float *s_f, float (&tb)[E], unsigned &proc, unsigned &post) {
+  const int lane = lane_id();
+  int m0 = 32 * E;
+#pragma unroll
+  for (int e = E - 1; e >= 0; e--) {
+    const unsigned vb = __ballot_sync(SG_FULL, (valid >> e) & 1u);
+    if (vb) m0 = e * 32 + __ffs(vb) - 1;
+  }
+#pragma unroll
+  for (int e = 0; e < E; e++) s_f[e * 32 + lane] = ((valid >> e) & 1u) ? (1.0f - al[e]) : 1.0f;
+  __syncwarp();
+  int stop = 1 << 30;  // position whose update took T below t_thres
+  int end = S;
+  if (m0 < S) {
+    float T = 1.0f;
+    for (int i = m0 & ~3; i < S; i += 4) {
+      const float4 f = *reinterpret_cast<const float4 *>(s_f + i);
+      const float T1 = T * f.x, T2 = T1 * f.y, T3 = T2 * f.z, T4 = T3 * f.w;
+      __syncwarp();
+      if (lane == 0) *reinterpret_cast<float4 *>(s_f + i) = make_float4(T, T1, T2, T3);
+      __syncwarp();
+      const bool c1 = i >= m0 && T1 < t_thres;
+      const bool c2 = i + 1 >= m0 && i + 1 < S && T2 < t_thres;
+      const bool c3 = i + 2 >= m0 && i + 2 < S && T3 < t_thres;
+      const bool c4 = i + 3 >= m0 && i + 3 < S && T4 < t_thres;
+      if (c1 || c2 || c3 || c4) {
+        stop = c1 ? i : (c2 ? i + 1 : (c3 ? i + 2 : i + 3));
+        end = stop + 1;
+        break;
+      }
+      T = T4;
+    }
+  } else {
+    end = 0;
+  }
+  __syncwarp();
+  proc = 0;
+  post = 0;
+#pragma unroll
+  for (int e = 0; e < E; e++) {
+    const int i = e * 32 + lane;
+    tb[e] = 0.0f;
+    if (i >= m0 && i < end) {
+      tb[e] = s_f[i];
+      proc |= 1u << e;
+      if (i != stop) post |= 1u << e;
+    }
+  }
+  __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// dense-grid trilinear tap (grid [D,D,D,C] channel-last of one frame, voxel
+// (x,y,z) centred at bbox_min + (x,y,z) * vs, outside corners contribute 0)
+// ---------------------------------------------------------------------------
+template <int C>
+__device__ __forceinline__ void grid_tap(const float *__restrict__ grid, int D, const float bmin[3], float vs,
+                                         const float pt[3], float (&acc)[C]) {
+  int i0[3];
+  float f[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const float u = (pt[a] - bmin[a]) / vs;
+    const float fl = floorf(u);
+    i0[a] = (int)fl;
+    f[a] = u - fl;
+  }
+#pragma unroll
+  for (int c = 0; c < C; c++) acc[c] = 0.0f;
+#pragma unroll
+  for (int cr = 0; cr < 8; cr++) {
+    const int dx = (cr >> 2) & 1, dy = (cr >> 1) & 1, dz = cr & 1;
+    const int ix = i0[0] + dx, iy = i0[1] + dy, iz = i0[2] + dz;
+    if (ix < 0 || iy < 0 || iz < 0 || ix >= D || iy >= D || iz >= D) continue;
+    const float w = (dx ? f[0] : 1.0f - f[0]) * (dy ? f[1] : 1.0f - f[1]) * (dz ? f[2] : 1.0f - f[2]);
+    const float *g = grid + (((size_t)ix * D + iy) * D + iz) * C;
+#pragma unroll
+    for (int c = 0; c < C; c++) acc[c] = __fmaf_rn(w, __ldg(g + c), acc[c]);
+  }
+}
+
+// density of a normalised TSDF value t: sigmoid(-t * scale / s) / s
+__device__ __forceinline__ float tsdf_density(float t, float scale, float s) {
+  const float v = t * scale / s;
+  return (1.0f / (1.0f + __expf(v))) / s;
+}
+
+}  // namespace sg

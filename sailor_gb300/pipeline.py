@@ -106,11 +106,15 @@ class FramePipeline:
         self._mark("tree")
 
     def render(self, ori, dirs, color_grid, color_bbox, color_vs, trunc_metres, rands=None, rand_const=0.5,
-               sdf_scale=0.005, t_thres=1e-4):
+               sdf_scale=0.005, t_thres=1e-4, fused=True, keep_samples=False):
         """Intersect, sample, gather fields and composite the rays [B, n_rays, 3].
 
         trunc_metres: the truncation margin (voxel_size * trunc_weight) that
-        turns the normalised TSDF into metres for the density transform."""
+        turns the normalised TSDF into metres for the density transform.
+        fused: one kernel for sampling, sort, field taps and compositing
+        (sg_render_fused); False runs them as four kernels with the sorted
+        samples, densities and colours in HBM (same results).
+        keep_samples: with fused, also write the sorted depths / node ids."""
         B, Nr, S, W = self.B, self.n_rays, self.S, self.W
         st = N.stream()
         N.check(N.lib.sg_intersect(C.byref(self.tree), N.ptr(ori), N.ptr(dirs), Nr, W, -1, -1, 0, 0,
@@ -118,6 +122,18 @@ class FramePipeline:
                                    N.ptr(self.valid_len), N.ptr(self.hit_count), N.ptr(self.status), st),
                 "intersect")
         self._mark("intersect")
+        if fused:
+            Dc = color_grid.shape[1]
+            N.check(N.lib.sg_render_fused(
+                C.byref(self.tree), N.ptr(self.hit_idx), N.ptr(self.hit_t0), N.ptr(self.hit_t1),
+                N.ptr(self.hit_count), Nr, W, N.ptr(rands), float(rand_const), N.ptr(self.valid_len), S, 2, 0,
+                N.ptr(ori), N.ptr(dirs), N.ptr(self.tsdf), self.D, float(trunc_metres), float(sdf_scale),
+                N.ptr(color_grid), Dc, N.ptr(color_bbox), N.ptr(color_vs), float(t_thres), N.ptr(self.out_rgb),
+                N.ptr(self.out_depth), N.ptr(self.out_ws), N.ptr(self.out_alpha),
+                N.ptr(self.z) if keep_samples else None, N.ptr(self.node) if keep_samples else None, st),
+                "render_fused")
+            self._mark("render")
+            return self.out_rgb, self.out_depth, self.out_ws, self.out_alpha
         N.check(N.lib.sg_sample_sorted(C.byref(self.tree), N.ptr(self.hit_idx), N.ptr(self.hit_t0),
                                        N.ptr(self.hit_t1), N.ptr(self.hit_count), Nr, W, N.ptr(rands),
                                        float(rand_const), N.ptr(self.valid_len), S, 2, 0, N.ptr(self.z),

@@ -346,8 +346,9 @@ def test_pipeline_matches_oracle():
     pipe.build(_t(sc["K"]), _t(sc["RT"]), _t(sc["colors"]), _t(sc["depths"]), _t(sc["vol_bbox"]),
                _t(sc["voxel_size"]), sc["trunc_weight"])
     trunc_m = float(sc["voxel_size"][0, 0]) * sc["trunc_weight"]
-    rgb, dep, ws, al = pipe.render(_t(ori), _t(dirs), _t(cgrid), _t(cbb), _t(cvs), trunc_m)
+    rgb, dep, ws, al = pipe.render(_t(ori), _t(dirs), _t(cgrid), _t(cbb), _t(cvs), trunc_m, fused=False)
     torch.cuda.synchronize()
+    unfused = [a.clone() for a in (rgb, dep, ws, al, pipe.z, pipe.node)]
     assert pipe.status[0].item() == 0
     rands = np.full((1, R, S), 0.5, np.float32)
     ref = orc.chain(sc, D, rate, S, ori, dirs, rands, W=1024, trunc_weight=sc["trunc_weight"])
@@ -377,3 +378,57 @@ def test_pipeline_matches_oracle():
     assert np.abs(rgb.cpu().numpy() - rf[0])[good].max() <= ATOL
     assert np.abs(dep.cpu().numpy() - rd[0, :, 0])[good].max() <= ATOL
     assert np.abs(ws.cpu().numpy() - rw[0, :, 0])[good].max() <= ATOL
+
+    # the fused render kernel gives the unfused chain's results bit for bit
+    pipe.render(_t(ori), _t(dirs), _t(cgrid), _t(cbb), _t(cvs), trunc_m, fused=True, keep_samples=True)
+    torch.cuda.synchronize()
+    for a, b in zip((pipe.out_rgb, pipe.out_depth, pipe.out_ws, pipe.out_alpha, pipe.z, pipe.node), unfused):
+        assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("obs,views,frac_colour", [(1.0, 12, False), (0.7, 4, False), (1.0, 4, True)])
+def test_fusion_paths_bit_exact(obs, views, frac_colour):
+    """The fused kernel's shortcuts (first observation, free space, integer
+    colour channels, approximate pixel quotient with exact fall-back) and
+    its general path all reproduce the reference arithmetic bit for bit."""
+    from sailor_gb300.dist import VoxelEncoding as VE
+    D = 96
+    sc = syn.make_scene(seed=41, n_views=views, res=160, n_prims=10, D=D, trunc=0.03)
+    colors = sc["colors"].copy()
+    if frac_colour:
+        colors = colors + np.float32(0.37)  # packed values that are not integers
+    occ = torch.full((1, D, D, D), -1, dtype=torch.int32, device="cuda")
+    cnt = torch.zeros((1, 1), dtype=torch.int32, device="cuda")
+    ts, w, c = VE.integrate_in_box(occ, cnt, _t(sc["K"]), _t(sc["RT"]), _t(colors), _t(sc["depths"]),
+                                   _t(sc["vol_bbox"]), _t(sc["voxel_size"]), obs, sc["trunc_weight"], 13.5, 13.5, 0)
+    ref = orc.integrate(sc["K"], sc["RT"], colors, sc["depths"], D, sc["vol_bbox"], sc["voxel_size"], obs,
+                        sc["trunc_weight"], 13.5, 13.5)
+    assert np.array_equal(ts.cpu().numpy(), ref["tsdf"])
+    assert np.array_equal(w.cpu().numpy(), ref["weight"])
+    assert np.array_equal(c.cpu().numpy(), ref["color"])
+    assert np.array_equal(occ.cpu().numpy(), ref["occ"])
+
+
+def test_launch_shapes_do_not_change_results():
+    """Every autotuner knob value gives bit-identical outputs."""
+    from sailor_gb300 import autotune
+    from sailor_gb300.dist import VoxelEncoding as VE
+    D = 64
+    sc = syn.make_scene(seed=51, n_views=4, res=128, n_prims=8, D=D, trunc=0.03)
+    saved = autotune.current()
+    outs = []
+    try:
+        for vpt, blk in ((1, 64), (2, 128), (4, 256)):
+            autotune.set_knob("fuse_vpt", vpt)
+            autotune.set_knob("fuse_block", blk)
+            occ = torch.full((1, D, D, D), -1, dtype=torch.int32, device="cuda")
+            cnt = torch.zeros((1, 1), dtype=torch.int32, device="cuda")
+            r = VE.integrate_in_box(occ, cnt, _t(sc["K"]), _t(sc["RT"]), _t(sc["colors"]), _t(sc["depths"]),
+                                    _t(sc["vol_bbox"]), _t(sc["voxel_size"]), 1.0, sc["trunc_weight"], 13.5, 13.5, 0)
+            outs.append([t.clone() for t in r] + [occ, cnt])
+    finally:
+        for k, v in saved.items():
+            autotune.set_knob(k, v)
+    for o in outs[1:]:
+        for a, b in zip(outs[0], o):
+            assert torch.equal(a, b)
