@@ -135,6 +135,31 @@ size_t sg_tree_scratch_bytes(int B, int Dt);
 int sg_tree_build(SgTree *tree, int *occ_top, int *occ_bot, void *scratch,
                   size_t scratch_bytes, SgStatus *status, sg_stream_t stream);
 
+/* Size of the device scratch array that sg_tree_build_static uses: 8 MiB,
+ * held on every GPU that loads the library until the process exits.  It
+ * covers sg_tree_scratch_bytes(B, Dt) up to about one million top bricks
+ * (B * Dt^3 <= 1,040,000), e.g. three 512^3 volumes with 8^3 bricks
+ * (786,432 bricks) or sixteen 256^3 volumes. */
+#define SG_TREE_STATIC_SCRATCH_BYTES (8u << 20)
+
+/* sg_tree_build for callers that cannot allocate device memory (their
+ * process's device memory belongs to another allocator, their per-frame loop
+ * cannot take the synchronisation of cudaMalloc/cudaFree, or they reach this
+ * library through a plain C foreign-function interface with no device
+ * allocator).  Same inputs, outputs and results as sg_tree_build; the scratch
+ * comes from the library's own fixed device array instead of the caller.
+ * No counterpart in the reference: its tree build allocates through ATen
+ * and thrust.
+ * Returns SG_ERR_CAPACITY, and launches nothing, when
+ * sg_tree_scratch_bytes(B, Dt) > SG_TREE_STATIC_SCRATCH_BYTES.  Allocates
+ * nothing.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) and caches it: make that call before any stream
+ * capture on the device.  All calls on a device share the array, so calls
+ * that overlap on the GPU race; order them on one stream.  Nothing in the
+ * array needs clearing between calls. */
+int sg_tree_build_static(SgTree *tree, int *occ_top, int *occ_bot,
+                         SgStatus *status, sg_stream_t stream);
+
 /* Node table [n_nodes, 6] = (centre x, y, z, edge, valid, frame) per node
  * id.  Replaces MultiLayerOctree::output_all_nodes_tensor
  * (octree_kernel.cu:309-328, 699-717). */

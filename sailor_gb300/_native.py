@@ -20,7 +20,7 @@ EXPORTS = (
     "sg_brick_occupancy", "sg_tree_scratch_bytes", "sg_tree_build", "sg_tree_nodes", "sg_intersect",
     "sg_sample_coarse", "sg_sort_samples", "sg_composite_fwd", "sg_composite_bwd",
     "sg_trilerp_nodes_fwd", "sg_trilerp_nodes_bwd", "sg_sample_sorted", "sg_grid_gather",
-    "sg_render_fused", "sg_tune_set", "sg_tune_get",
+    "sg_render_fused", "sg_tune_set", "sg_tune_get", "sg_tree_build_static",
 )
 
 
@@ -51,6 +51,7 @@ def _load():
     lib.sg_tree_scratch_bytes.argtypes = [i, i]
     lib.sg_tree_scratch_bytes.restype = sz
     lib.sg_tree_build.argtypes = [C.POINTER(SgTree), p, p, p, sz, p, p]
+    lib.sg_tree_build_static.argtypes = [C.POINTER(SgTree), p, p, p, p]
     lib.sg_tree_nodes.argtypes = [C.POINTER(SgTree), i, p, p]
     lib.sg_intersect.argtypes = [C.POINTER(SgTree), p, p, i, i, i, i, i, i, p, p, p, p, p, p, p]
     lib.sg_sample_coarse.argtypes = [C.POINTER(SgTree), p, p, p, i, i, p, p, i, i, i, p, p, p]

@@ -392,3 +392,78 @@ extern "C" int sg_tree_build(SgTree *tree, int *occ_top, int *occ_bot, void *scr
   SG_LAUNCH_CHECK();
   return SG_OK;
 }
+
+// ---------------------------------------------------------------------------
+// sg_tree_build_static: sg_tree_build without a caller-provided scratch
+// buffer.
+//
+// Some callers cannot call cudaMalloc: a host process whose device memory is
+// owned by another allocator (a framework's caching pool or a fixed memory
+// budget, where an extra allocation can fail or fragment the pool), per-frame
+// loops that cannot afford the device-wide synchronisation cudaFree may take,
+// and plain-C callers through a foreign-function interface that have no device
+// allocator of their own to size and own a buffer.  This variant takes its
+// scratch (the per-brick keep flags and child counts and the per-tile scan
+// totals) from a fixed array in the library's device memory instead.
+//
+// The array is SG_TREE_STATIC_SCRATCH_BYTES (8 MiB) of device memory that every
+// GPU which loads the library holds until the process exits.  In host code
+// g_tree_static_scratch is only a host-side stand-in for the device array, so
+// its device address is looked up with cudaGetSymbolAddress -- once per
+// device, on the first call made with that device current, and cached.  Make
+// that first call before any stream capture on the device.
+//
+// Every call shares the one array per device, and the array keeps what the
+// last call left in it.  Nothing here needs zeroing first: every scratch word
+// a call reads was written earlier in the same call.  Calls whose work
+// overlaps on the GPU (different streams, no ordering between them) race on
+// the array and produce wrong trees; order them on one stream or with events.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+static __device__ __align__(256) unsigned char g_tree_static_scratch[SG_TREE_STATIC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kMaxStaticDevices = 64;
+std::mutex g_static_mu;
+void *g_static_ptr[kMaxStaticDevices] = {};
+}  // namespace
+
+extern "C" int sg_tree_build_static(SgTree *tree, int *occ_top, int *occ_bot, SgStatus *status,
+                                    sg_stream_t stream) {
+  if (!tree || !occ_top || !occ_bot) return SG_ERR_INVALID_ARG;
+  SgTree t = *tree;
+  if (t.B <= 0 || t.Dt <= 0 || t.rate <= 0 || t.Db != t.Dt * t.rate) return SG_ERR_INVALID_ARG;
+  if (!t.brick_node || !t.brick_mask || !t.top_key || !t.top_child_base || !t.bot_key || !t.bot_parent ||
+      !t.counts)
+    return SG_ERR_INVALID_ARG;
+  if (t.rate * t.rate * t.rate > 4096) return SG_ERR_UNSUPPORTED;
+  if (sg_tree_scratch_bytes(t.B, t.Dt) > (size_t)SG_TREE_STATIC_SCRATCH_BYTES) return SG_ERR_CAPACITY;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) return SG_ERR_CUDA;
+  if (dev < 0 || dev >= kMaxStaticDevices) return SG_ERR_UNSUPPORTED;
+  void *base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_ptr[dev]) {
+      void *p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_tree_static_scratch) != cudaSuccess || !p) return SG_ERR_CUDA;
+      g_static_ptr[dev] = p;
+    }
+    base = g_static_ptr[dev];
+  }
+  TreeScratch s;
+  scratch_layout(t.B, t.Dt, (char *)base, &s, nullptr);
+  long nb = (long)t.B * t.Dt * t.Dt * t.Dt;
+  int ntiles = ceil_div(nb, kTile);
+  int mw = sg_mask_words(t.rate);
+  int gw = ceil_div(nb * 32, 256);
+  if (gw > 152 * 64) gw = 152 * 64;
+  tree_classify_kernel<<<gw, 256, 0, stream>>>(t, occ_top, occ_bot, s, mw);
+  tree_tile_sum_kernel<<<ntiles, 256, 0, stream>>>(s, nb);
+  tree_tile_scan_kernel<<<1, 1024, 0, stream>>>(s, ntiles, t, status);
+  tree_emit_top_kernel<<<ntiles, 256, 0, stream>>>(t, occ_top, s, nb);
+  tree_emit_children_kernel<<<152 * 8, 256, 0, stream>>>(t, occ_bot, mw);
+  SG_LAUNCH_CHECK();
+  return SG_OK;
+}
