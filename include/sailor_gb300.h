@@ -84,7 +84,9 @@ enum {
   SG_TUNE_FUSE_BLOCK = 1,    /* threads per CTA in sg_fuse_tsdf: 32..256   */
   SG_TUNE_ISECT_BLOCK = 2,   /* threads per CTA in sg_intersect: 32..512   */
   SG_TUNE_RENDER_WARPS = 3,  /* CTAs per SM (x152) in warp-per-ray kernels */
-  SG_TUNE_COUNT = 4
+  SG_TUNE_FUSE_TILED = 4,    /* sg_fuse_tsdf voxel order: 1 = 16^3 tiles,   */
+                             /* 0 = linear runs (FUSE_VPT, FUSE_BLOCK)      */
+  SG_TUNE_COUNT = 5
 };
 int sg_tune_set(int knob, int value);
 int sg_tune_get(int knob);

@@ -17,13 +17,14 @@ import torch
 
 from . import _native as N
 
-KNOBS = {"fuse_vpt": 0, "fuse_block": 1, "isect_block": 2, "render_warps": 3}
+KNOBS = {"fuse_vpt": 0, "fuse_block": 1, "isect_block": 2, "render_warps": 3, "fuse_tiled": 4}
 
 CANDIDATES = {
     "fuse_vpt": (1, 2, 4),
     "fuse_block": (64, 128, 256),  # the kernel is built for <= 256 threads
     "isect_block": (64, 128, 256),
     "render_warps": (16, 32, 64),
+    "fuse_tiled": (0, 1),  # 1: 16^3 voxel tiles; 0: linear runs shaped by fuse_vpt / fuse_block
 }
 
 CACHE = os.path.join(os.path.expanduser("~"), ".cache", "sailor_gb300", "tune.json")
@@ -94,5 +95,15 @@ def tune_pipeline(pipe, build_fn, render_fn, reps=3, cache=True, verbose=False):
     key = None
     if cache:
         key = f"B{pipe.B}_D{pipe.D}_r{pipe.rate}_n{pipe.n_rays}_S{pipe.S}_{torch.cuda.get_device_name()}"
-    return tune({"fuse_vpt": build_fn, "fuse_block": build_fn, "isect_block": render_fn,
-                 "render_warps": render_fn}, reps=reps, cache_key=key, verbose=verbose)
+    if not (cache and key and _cached(key)):
+        set_knob("fuse_tiled", 0)  # the linear shape knobs only act with tiling off
+    return tune({"fuse_vpt": build_fn, "fuse_block": build_fn, "fuse_tiled": build_fn,
+                 "isect_block": render_fn, "render_warps": render_fn}, reps=reps, cache_key=key,
+                verbose=verbose)
+
+
+def _cached(key, cache_path=CACHE):
+    try:
+        return key in json.load(open(cache_path))
+    except (OSError, ValueError):
+        return False

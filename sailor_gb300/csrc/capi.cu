@@ -18,7 +18,7 @@ extern "C" int sg_version(void) { return 100; }
 // launch-shape knobs
 // ---------------------------------------------------------------------------
 namespace sg {
-static int g_tune[SG_TUNE_COUNT] = {4, 128, 64, 64};
+static int g_tune[SG_TUNE_COUNT] = {4, 128, 64, 64, 1};
 
 int tune(int knob) { return (knob >= 0 && knob < SG_TUNE_COUNT) ? g_tune[knob] : 0; }
 }  // namespace sg
@@ -36,6 +36,9 @@ extern "C" int sg_tune_set(int knob, int value) {
       break;
     case SG_TUNE_RENDER_WARPS:
       if (value < 1 || value > 64) return SG_ERR_INVALID_ARG;
+      break;
+    case SG_TUNE_FUSE_TILED:
+      if (value != 0 && value != 1) return SG_ERR_INVALID_ARG;
       break;
     default:
       return SG_ERR_INVALID_ARG;

@@ -4,8 +4,9 @@
 //   inverse_mat3x3 :105, obtain_origin_bbox :137, obtain_resized_bbox :51,
 //   integrate_cuda :236 and the host wrapper fusion_cuda_integrate :600.
 //
-// fuse_tsdf: one thread per 4 consecutive z voxels of one x-y row, one CTA
-// row of the grid per frame (blockIdx.y).  Cameras (K, [R|T] of every view)
+// fuse_tsdf: one thread per 4 consecutive z voxels, one CTA row of the grid
+// per frame (blockIdx.y); CTAs take 16^3 voxel tiles (or, as a tuning
+// alternative, linear runs of voxels).  Cameras (K, [R|T] of every view)
 // sit in shared memory; tsdf/weight/colour live in registers across the view
 // loop and are stored once with 16-byte vector stores (the reference pre-
 // fills three full volumes with torch::full and then read-modify-writes them
@@ -187,24 +188,107 @@ __device__ __forceinline__ void integrate_view(const float *__restrict__ Kk, con
   col = nb * 256.0f * 256.0f + ng * 256.0f + nr;
 }
 
-template <int VPT>
-__global__ void __launch_bounds__(256) fuse_tsdf_kernel(FuseParams p) {
-  __shared__ float s_K[kMaxViews][9];
-  __shared__ float s_P[kMaxViews][12];
-  const int b = blockIdx.y;
+// Common per-frame constants of the fusion kernels.
+struct FuseFrame {
+  int b;
+  long vol;
+  size_t img;
+  float vs, trunc, bx, by, bz, hi_th, lo_th;
+};
+
+__device__ __forceinline__ FuseFrame fuse_frame(const FuseParams &p, int b) {
+  FuseFrame f;
+  f.b = b;
+  f.vol = (long)p.Dx * p.Dy * p.Dz;
+  f.img = (size_t)p.H * p.W;
+  f.vs = p.voxel_size[b];
+  f.trunc = f.vs * p.trunc_weight;
+  f.bx = p.vol_bbox[b * 6 + 0];
+  f.by = p.vol_bbox[b * 6 + 2];
+  f.bz = p.vol_bbox[b * 6 + 4];
+  f.hi_th = f.trunc * p.th_high;
+  f.lo_th = -f.trunc * p.th_low;
+  return f;
+}
+
+// Cameras of frame b into shared memory (all threads of the CTA take part).
+__device__ __forceinline__ void load_cameras(const FuseParams &p, int b, float (*s_K)[9], float (*s_P)[12]) {
   for (int i = threadIdx.x; i < p.N * 21; i += blockDim.x) {
     int v = i / 21, k = i - v * 21;
     if (k < 9) s_K[v][k] = p.K[(size_t)(b * p.N + v) * 9 + k];
     else s_P[v][k - 9] = p.RT[(size_t)(b * p.N + v) * 12 + (k - 9)];
   }
   __syncthreads();
-  const long vol = (long)p.Dx * p.Dy * p.Dz;
-  const long groups = vol / VPT;
-  const float vs = p.voxel_size[b];
-  const float trunc = vs * p.trunc_weight;
-  const float bx = p.vol_bbox[b * 6 + 0], by = p.vol_bbox[b * 6 + 2], bz = p.vol_bbox[b * 6 + 4];
-  const float hi_th = trunc * p.th_high, lo_th = -trunc * p.th_low;
-  const size_t img = (size_t)p.H * p.W;
+}
+
+// Fuse the VPT z-consecutive voxels (x, y, z0 .. z0+VPT-1) over all views and
+// store them; returns how many of them are occupied.
+template <int VPT>
+__device__ __forceinline__ int fuse_group(const FuseParams &p, const FuseFrame &f, const float (*s_K)[9],
+                                          const float (*s_P)[12], int x, int y, int z0) {
+  const long v0 = ((long)x * p.Dy + y) * p.Dz + z0;
+  float px = __fmaf_rn((float)x, f.vs, f.bx);
+  float py = __fmaf_rn((float)y, f.vs, f.by);
+  float pz[VPT], ts[VPT], w[VPT], col[VPT];
+#pragma unroll
+  for (int j = 0; j < VPT; j++) {
+    pz[j] = __fmaf_rn((float)(z0 + j), f.vs, f.bz);
+    ts[j] = 1.0f;
+    w[j] = 0.0f;
+    col[j] = 0.0f;
+  }
+  for (int k = 0; k < p.N; k++) {
+    const float *P = s_P[k];
+    const float *Kk = s_K[k];
+    float ax = __fmaf_rn(P[0], px, P[1] * py);
+    float ay = __fmaf_rn(P[4], px, P[5] * py);
+    float az = __fmaf_rn(P[8], px, P[9] * py);
+    const float *dimg = p.depth + ((size_t)f.b * p.N + k) * f.img;
+    const float *cimg = p.color + ((size_t)f.b * p.N + k) * f.img;
+#pragma unroll
+    for (int j = 0; j < VPT; j++)
+      integrate_view(Kk, P, ax, ay, az, pz[j], dimg, cimg, p.H, p.W, f.trunc, p.obs_weight, ts[j], w[j],
+                     col[j]);
+  }
+  int oc[VPT], cnt = 0;
+#pragma unroll
+  for (int j = 0; j < VPT; j++) {
+    bool o = ts[j] < f.hi_th && ts[j] > f.lo_th;
+    oc[j] = o ? (int)(v0 + j) : -1;
+    cnt += o;
+  }
+  size_t o = (size_t)f.b * f.vol + v0;
+  if constexpr (VPT == 4) {
+    *reinterpret_cast<float4 *>(p.tsdf + o) = make_float4(ts[0], ts[1], ts[2], ts[3]);
+    *reinterpret_cast<float4 *>(p.weight + o) = make_float4(w[0], w[1], w[2], w[3]);
+    *reinterpret_cast<float4 *>(p.colorv + o) = make_float4(col[0], col[1], col[2], col[3]);
+    *reinterpret_cast<int4 *>(p.occ + o) = make_int4(oc[0], oc[1], oc[2], oc[3]);
+  } else if constexpr (VPT == 2) {
+    *reinterpret_cast<float2 *>(p.tsdf + o) = make_float2(ts[0], ts[1]);
+    *reinterpret_cast<float2 *>(p.weight + o) = make_float2(w[0], w[1]);
+    *reinterpret_cast<float2 *>(p.colorv + o) = make_float2(col[0], col[1]);
+    *reinterpret_cast<int2 *>(p.occ + o) = make_int2(oc[0], oc[1]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < VPT; j++) {
+      p.tsdf[o + j] = ts[j];
+      p.weight[o + j] = w[j];
+      p.colorv[o + j] = col[j];
+      p.occ[o + j] = oc[j];
+    }
+  }
+  return cnt;
+}
+
+// Linear order: thread g takes voxels [g*VPT, g*VPT + VPT) of the frame.
+template <int VPT>
+__global__ void __launch_bounds__(256) fuse_tsdf_kernel(FuseParams p) {
+  __shared__ float s_K[kMaxViews][9];
+  __shared__ float s_P[kMaxViews][12];
+  const int b = blockIdx.y;
+  load_cameras(p, b, s_K, s_P);
+  const FuseFrame f = fuse_frame(p, b);
+  const long groups = f.vol / VPT;
   int cnt = 0;
   for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < groups; g += (long)gridDim.x * blockDim.x) {
     long v0 = g * VPT;
@@ -212,55 +296,39 @@ __global__ void __launch_bounds__(256) fuse_tsdf_kernel(FuseParams p) {
     long rem = v0 - (long)x * p.Dy * p.Dz;
     int y = (int)(rem / p.Dz);
     int z0 = (int)(rem - (long)y * p.Dz);
-    float px = __fmaf_rn((float)x, vs, bx);
-    float py = __fmaf_rn((float)y, vs, by);
-    float pz[VPT], ts[VPT], w[VPT], col[VPT];
-#pragma unroll
-    for (int j = 0; j < VPT; j++) {
-      pz[j] = __fmaf_rn((float)(z0 + j), vs, bz);
-      ts[j] = 1.0f;
-      w[j] = 0.0f;
-      col[j] = 0.0f;
-    }
-    for (int k = 0; k < p.N; k++) {
-      const float *P = s_P[k];
-      const float *Kk = s_K[k];
-      float ax = __fmaf_rn(P[0], px, P[1] * py);
-      float ay = __fmaf_rn(P[4], px, P[5] * py);
-      float az = __fmaf_rn(P[8], px, P[9] * py);
-      const float *dimg = p.depth + ((size_t)b * p.N + k) * img;
-      const float *cimg = p.color + ((size_t)b * p.N + k) * img;
-#pragma unroll
-      for (int j = 0; j < VPT; j++)
-        integrate_view(Kk, P, ax, ay, az, pz[j], dimg, cimg, p.H, p.W, trunc, p.obs_weight, ts[j],
-                       w[j], col[j]);
-    }
-    int oc[VPT];
-#pragma unroll
-    for (int j = 0; j < VPT; j++) {
-      bool o = ts[j] < hi_th && ts[j] > lo_th;
-      oc[j] = o ? (int)(v0 + j) : -1;
-      cnt += o;
-    }
-    size_t o = (size_t)b * vol + v0;
-    if constexpr (VPT == 4) {
-      *reinterpret_cast<float4 *>(p.tsdf + o) = make_float4(ts[0], ts[1], ts[2], ts[3]);
-      *reinterpret_cast<float4 *>(p.weight + o) = make_float4(w[0], w[1], w[2], w[3]);
-      *reinterpret_cast<float4 *>(p.colorv + o) = make_float4(col[0], col[1], col[2], col[3]);
-      *reinterpret_cast<int4 *>(p.occ + o) = make_int4(oc[0], oc[1], oc[2], oc[3]);
-    } else if constexpr (VPT == 2) {
-      *reinterpret_cast<float2 *>(p.tsdf + o) = make_float2(ts[0], ts[1]);
-      *reinterpret_cast<float2 *>(p.weight + o) = make_float2(w[0], w[1]);
-      *reinterpret_cast<float2 *>(p.colorv + o) = make_float2(col[0], col[1]);
-      *reinterpret_cast<int2 *>(p.occ + o) = make_int2(oc[0], oc[1]);
-    } else {
-#pragma unroll
-      for (int j = 0; j < VPT; j++) {
-        p.tsdf[o + j] = ts[j];
-        p.weight[o + j] = w[j];
-        p.colorv[o + j] = col[j];
-        p.occ[o + j] = oc[j];
-      }
+    cnt += fuse_group<VPT>(p, f, s_K, s_P, x, y, z0);
+  }
+  cnt = warp_sum(cnt);
+  if (lane_id() == 0 && cnt) atomicAdd(p.count + b, cnt);
+}
+
+// Tiled order: a CTA of 256 threads fuses a 16 x 16 x 16 voxel tile, as four
+// passes of 4 (x) x 16 (y) x 16 (z) voxels, each thread 4 consecutive z.  The
+// voxels of one tile project to one compact patch of every view, so the
+// depth/colour gathers of the tile reuse L1 lines (a linear run of z voxels
+// projects to a line of distinct pixels instead).  Tiles are taken z-fastest
+// so CTAs resident at the same time work on neighbouring tiles.
+constexpr int kTileEdge = 16;
+
+__global__ void __launch_bounds__(256) fuse_tsdf_tiled_kernel(FuseParams p, int tiles_y, int tiles_z,
+                                                              long n_tiles) {
+  __shared__ float s_K[kMaxViews][9];
+  __shared__ float s_P[kMaxViews][12];
+  const int b = blockIdx.y;
+  load_cameras(p, b, s_K, s_P);
+  const FuseFrame f = fuse_frame(p, b);
+  const int tz = threadIdx.x & 3, ty = (threadIdx.x >> 2) & 15, tx = threadIdx.x >> 6;
+  int cnt = 0;
+  for (long t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    const int Tz = (int)(t % tiles_z);
+    const long r = t / tiles_z;
+    const int Ty = (int)(r % tiles_y), Tx = (int)(r / tiles_y);
+    const int y = Ty * kTileEdge + ty, z0 = Tz * kTileEdge + tz * 4;
+    if (y >= p.Dy || z0 >= p.Dz) continue;
+#pragma unroll 1
+    for (int pass = 0; pass < kTileEdge / 4; pass++) {
+      const int x = Tx * kTileEdge + pass * 4 + tx;
+      if (x < p.Dx) cnt += fuse_group<4>(p, f, s_K, s_P, x, y, z0);
     }
   }
   cnt = warp_sum(cnt);
@@ -299,9 +367,17 @@ extern "C" int sg_fuse_tsdf(const float *K, const float *RT, const float *color,
   FuseParams p{K, RT, color, depth, vol_bbox, voxel_size, tsdf, weight, colorv, occ, count,
                N, H, W, Dx, Dy, Dz, obs_weight, trunc_weight, th_low, th_high};
   long vol = (long)Dx * Dy * Dz;
+  const uintptr_t ptrs = ((uintptr_t)tsdf) | ((uintptr_t)weight) | ((uintptr_t)colorv) | ((uintptr_t)occ);
+  if (tune(SG_TUNE_FUSE_TILED) && Dz % 4 == 0 && ptrs % 16 == 0) {
+    const int ty = ceil_div(Dy, kTileEdge), tz = ceil_div(Dz, kTileEdge);
+    const long n_tiles = (long)ceil_div(Dx, kTileEdge) * ty * tz;
+    const int gx = n_tiles < 65535L * 16 ? (int)n_tiles : 65535 * 16;
+    fuse_tsdf_tiled_kernel<<<dim3(gx, B), 256, 0, stream>>>(p, ty, tz, n_tiles);
+    SG_LAUNCH_CHECK();
+    return SG_OK;
+  }
   int vpt = tune(SG_TUNE_FUSE_VPT);
   const int blk = tune(SG_TUNE_FUSE_BLOCK);
-  const uintptr_t ptrs = ((uintptr_t)tsdf) | ((uintptr_t)weight) | ((uintptr_t)colorv) | ((uintptr_t)occ);
   while (vpt > 1 && (Dz % vpt != 0 || ptrs % (4 * vpt) != 0)) vpt >>= 1;
   const int gx = ceil_div(vol / vpt, blk);
   if (vpt == 4) fuse_tsdf_kernel<4><<<dim3(gx, B), blk, 0, stream>>>(p);

@@ -409,16 +409,18 @@ def test_fusion_paths_bit_exact(obs, views, frac_colour):
     assert np.array_equal(occ.cpu().numpy(), ref["occ"])
 
 
-def test_launch_shapes_do_not_change_results():
-    """Every autotuner knob value gives bit-identical outputs."""
+@pytest.mark.parametrize("D", [64, 72])
+def test_launch_shapes_do_not_change_results(D):
+    """Every autotuner knob value gives bit-identical outputs (D = 72: the
+    16^3 fusion tiles are partial at the grid's far faces)."""
     from sailor_gb300 import autotune
     from sailor_gb300.dist import VoxelEncoding as VE
-    D = 64
     sc = syn.make_scene(seed=51, n_views=4, res=128, n_prims=8, D=D, trunc=0.03)
     saved = autotune.current()
     outs = []
     try:
-        for vpt, blk in ((1, 64), (2, 128), (4, 256)):
+        for tiled, vpt, blk in ((1, 4, 128), (0, 1, 64), (0, 2, 128), (0, 4, 256)):
+            autotune.set_knob("fuse_tiled", tiled)
             autotune.set_knob("fuse_vpt", vpt)
             autotune.set_knob("fuse_block", blk)
             occ = torch.full((1, D, D, D), -1, dtype=torch.int32, device="cuda")
