@@ -144,8 +144,45 @@ struct FuseParams {
   float obs_weight, trunc_weight, th_low, th_high;
 };
 
+// Approximate reciprocal of the hardware (PTX rcp.approx.ftz.f32: at most
+// 1 ulp relative error for normal inputs).
+__device__ __forceinline__ float rcp_approx(float b) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(b));
+  return r;
+}
+
+// roundf(a / b) (half away from zero), exactly as the IEEE quotient would
+// round, given r = rcp_approx(b).  q = a * r is within 1.5 * 2^-23 |q| of
+// a / b, so q and a / b round to the same integer unless a half-integer lies
+// within that distance; the test below keeps a margin of 4.8e-7 |q| + 6e-8
+// (2.7x the bound, plus the rounding of q - floor(q) for -1 < q < 0).  Near a
+// tie, for |q| >= 2^20, a non-finite q, or b outside [1e-30, 1e30] the IEEE
+// quotient decides.
+__device__ __forceinline__ float round_div(float a, float b, float r) {
+  const float q = a * r;
+  const float aq = fabsf(q), ab = fabsf(b);
+  const float fl = floorf(q);
+  const float d = q - fl;
+  if (aq < 1048576.0f && ab >= 1.0e-30f && ab <= 1.0e30f && fabsf(d - 0.5f) > __fmaf_rn(aq, 4.8e-7f, 6.0e-8f))
+    return copysignf(d > 0.5f ? fl + 1.0f : fl, q);
+  return roundf(a / b);
+}
+
+// x / w: a product with the exact reciprocal when w is a power of two in
+// [2^-126, 2^126] (x * 2^-e and x / 2^e are the same real number, rounded
+// once), else the IEEE quotient.
+__device__ __forceinline__ float div_weight(float x, float w) {
+  const unsigned wb = __float_as_uint(w);
+  if ((wb & 0x807fffffu) == 0u && wb - 0x00800000u <= 0x7e000000u) return x * __uint_as_float(0x7f000000u - wb);
+  return x / w;
+}
+
 // Integrate one view into the running state of one voxel (the body of the
-// view loop of integrate_cuda, fusion_kernel.cu:279-332).
+// view loop of integrate_cuda, fusion_kernel.cu:279-332).  Every value is
+// the one the reference computes; the divisions take the exact shortcuts
+// above (rounded quotients from the approximate reciprocal, power-of-two
+// weights, and dist = 1 when diff >= trunc > 0, where diff / trunc >= 1).
 __device__ __forceinline__ void integrate_view(const float *__restrict__ Kk, const float *__restrict__ P,
                                                float ax, float ay, float az, float pz,
                                                const float *__restrict__ dimg,
@@ -157,34 +194,36 @@ __device__ __forceinline__ void integrate_view(const float *__restrict__ Kk, con
   float cx = __fmaf_rn(P[2], pz, ax) + P[3];
   float cy = __fmaf_rn(P[6], pz, ay) + P[7];
   float cz = __fmaf_rn(P[10], pz, az) + P[11];
+  if (cz < 0.0f) return;  // rejected by the reference after the pixel test
   float ux = dot3c(Kk[0], Kk[1], Kk[2], cx, cy, cz);
   float uy = dot3c(Kk[3], Kk[4], Kk[5], cx, cy, cz);
   float uz = dot3c(Kk[6], Kk[7], Kk[8], cx, cy, cz);
-  ux = ux / uz;
-  uy = uy / uz;
-  int pxi = (int)roundf(ux), pyi = (int)roundf(uy);
-  if (pxi < 0 || pxi >= W || pyi < 0 || pyi >= H || cz < 0) return;
+  const float ru = rcp_approx(uz);
+  int pxi = (int)round_div(ux, uz, ru), pyi = (int)round_div(uy, uz, ru);
+  if (pxi < 0 || pxi >= W || pyi < 0 || pyi >= H) return;
   size_t pidx = (size_t)pyi * W + pxi;
   float dv = __ldg(dimg + pidx);
   if (dv < 0.1f || dv > 4.0f) return;
   float diff = dv - cz;
   if (diff < -trunc) return;
-  float dist = fminf(1.0f, diff / trunc);
+  float dist = (diff >= trunc && trunc > 0.0f) ? 1.0f : fminf(1.0f, diff / trunc);
   float w_old = w, w_new = w_old + obs;
   w = w_new;
   // (tsdf*w_old + obs*dist)/w_new: nvcc fuses the second product
-  ts = __fmaf_rn(obs, dist, ts * w_old) / w_new;
+  ts = div_weight(__fmaf_rn(obs, dist, ts * w_old), w_new);
   // packed colour b*65536 + g*256 + r: integer-valued floats, exact steps
-  float old_b = floorf(col / 65536.0f);
-  float old_g = floorf((col - old_b * 256.0f * 256.0f) / 256.0f);
+  // (products with 2^-16 and 2^-8 are the reference's exact divisions)
+  float old_b = floorf(col * (1.0f / 65536.0f));
+  float old_g = floorf((col - old_b * 256.0f * 256.0f) * (1.0f / 256.0f));
   float old_r = col - old_b * 256.0f * 256.0f - old_g * 256.0f;
   float nc = __ldg(cimg + pidx);
-  float nb = floorf(nc / 65536.0f);
-  float ng = floorf((nc - nb * 256.0f * 256.0f) / 256.0f);
+  float nb = floorf(nc * (1.0f / 65536.0f));
+  float ng = floorf((nc - nb * 256.0f * 256.0f) * (1.0f / 256.0f));
   float nr = nc - nb * 256.0f * 256.0f - ng * 256.0f;
-  nb = fminf(roundf(__fmaf_rn(old_b, w_old, obs * nb) / w_new), 255.0f);
-  ng = fminf(roundf(__fmaf_rn(old_g, w_old, obs * ng) / w_new), 255.0f);
-  nr = fminf(roundf(__fmaf_rn(old_r, w_old, obs * nr) / w_new), 255.0f);
+  const float rw = rcp_approx(w_new);
+  nb = fminf(round_div(__fmaf_rn(old_b, w_old, obs * nb), w_new, rw), 255.0f);
+  ng = fminf(round_div(__fmaf_rn(old_g, w_old, obs * ng), w_new, rw), 255.0f);
+  nr = fminf(round_div(__fmaf_rn(old_r, w_old, obs * nr), w_new, rw), 255.0f);
   col = nb * 256.0f * 256.0f + ng * 256.0f + nr;
 }
 
