@@ -258,6 +258,22 @@ int sg_grid_gather(const float *ori, const float *dir, const float *z, int B,
                    const float *vol_bbox, const float *voxel_size, int mode,
                    float scale, float s, float *out, sg_stream_t stream);
 
+/* Adjoint of sg_grid_gather: grad_grid [B, D, D, D, C] += the sum over the
+ * samples of the trilinear corner weights times grad_out [B*N, S, C]
+ * (mode 0), or, for mode 1 (C == 1), times grad_out * d sigma / d t at the
+ * TSDF value the forward gathered (grid is read again to recompute it).
+ * grad_grid is accumulated into, not overwritten.  Per ray, consecutive
+ * samples in one trilinear cell are summed first; the per-cell sums of all
+ * rays then meet in atomic adds, whose order is not fixed, so the last bits
+ * can differ between runs.  No counterpart in the reference: its trilinear
+ * backward (c_lib/VoxelEncoding/src/sampling_kernel.cu:237-327) returns
+ * per-corner gradients of per-node features and scatters into no grid. */
+int sg_grid_scatter(const float *ori, const float *dir, const float *z, int B,
+                    int N, int S, const float *grad_out, const float *grid,
+                    int D, int C, const float *vol_bbox,
+                    const float *voxel_size, int mode, float scale, float s,
+                    float *grad_grid, sg_stream_t stream);
+
 /* Node-corner trilinear aggregation.  Replaces
  * MultiLayerOctree::trilinear_aggregate_features(_backward)
  * (sampling_kernel.cu:162-327, 1384-1462).  ori/dir [B,N,3],

@@ -21,6 +21,7 @@ EXPORTS = (
     "sg_sample_coarse", "sg_sort_samples", "sg_composite_fwd", "sg_composite_bwd",
     "sg_trilerp_nodes_fwd", "sg_trilerp_nodes_bwd", "sg_sample_sorted", "sg_grid_gather",
     "sg_render_fused", "sg_tune_set", "sg_tune_get", "sg_tree_build_static",
+    "sg_grid_scatter",
 )
 
 
@@ -60,6 +61,7 @@ def _load():
     lib.sg_composite_bwd.argtypes = [p] * 12 + [i, i, i, f, i, i, p, p, p]
     lib.sg_sample_sorted.argtypes = [C.POINTER(SgTree), p, p, p, p, i, i, p, f, p, i, i, i, p, p, p]
     lib.sg_grid_gather.argtypes = [p, p, p, i, i, i, p, i, i, p, p, i, f, f, p, p]
+    lib.sg_grid_scatter.argtypes = [p, p, p, i, i, i, p, p, i, i, p, p, i, f, f, p, p]
     lib.sg_render_fused.argtypes = [C.POINTER(SgTree), p, p, p, p, i, i, p, f, p, i, i, i, p, p, p, i, f, f, p, i,
                                     p, p, f, p, p, p, p, p, p, p]
     lib.sg_tune_set.argtypes = [i, i]

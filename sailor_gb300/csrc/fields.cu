@@ -13,10 +13,21 @@
 // depth-sorted), so HBM traffic is about the touched grid bytes plus the
 // 4*C output bytes and 4-byte depth per sample.
 //
+// grid_scatter_kernel (the adjoint): one warp per ray walks the ray's
+// samples in order; lane l owns the (corner, channel) slots l, l+32, ... of
+// the 8*C values a trilinear cell receives.  While consecutive samples stay in
+// one cell their contributions w_corner * g_channel accumulate in registers;
+// at a cell change (and at the end of the ray) the slots are flushed with one
+// atomic add each, C consecutive lanes covering one corner's C contiguous
+// channels.  Samples of a ray are depth-sorted and cluster in the few hit
+// voxels, so a flush carries many samples.
+//
 // mode 1 turns a gathered normalised TSDF t (C == 1) into a density
 // sigma = sigmoid(-t * scale / s) / s  (scale = truncation margin in metres,
 // s = the density's length scale), so the gather is fused with the field
 // transform that feeds compositing.
+#include <climits>
+
 #include "ray_core.cuh"
 
 namespace sg {
@@ -57,6 +68,119 @@ __global__ void __launch_bounds__(256) grid_gather_kernel(GatherParams p) {
   }
 }
 
+
+struct ScatterParams {
+  const float *ori, *dir, *z;
+  long R;
+  int N, S;
+  const float *gout;   // [R, S, C]
+  const float *grid;   // mode 1: the TSDF grid the forward gathered from
+  int D;
+  const float *vol_bbox, *voxel_size;
+  int mode;
+  float scale, s;
+  float *ggrid;        // [B, D, D, D, C], accumulated
+};
+
+template <int C>
+__device__ __forceinline__ void scatter_flush(const ScatterParams &p, int b, const int cell[3],
+                                              const float (&acc)[(8 * C + 31) / 32]) {
+  constexpr int NSLOT = (8 * C + 31) / 32;
+  const int lane = lane_id();
+#pragma unroll
+  for (int q = 0; q < NSLOT; q++) {
+    const int slot = lane + 32 * q;
+    if (slot >= 8 * C || acc[q] == 0.0f) continue;
+    const int cr = slot / C, ch = slot - cr * C;
+    const int ix = cell[0] + ((cr >> 2) & 1), iy = cell[1] + ((cr >> 1) & 1), iz = cell[2] + (cr & 1);
+    if (ix < 0 || iy < 0 || iz < 0 || ix >= p.D || iy >= p.D || iz >= p.D) continue;
+    atomicAdd(p.ggrid + ((((size_t)b * p.D + ix) * p.D + iy) * p.D + iz) * C + ch, acc[q]);
+  }
+}
+
+template <int C>
+__global__ void __launch_bounds__(256) grid_scatter_kernel(ScatterParams p) {
+  constexpr int NSLOT = (8 * C + 31) / 32;
+  __shared__ float s_w[8][32][9];      // padded rows: conflict-free per-lane writes
+  __shared__ float s_g[8][32][C + 1];
+  __shared__ int s_cell[8][32][5];
+  const int lane = lane_id(), w8 = threadIdx.x >> 5;
+  for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < p.R;
+       r += ((long)gridDim.x * blockDim.x) >> 5) {
+    const int b = (int)(r / p.N);
+    const float *bb = p.vol_bbox + 6 * b;
+    const float bmin[3] = {bb[0], bb[2], bb[4]};
+    const float vs = __ldg(p.voxel_size + b);
+    float acc[NSLOT];
+#pragma unroll
+    for (int q = 0; q < NSLOT; q++) acc[q] = 0.0f;
+    int cur[3] = {INT_MIN, 0, 0};
+    for (int c0 = 0; c0 < p.S; c0 += 32) {
+      // per sample: cell, corner weights (as the forward tap forms them) and gradient
+      const int i = c0 + lane;
+      const float zz = i < p.S ? __ldg(p.z + r * p.S + i) : -1.0f;
+      int valid = 0;
+      if (zz >= 0.0f) {
+        float pt[3], f[3];
+        int i0[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+          pt[a] = __fmaf_rn(__ldg(p.dir + r * 3 + a), zz, __ldg(p.ori + r * 3 + a));
+          const float u = (pt[a] - bmin[a]) / vs;
+          const float fl = floorf(u);
+          i0[a] = (int)fl;
+          f[a] = u - fl;
+        }
+#pragma unroll
+        for (int cr = 0; cr < 8; cr++) {
+          const int dx = (cr >> 2) & 1, dy = (cr >> 1) & 1, dz = cr & 1;
+          s_w[w8][lane][cr] = (dx ? f[0] : 1.0f - f[0]) * (dy ? f[1] : 1.0f - f[1]) * (dz ? f[2] : 1.0f - f[2]);
+        }
+        s_cell[w8][lane][0] = i0[0];
+        s_cell[w8][lane][1] = i0[1];
+        s_cell[w8][lane][2] = i0[2];
+        const float *g = p.gout + ((size_t)r * p.S + i) * C;
+        if (p.mode == 1) {
+          // d sigma / d t of sigma = sigmoid(-t scale / s) / s at the gathered t
+          float t1[1];
+          grid_tap<1>(p.grid + (size_t)b * p.D * p.D * p.D, p.D, bmin, vs, pt, t1);
+          const float sg = 1.0f / (1.0f + __expf(t1[0] * p.scale / p.s));
+          s_g[w8][lane][0] = __ldg(g) * (-sg * (1.0f - sg) * p.scale / (p.s * p.s));
+        } else {
+#pragma unroll
+          for (int c = 0; c < C; c++) s_g[w8][lane][c] = __ldg(g + c);
+        }
+        valid = 1;
+      }
+      s_cell[w8][lane][3] = valid;
+      __syncwarp();
+      const int n = min(32, p.S - c0);
+      for (int j = 0; j < n; j++) {
+        if (!s_cell[w8][j][3]) continue;
+        const int cj[3] = {s_cell[w8][j][0], s_cell[w8][j][1], s_cell[w8][j][2]};
+        if (cj[0] != cur[0] || cj[1] != cur[1] || cj[2] != cur[2]) {
+          if (cur[0] != INT_MIN) scatter_flush<C>(p, b, cur, acc);
+#pragma unroll
+          for (int q = 0; q < NSLOT; q++) acc[q] = 0.0f;
+          cur[0] = cj[0];
+          cur[1] = cj[1];
+          cur[2] = cj[2];
+        }
+#pragma unroll
+        for (int q = 0; q < NSLOT; q++) {
+          const int slot = lane + 32 * q;
+          if (slot < 8 * C) {
+            const int cr = slot / C, ch = slot - cr * C;
+            acc[q] = __fmaf_rn(s_w[w8][j][cr], s_g[w8][j][ch], acc[q]);
+          }
+        }
+      }
+      __syncwarp();
+    }
+    if (cur[0] != INT_MIN) scatter_flush<C>(p, b, cur, acc);
+  }
+}
+
 }  // namespace sg
 
 using namespace sg;
@@ -77,6 +201,31 @@ extern "C" int sg_grid_gather(const float *ori, const float *dir, const float *z
     case 4: grid_gather_kernel<4><<<g, 256, 0, stream>>>(p); break;
     case 8: grid_gather_kernel<8><<<g, 256, 0, stream>>>(p); break;
     case 16: grid_gather_kernel<16><<<g, 256, 0, stream>>>(p); break;
+    default: return SG_ERR_UNSUPPORTED;
+  }
+  SG_LAUNCH_CHECK();
+  return SG_OK;
+}
+
+extern "C" int sg_grid_scatter(const float *ori, const float *dir, const float *z, int B, int N, int S,
+                               const float *grad_out, const float *grid, int D, int C, const float *vol_bbox,
+                               const float *voxel_size, int mode, float scale, float s, float *grad_grid,
+                               sg_stream_t stream) {
+  if (!ori || !dir || !z || !grad_out || !vol_bbox || !voxel_size || !grad_grid) return SG_ERR_INVALID_ARG;
+  if (B <= 0 || N <= 0 || S <= 0 || D <= 0 || C <= 0 || C > 16) return SG_ERR_INVALID_ARG;
+  if (mode == 1 && (C != 1 || s == 0.0f || !grid)) return SG_ERR_INVALID_ARG;
+  if (mode != 0 && mode != 1) return SG_ERR_INVALID_ARG;
+  ScatterParams p{ori, dir, z, (long)B * N, N, S, grad_out, grid, D, vol_bbox, voxel_size, mode, scale, s,
+                  grad_grid};
+  long R = (long)B * N;
+  int g = ceil_div(R * 32, 256);
+  if (g > 152 * 32) g = 152 * 32;
+  switch (C) {
+    case 1: grid_scatter_kernel<1><<<g, 256, 0, stream>>>(p); break;
+    case 3: grid_scatter_kernel<3><<<g, 256, 0, stream>>>(p); break;
+    case 4: grid_scatter_kernel<4><<<g, 256, 0, stream>>>(p); break;
+    case 8: grid_scatter_kernel<8><<<g, 256, 0, stream>>>(p); break;
+    case 16: grid_scatter_kernel<16><<<g, 256, 0, stream>>>(p); break;
     default: return SG_ERR_UNSUPPORTED;
   }
   SG_LAUNCH_CHECK();
