@@ -312,6 +312,110 @@ int sg_render_fused(const SgTree *tree, const int *hit_idx,
                     float *out_ws, float *out_alpha, float *out_z,
                     int *out_node, sg_stream_t stream);
 
+/* ---- batched launches over segment tables -------------------------------- */
+/* Many frames, views and target cameras of uneven sizes go through one
+ * launch per stage.  No reference counterpart: the reference runs one frame
+ * and one target view per call sequence (SRONet/BasicRenNet.py:170-318). */
+
+/* Views of B frames with uneven counts and resolutions (device arrays).
+ * Frame b owns views [view_begin[b], view_begin[b+1]) (at most 32); view v
+ * has K [3,3] and RT [3,4] at K + 9v / RT + 12v and an H x W image
+ * (view_hw[2v], view_hw[2v+1]) starting at element view_offset[v] of the
+ * packed depth / colour buffers. */
+typedef struct SgViews {
+  int max_views;                /* most views of one frame (host value, <= 32) */
+  const int *view_begin;        /* [B+1]           */
+  const int *view_hw;           /* [n_views, 2]    */
+  const long long *view_offset; /* [n_views]       */
+  const float *K;               /* [n_views, 3, 3] */
+  const float *RT;              /* [n_views, 3, 4] */
+  const float *depth;           /* packed images   */
+  const float *color;           /* packed images   */
+} SgViews;
+
+/* Ray segments (device arrays): segment s (one target camera) owns rays
+ * [ray_begin[s], ray_begin[s+1]) of the packed ray buffers; they look into
+ * frame frame[s] of the tree and grids and take samples[s] samples per ray
+ * (at most the S of the launch). */
+typedef struct SgRaySegments {
+  int count;
+  int total;            /* rays of all segments (= ray_begin[count]) */
+  const int *ray_begin; /* [count+1] */
+  const int *frame;     /* [count]   */
+  const int *samples;   /* [count]   */
+} SgRaySegments;
+
+/* Inputs of the batched render.  Rays ori/dir [R,3]; hit rows [R,W] with
+ * hit_count [R] and valid_len [R] from sg_intersect_segments; sample jitter
+ * from rands [R,S] if given, else a hash of (rand_seed, ray, position) if
+ * rand_seed != 0, else rand_const.  Density sigma = sigmoid(-t * sdf_scale /
+ * sdf_s) / sdf_s of the trilinear TSDF t (tsdf [B,D,D,D] over the tree's
+ * vol_bbox / voxel_size); colour = head [3,C] x trilinear features of feat
+ * [B,Df,Df,Df,C] over feat_bbox / feat_vs (head NULL: C == 3 and colour =
+ * features).  C is 3 or 16. */
+typedef struct SgRenderArgs {
+  const float *ori, *dir;
+  const int *hit_idx;
+  const float *hit_t0, *hit_t1;
+  const int *hit_count;
+  const float *valid_len;
+  int W;
+  int S;
+  const float *rands;
+  float rand_const;
+  unsigned long long rand_seed;
+  const float *tsdf;
+  int D;
+  float sdf_scale, sdf_s;
+  const float *feat;
+  int Df, C;
+  const float *feat_bbox, *feat_vs;
+  const float *head;
+  float t_thres;
+} SgRenderArgs;
+
+/* sg_fuse_tsdf over a view table: frame b fuses its own views into volume
+ * b of tsdf / weight / colorv / occ [B,D,D,D]; count [B] += occupied. */
+int sg_fuse_tsdf_views(const SgViews *views, int B, int D,
+                       const float *vol_bbox, const float *voxel_size,
+                       float obs_weight, float trunc_weight, float th_low,
+                       float th_high, float *tsdf, float *weight,
+                       float *colorv, int *occ, int *count,
+                       sg_stream_t stream);
+
+/* sg_intersect (compact rows, inference mode) over ray segments: ray r of
+ * segment s traverses frame frame[s] of the tree. */
+int sg_intersect_segments(const SgTree *tree, const SgRaySegments *seg,
+                          const float *ori, const float *dir, int W,
+                          int *hit_idx, float *hit_t0, float *hit_t1,
+                          float *valid_len, int *hit_count,
+                          SgStatus *status, sg_stream_t stream);
+
+/* Forward of the batched render (as sg_render_fused, per segment):
+ * out_rgb [R,3], out_depth / out_ws / out_alpha [R]; out_z / out_node
+ * [R,S] (both NULL or both set) receive the sorted samples. */
+int sg_render_segments_fwd(const SgTree *tree, const SgRaySegments *seg,
+                           const SgRenderArgs *args, float *out_rgb,
+                           float *out_depth, float *out_ws, float *out_alpha,
+                           float *out_z, int *out_node, sg_stream_t stream);
+
+/* Backward of the batched render.  Per ray it recomputes samples, sort,
+ * field taps, alpha and transmittance from the same inputs (nothing is saved
+ * by the forward), forms the exact adjoint of compositing for upstream
+ * gradients g_rgb [R,3], g_depth / g_ws / g_alpha [R] (any may be NULL =
+ * 0), and accumulates (+=) the gradient of the feature grid into grad_feat
+ * [B,Df,Df,Df,C] and of the TSDF grid into grad_tsdf [B,D,D,D] (either may
+ * be NULL) -- per ray, consecutive samples in one trilinear cell are summed
+ * before one atomic add per cell corner and channel.  grad_sigma [R,S] /
+ * grad_rgb [R,S,3] (both NULL or both set) receive the per-sample gradients
+ * by sorted position. */
+int sg_render_segments_bwd(const SgTree *tree, const SgRaySegments *seg,
+                           const SgRenderArgs *args, const float *g_rgb,
+                           const float *g_depth, const float *g_ws,
+                           const float *g_alpha, float *grad_feat,
+                           float *grad_tsdf, float *grad_sigma,
+                           float *grad_rgb, sg_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

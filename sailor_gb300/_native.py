@@ -21,7 +21,8 @@ EXPORTS = (
     "sg_sample_coarse", "sg_sort_samples", "sg_composite_fwd", "sg_composite_bwd",
     "sg_trilerp_nodes_fwd", "sg_trilerp_nodes_bwd", "sg_sample_sorted", "sg_grid_gather",
     "sg_render_fused", "sg_tune_set", "sg_tune_get", "sg_tree_build_static",
-    "sg_grid_scatter",
+    "sg_grid_scatter", "sg_fuse_tsdf_views", "sg_intersect_segments", "sg_render_segments_fwd",
+    "sg_render_segments_bwd",
 )
 
 
@@ -31,6 +32,26 @@ class SgTree(C.Structure):
                 ("brick_node", C.c_void_p), ("brick_mask", C.c_void_p), ("top_key", C.c_void_p),
                 ("top_child_base", C.c_void_p), ("bot_key", C.c_void_p), ("bot_parent", C.c_void_p),
                 ("counts", C.c_void_p), ("voxel_size", C.c_void_p), ("vol_bbox", C.c_void_p)]
+
+
+class SgViews(C.Structure):
+    _fields_ = [("max_views", C.c_int), ("view_begin", C.c_void_p), ("view_hw", C.c_void_p),
+                ("view_offset", C.c_void_p), ("K", C.c_void_p), ("RT", C.c_void_p), ("depth", C.c_void_p),
+                ("color", C.c_void_p)]
+
+
+class SgRaySegments(C.Structure):
+    _fields_ = [("count", C.c_int), ("total", C.c_int), ("ray_begin", C.c_void_p), ("frame", C.c_void_p),
+                ("samples", C.c_void_p)]
+
+
+class SgRenderArgs(C.Structure):
+    _fields_ = [("ori", C.c_void_p), ("dir", C.c_void_p), ("hit_idx", C.c_void_p), ("hit_t0", C.c_void_p),
+                ("hit_t1", C.c_void_p), ("hit_count", C.c_void_p), ("valid_len", C.c_void_p), ("W", C.c_int),
+                ("S", C.c_int), ("rands", C.c_void_p), ("rand_const", C.c_float), ("rand_seed", C.c_ulonglong),
+                ("tsdf", C.c_void_p), ("D", C.c_int), ("sdf_scale", C.c_float), ("sdf_s", C.c_float),
+                ("feat", C.c_void_p), ("Df", C.c_int), ("C", C.c_int), ("feat_bbox", C.c_void_p),
+                ("feat_vs", C.c_void_p), ("head", C.c_void_p), ("t_thres", C.c_float)]
 
 
 def _load():
@@ -64,6 +85,11 @@ def _load():
     lib.sg_grid_scatter.argtypes = [p, p, p, i, i, i, p, p, i, i, p, p, i, f, f, p, p]
     lib.sg_render_fused.argtypes = [C.POINTER(SgTree), p, p, p, p, i, i, p, f, p, i, i, i, p, p, p, i, f, f, p, i,
                                     p, p, f, p, p, p, p, p, p, p]
+    T, V, G, A = C.POINTER(SgTree), C.POINTER(SgViews), C.POINTER(SgRaySegments), C.POINTER(SgRenderArgs)
+    lib.sg_fuse_tsdf_views.argtypes = [V, i, i, p, p, f, f, f, f, p, p, p, p, p, p]
+    lib.sg_intersect_segments.argtypes = [T, G, p, p, i, p, p, p, p, p, p, p]
+    lib.sg_render_segments_fwd.argtypes = [T, G, A, p, p, p, p, p, p, p]
+    lib.sg_render_segments_bwd.argtypes = [T, G, A, p, p, p, p, p, p, p, p, p]
     lib.sg_tune_set.argtypes = [i, i]
     lib.sg_tune_get.argtypes = [i]
     lib.sg_trilerp_nodes_fwd.argtypes = [C.POINTER(SgTree), p, p, p, p, p, i, i, i, p, p]

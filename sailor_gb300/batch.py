@@ -1,0 +1,259 @@
+"""Batched fusion, tree build, intersection and render over many frames and
+target cameras of uneven sizes, one launch per stage.
+
+``BatchPipeline`` keeps every buffer resident in HBM, sized once for a fixed
+layout of frames (views of uneven count and resolution) and target cameras
+(uneven ray counts and sample counts).  Each stage is one persistent launch
+over all frames / all rays, indexed by segment tables:
+
+* fusion: ``sg_fuse_tsdf_views`` over the view table (per-view image offsets
+  and sizes);
+* coarse occupancy and tree: ``sg_brick_occupancy`` / ``sg_tree_build`` over
+  the frame axis;
+* intersection: ``sg_intersect_segments`` (each ray's frame from its target's
+  segment);
+* render: ``sg_render_segments_fwd`` (per-ray outputs only) and
+  ``sg_render_segments_bwd`` (recomputes each ray, exact compositing adjoint,
+  gradients scattered into the per-frame feature and TSDF grids).
+
+``train_step`` runs the whole step (build, intersect, forward, an L2 loss
+gradient against target colours, backward) with no allocation, so it can be
+captured once in a CUDA graph (``capture``) and replayed.
+
+The colour model is a dense per-frame feature grid [B, D, D, D, C] with a
+fixed linear head [3, C] (the stand-in for SRONet's MLP); density comes from
+the fused TSDF grid.  No reference counterpart as one object: the reference
+runs one frame and one target view per call sequence
+(SRONet/BasicRenNet.py:170-318).
+"""
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _native as N
+
+
+class BatchPipeline:
+    def __init__(self, view_hw, targets, D=256, rate=8, C=16, W_hits=64, device="cuda"):
+        """view_hw: per frame, a list of (H, W) per view.  targets: list of
+        (frame, n_rays, S)."""
+        self.B = B = len(view_hw)
+        self.D, self.rate, self.C, self.W = D, rate, C, W_hits
+        self.Dt = D // rate
+        if self.Dt * rate != D or D % 4:
+            raise ValueError("D must be a multiple of rate and of 4")
+        self.dev = dev = torch.device(device)
+        f32 = dict(dtype=torch.float32, device=dev)
+        i32 = dict(dtype=torch.int32, device=dev)
+        # views
+        nv = [len(v) for v in view_hw]
+        if max(nv) > 32:
+            raise ValueError("at most 32 views per frame")
+        self.views_hw = [tuple(map(int, hw)) for v in view_hw for hw in v]
+        V = len(self.views_hw)
+        sizes = [h * w for h, w in self.views_hw]
+        offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        self.view_pix = int(offs[-1])
+        self.view_begin = torch.tensor(np.concatenate([[0], np.cumsum(nv)]), **i32)
+        self.view_hw_t = torch.tensor(np.array(self.views_hw, np.int32).reshape(-1), **i32)
+        self.view_off = torch.tensor(offs[:-1], dtype=torch.int64, device=dev)
+        self._view_slices = [(int(offs[k]), int(offs[k + 1])) for k in range(V)]
+        self.K = torch.zeros((V, 3, 3), **f32)
+        self.RT = torch.zeros((V, 3, 4), **f32)
+        self.depth = torch.zeros(self.view_pix, **f32)
+        self.color = torch.zeros(self.view_pix, **f32)
+        self.views = N.SgViews(max(nv), N.ptr(self.view_begin), N.ptr(self.view_hw_t), N.ptr(self.view_off),
+                               N.ptr(self.K), N.ptr(self.RT), N.ptr(self.depth), N.ptr(self.color))
+        # volumes and tree
+        Vol, Vt = B * D ** 3, B * self.Dt ** 3
+        self.vol_bbox = torch.zeros((B, 3, 2), **f32)
+        self.voxel_size = torch.zeros(B, **f32)
+        self.tsdf = torch.empty((B, D, D, D), **f32)
+        self.weight = torch.empty((B, D, D, D), **f32)
+        self.colorv = torch.empty((B, D, D, D), **f32)
+        self.occ0 = torch.empty((B, D, D, D), **i32)
+        self.occ1 = torch.empty((B, self.Dt, self.Dt, self.Dt), **i32)
+        self.cnt = torch.zeros((2, B), **i32)
+        mw = N.mask_words(rate)
+        self.brick_node = torch.empty(Vt, **i32)
+        self.brick_mask = torch.empty(Vt * mw, **i32)
+        self.top_key = torch.empty(Vt, **i32)
+        self.top_child_base = torch.empty(Vt, **i32)
+        self.bot_key = torch.empty(Vol, **i32)
+        self.bot_parent = torch.empty(Vol, **i32)
+        self.counts = torch.zeros(2, **i32)
+        self.scratch = torch.empty(int(N.lib.sg_tree_scratch_bytes(B, self.Dt)), dtype=torch.uint8, device=dev)
+        self.status = torch.zeros(4, **i32)
+        self.tree = N.SgTree(B, self.Dt, D, rate, Vol, 0, Vt, Vol, N.ptr(self.brick_node), N.ptr(self.brick_mask),
+                             N.ptr(self.top_key), N.ptr(self.top_child_base), N.ptr(self.bot_key),
+                             N.ptr(self.bot_parent), N.ptr(self.counts), N.ptr(self.voxel_size),
+                             N.ptr(self.vol_bbox))
+        # rays and segments
+        self.targets = [(int(f), int(n), int(s)) for f, n, s in targets]
+        T = len(self.targets)
+        counts = [n for _, n, _ in self.targets]
+        rb = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+        if rb[-1] >= 2 ** 31:
+            raise ValueError("at most 2^31 - 1 rays per launch")
+        self.R = R = int(rb[-1])
+        self.S = S = max(s for _, _, s in self.targets)
+        self.ray_slices = [(int(rb[t]), int(rb[t + 1])) for t in range(T)]
+        self.seg_begin = torch.tensor(rb.astype(np.int32), **i32)
+        self.seg_frame = torch.tensor([f for f, _, _ in self.targets], **i32)
+        self.seg_samples = torch.tensor([s for _, _, s in self.targets], **i32)
+        self.seg = N.SgRaySegments(T, R, N.ptr(self.seg_begin), N.ptr(self.seg_frame), N.ptr(self.seg_samples))
+        self.ori = torch.zeros((R, 3), **f32)
+        self.dirs = torch.zeros((R, 3), **f32)
+        self.hit_idx = torch.empty((R, W_hits), **i32)
+        self.hit_t0 = torch.empty((R, W_hits), **f32)
+        self.hit_t1 = torch.empty((R, W_hits), **f32)
+        self.hit_count = torch.empty(R, **i32)
+        self.valid_len = torch.empty(R, **f32)
+        # fields, outputs, gradients
+        self.feat = torch.zeros((B, D, D, D, C), **f32)
+        self.head = torch.zeros((3, C), **f32)
+        self.grad_feat = torch.zeros((B, D, D, D, C), **f32)
+        self.grad_tsdf = torch.zeros((B, D, D, D), **f32)
+        self.out_rgb = torch.empty((R, 3), **f32)
+        self.out_depth = torch.empty(R, **f32)
+        self.out_ws = torch.empty(R, **f32)
+        self.out_alpha = torch.empty(R, **f32)
+        self.target_rgb = torch.zeros((R, 3), **f32)
+        self.g_rgb = torch.empty((R, 3), **f32)
+        self.args = None
+        self.trunc_weight = None
+        self.events = None
+
+    # ------------------------------------------------------------------ inputs
+    def load_views(self, frames, vol_bbox, voxel_size, trunc_weight):
+        """frames: per frame dict(K, RT, depth, color) lists of per-view arrays
+        in the layout given to the constructor."""
+        k = 0
+        for fr in frames:
+            for v in range(len(fr["K"])):
+                a, b = self._view_slices[k]
+                h, w = self.views_hw[k]
+                if fr["depth"][v].shape != (h, w):
+                    raise ValueError("view resolution differs from the layout")
+                self.K[k].copy_(torch.as_tensor(fr["K"][v]))
+                self.RT[k].copy_(torch.as_tensor(fr["RT"][v]))
+                self.depth[a:b].copy_(torch.as_tensor(fr["depth"][v]).reshape(-1))
+                self.color[a:b].copy_(torch.as_tensor(fr["color"][v]).reshape(-1))
+                k += 1
+        self.vol_bbox.copy_(torch.as_tensor(vol_bbox))
+        self.voxel_size.copy_(torch.as_tensor(voxel_size).reshape(-1))
+        self.trunc_weight = float(trunc_weight)
+
+    def load_rays(self, rays):
+        """rays: per target (ori [n,3], dir [n,3])."""
+        for (a, b), (o, d) in zip(self.ray_slices, rays):
+            self.ori[a:b].copy_(torch.as_tensor(o))
+            self.dirs[a:b].copy_(torch.as_tensor(d))
+
+    def set_fields(self, feat=None, head=None, target_rgb=None):
+        if feat is not None:
+            self.feat.copy_(feat)
+        if head is not None:
+            self.head.copy_(head)
+        if target_rgb is not None:
+            self.target_rgb.copy_(target_rgb)
+
+    def render_args(self, trunc_metres, sdf_s=0.005, t_thres=1e-4, rand_seed=0, rand_const=0.5):
+        """Fix the render's scalar parameters (trunc_metres: the truncation
+        margin in metres; sdf_s: the density's length scale)."""
+        self.args = N.SgRenderArgs(
+            N.ptr(self.ori), N.ptr(self.dirs), N.ptr(self.hit_idx), N.ptr(self.hit_t0), N.ptr(self.hit_t1),
+            N.ptr(self.hit_count), N.ptr(self.valid_len), self.W, self.S, None, float(rand_const),
+            int(rand_seed), N.ptr(self.tsdf), self.D, float(trunc_metres), float(sdf_s), N.ptr(self.feat), self.D,
+            self.C, N.ptr(self.vol_bbox), N.ptr(self.voxel_size), N.ptr(self.head) if self.C != 3 else None,
+            float(t_thres))
+        return self.args
+
+    def _mark(self, name):
+        if self.events is not None:
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record()
+            self.events.append((name, ev))
+
+    # ------------------------------------------------------------------ stages
+    def build(self, obs_weight=1.0, th_low=13.5, th_high=13.5):
+        st = N.stream()
+        self.cnt.zero_()
+        self.status.zero_()
+        self._mark("start")
+        N.check(N.lib.sg_fuse_tsdf_views(C.byref(self.views), self.B, self.D, N.ptr(self.vol_bbox),
+                                         N.ptr(self.voxel_size), float(obs_weight), self.trunc_weight,
+                                         float(th_low), float(th_high), N.ptr(self.tsdf), N.ptr(self.weight),
+                                         N.ptr(self.colorv), N.ptr(self.occ0), N.ptr(self.cnt[0]), st),
+                "fuse_tsdf_views")
+        self._mark("fusion")
+        N.check(N.lib.sg_brick_occupancy(N.ptr(self.occ0), self.B, self.D, self.rate, N.ptr(self.occ1),
+                                         N.ptr(self.cnt[1]), st), "brick_occupancy")
+        N.check(N.lib.sg_tree_build(C.byref(self.tree), N.ptr(self.occ1), N.ptr(self.occ0), N.ptr(self.scratch),
+                                    self.scratch.numel(), N.ptr(self.status), st), "tree_build")
+        self._mark("tree")
+
+    def intersect(self):
+        N.check(N.lib.sg_intersect_segments(C.byref(self.tree), C.byref(self.seg), N.ptr(self.ori),
+                                            N.ptr(self.dirs), self.W, N.ptr(self.hit_idx), N.ptr(self.hit_t0),
+                                            N.ptr(self.hit_t1), N.ptr(self.valid_len), N.ptr(self.hit_count),
+                                            N.ptr(self.status), N.stream()), "intersect_segments")
+        self._mark("intersect")
+
+    def forward(self, out_z=None, out_node=None):
+        N.check(N.lib.sg_render_segments_fwd(C.byref(self.tree), C.byref(self.seg), C.byref(self.args),
+                                             N.ptr(self.out_rgb), N.ptr(self.out_depth), N.ptr(self.out_ws),
+                                             N.ptr(self.out_alpha), N.ptr(out_z), N.ptr(out_node), N.stream()),
+                "render_fwd")
+        self._mark("forward")
+        return self.out_rgb, self.out_depth, self.out_ws, self.out_alpha
+
+    def backward(self, g_rgb=None, g_depth=None, g_ws=None, g_alpha=None, grad_sigma=None, grad_rgb=None,
+                 tsdf_grad=True, zero=True):
+        if zero:
+            self.grad_feat.zero_()
+            if tsdf_grad:
+                self.grad_tsdf.zero_()
+        N.check(N.lib.sg_render_segments_bwd(C.byref(self.tree), C.byref(self.seg), C.byref(self.args),
+                                             N.ptr(g_rgb), N.ptr(g_depth), N.ptr(g_ws), N.ptr(g_alpha),
+                                             N.ptr(self.grad_feat), N.ptr(self.grad_tsdf) if tsdf_grad else None,
+                                             N.ptr(grad_sigma), N.ptr(grad_rgb), N.stream()), "render_bwd")
+        self._mark("backward")
+
+    def train_step(self):
+        """Build, intersect, forward, gradient of the mean squared colour error
+        against target_rgb, backward.  Allocates nothing."""
+        self.build()
+        self.intersect()
+        self.forward()
+        torch.sub(self.out_rgb, self.target_rgb, out=self.g_rgb)
+        self.g_rgb.mul_(2.0 / (3.0 * self.R))
+        self.backward(self.g_rgb)
+
+    def capture(self, warmup=2):
+        """CUDA graph of train_step (run it a few times first, then capture)."""
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            for _ in range(warmup):
+                self.train_step()
+        torch.cuda.current_stream().wait_stream(s)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.train_step()
+        return g
+
+    def stage_times(self):
+        torch.cuda.synchronize()
+        out = {}
+        prev = None
+        for name, ev in self.events or []:
+            if prev is not None:
+                out[name] = out.get(name, 0.0) + prev.elapsed_time(ev)
+            prev = ev
+        return out
+
+    def frame_rays(self, t):
+        a, b = self.ray_slices[t]
+        return slice(a, b)

@@ -190,6 +190,29 @@ int tune(int knob);
 }  // namespace sg
 
 // launch-error check used by every entry point
+// Segment of ray r: the last s with begin[s] <= r (begin ascending, n >= 1).
+__device__ __forceinline__ int segment_of(const int *__restrict__ begin, int n, long r) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if ((long)__ldg(begin + mid) <= r) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Uniform [0, 1) jitter from (seed, ray, position): the SplitMix64
+// finaliser (Steele, Lea and Flood, 2014) of a Weyl-sequence key; 24 bits.
+__device__ __forceinline__ float hash_uniform(unsigned long long seed, long r, int q) {
+  unsigned long long x = seed + (unsigned long long)r * 0x9E3779B97F4A7C15ull + (unsigned long long)q;
+  x ^= x >> 30;
+  x *= 0xBF58476D1CE4E5B9ull;
+  x ^= x >> 27;
+  x *= 0x94D049BB133111EBull;
+  x ^= x >> 31;
+  return (float)(x >> 40) * (1.0f / 16777216.0f);
+}
+
 #define SG_LAUNCH_CHECK()                           \
   do {                                              \
     cudaError_t _e = cudaGetLastError();            \

@@ -78,7 +78,8 @@ __device__ __forceinline__ bool load_ray(const CompParams &p, long r, float *s_z
     s_z[i] = st.z[e];
   }
   __syncwarp();
-  ray_alpha<E>(st.z, st.sg, st.valid, S, p.mode, s_z, st.al);
+  float dl[E];
+  ray_alpha<E>(st.z, st.sg, st.valid, S, p.mode, s_z, st.al, dl);
   ray_transmittance<E>(st.al, st.valid, S, p.t_thres, s_f, st.tb, st.proc, st.post);
   return true;
 }

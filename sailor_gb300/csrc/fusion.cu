@@ -142,6 +142,18 @@ struct FuseParams {
   int *occ, *count;
   int N, H, W, Dx, Dy, Dz;
   float obs_weight, trunc_weight, th_low, th_high;
+  // view table (NULL: every frame has N views of H x W at [b, k] of K / RT / images)
+  const int *view_begin, *view_hw;
+  const long long *view_off;
+};
+
+// Cameras and images of one frame's views, staged in shared memory.
+struct ViewSmem {
+  float K[kMaxViews][9];
+  float P[kMaxViews][12];
+  long long off[kMaxViews];
+  int hw[kMaxViews][2];
+  int n;
 };
 
 // Approximate reciprocal of the hardware (PTX rcp.approx.ftz.f32: at most
@@ -231,7 +243,6 @@ __device__ __forceinline__ void integrate_view(const float *__restrict__ Kk, con
 struct FuseFrame {
   int b;
   long vol;
-  size_t img;
   float vs, trunc, bx, by, bz, hi_th, lo_th;
 };
 
@@ -239,7 +250,6 @@ __device__ __forceinline__ FuseFrame fuse_frame(const FuseParams &p, int b) {
   FuseFrame f;
   f.b = b;
   f.vol = (long)p.Dx * p.Dy * p.Dz;
-  f.img = (size_t)p.H * p.W;
   f.vs = p.voxel_size[b];
   f.trunc = f.vs * p.trunc_weight;
   f.bx = p.vol_bbox[b * 6 + 0];
@@ -250,21 +260,42 @@ __device__ __forceinline__ FuseFrame fuse_frame(const FuseParams &p, int b) {
   return f;
 }
 
-// Cameras of frame b into shared memory (all threads of the CTA take part).
-__device__ __forceinline__ void load_cameras(const FuseParams &p, int b, float (*s_K)[9], float (*s_P)[12]) {
-  for (int i = threadIdx.x; i < p.N * 21; i += blockDim.x) {
-    int v = i / 21, k = i - v * 21;
-    if (k < 9) s_K[v][k] = p.K[(size_t)(b * p.N + v) * 9 + k];
-    else s_P[v][k - 9] = p.RT[(size_t)(b * p.N + v) * 12 + (k - 9)];
+// Cameras and image placement of frame b's views into shared memory (all
+// threads of the CTA take part).
+__device__ __forceinline__ void load_views(const FuseParams &p, int b, ViewSmem &vw) {
+  int v0, n;
+  if (p.view_begin) {
+    v0 = __ldg(p.view_begin + b);
+    n = min(__ldg(p.view_begin + b + 1) - v0, kMaxViews);
+  } else {
+    v0 = b * p.N;
+    n = p.N;
   }
+  for (int i = threadIdx.x; i < n * 21; i += blockDim.x) {
+    int v = i / 21, k = i - v * 21;
+    if (k < 9) vw.K[v][k] = p.K[(size_t)(v0 + v) * 9 + k];
+    else vw.P[v][k - 9] = p.RT[(size_t)(v0 + v) * 12 + (k - 9)];
+  }
+  for (int v = threadIdx.x; v < n; v += blockDim.x) {
+    if (p.view_begin) {
+      vw.off[v] = p.view_off[v0 + v];
+      vw.hw[v][0] = p.view_hw[2 * (v0 + v)];
+      vw.hw[v][1] = p.view_hw[2 * (v0 + v) + 1];
+    } else {
+      vw.off[v] = (long long)(v0 + v) * p.H * p.W;
+      vw.hw[v][0] = p.H;
+      vw.hw[v][1] = p.W;
+    }
+  }
+  if (threadIdx.x == 0) vw.n = n;
   __syncthreads();
 }
 
 // Fuse the VPT z-consecutive voxels (x, y, z0 .. z0+VPT-1) over all views and
 // store them; returns how many of them are occupied.
 template <int VPT>
-__device__ __forceinline__ int fuse_group(const FuseParams &p, const FuseFrame &f, const float (*s_K)[9],
-                                          const float (*s_P)[12], int x, int y, int z0) {
+__device__ __forceinline__ int fuse_group(const FuseParams &p, const FuseFrame &f, const ViewSmem &vw, int x,
+                                          int y, int z0) {
   const long v0 = ((long)x * p.Dy + y) * p.Dz + z0;
   float px = __fmaf_rn((float)x, f.vs, f.bx);
   float py = __fmaf_rn((float)y, f.vs, f.by);
@@ -276,18 +307,18 @@ __device__ __forceinline__ int fuse_group(const FuseParams &p, const FuseFrame &
     w[j] = 0.0f;
     col[j] = 0.0f;
   }
-  for (int k = 0; k < p.N; k++) {
-    const float *P = s_P[k];
-    const float *Kk = s_K[k];
+  for (int k = 0; k < vw.n; k++) {
+    const float *P = vw.P[k];
+    const float *Kk = vw.K[k];
     float ax = __fmaf_rn(P[0], px, P[1] * py);
     float ay = __fmaf_rn(P[4], px, P[5] * py);
     float az = __fmaf_rn(P[8], px, P[9] * py);
-    const float *dimg = p.depth + ((size_t)f.b * p.N + k) * f.img;
-    const float *cimg = p.color + ((size_t)f.b * p.N + k) * f.img;
+    const float *dimg = p.depth + vw.off[k];
+    const float *cimg = p.color + vw.off[k];
+    const int H = vw.hw[k][0], W = vw.hw[k][1];
 #pragma unroll
     for (int j = 0; j < VPT; j++)
-      integrate_view(Kk, P, ax, ay, az, pz[j], dimg, cimg, p.H, p.W, f.trunc, p.obs_weight, ts[j], w[j],
-                     col[j]);
+      integrate_view(Kk, P, ax, ay, az, pz[j], dimg, cimg, H, W, f.trunc, p.obs_weight, ts[j], w[j], col[j]);
   }
   int oc[VPT], cnt = 0;
 #pragma unroll
@@ -322,10 +353,9 @@ __device__ __forceinline__ int fuse_group(const FuseParams &p, const FuseFrame &
 // Linear order: thread g takes voxels [g*VPT, g*VPT + VPT) of the frame.
 template <int VPT>
 __global__ void __launch_bounds__(256) fuse_tsdf_kernel(FuseParams p) {
-  __shared__ float s_K[kMaxViews][9];
-  __shared__ float s_P[kMaxViews][12];
+  __shared__ ViewSmem vw;
   const int b = blockIdx.y;
-  load_cameras(p, b, s_K, s_P);
+  load_views(p, b, vw);
   const FuseFrame f = fuse_frame(p, b);
   const long groups = f.vol / VPT;
   int cnt = 0;
@@ -335,7 +365,7 @@ __global__ void __launch_bounds__(256) fuse_tsdf_kernel(FuseParams p) {
     long rem = v0 - (long)x * p.Dy * p.Dz;
     int y = (int)(rem / p.Dz);
     int z0 = (int)(rem - (long)y * p.Dz);
-    cnt += fuse_group<VPT>(p, f, s_K, s_P, x, y, z0);
+    cnt += fuse_group<VPT>(p, f, vw, x, y, z0);
   }
   cnt = warp_sum(cnt);
   if (lane_id() == 0 && cnt) atomicAdd(p.count + b, cnt);
@@ -351,10 +381,9 @@ constexpr int kTileEdge = 16;
 
 __global__ void __launch_bounds__(256) fuse_tsdf_tiled_kernel(FuseParams p, int tiles_y, int tiles_z,
                                                               long n_tiles) {
-  __shared__ float s_K[kMaxViews][9];
-  __shared__ float s_P[kMaxViews][12];
+  __shared__ ViewSmem vw;
   const int b = blockIdx.y;
-  load_cameras(p, b, s_K, s_P);
+  load_views(p, b, vw);
   const FuseFrame f = fuse_frame(p, b);
   const int tz = threadIdx.x & 3, ty = (threadIdx.x >> 2) & 15, tx = threadIdx.x >> 6;
   int cnt = 0;
@@ -367,7 +396,7 @@ __global__ void __launch_bounds__(256) fuse_tsdf_tiled_kernel(FuseParams p, int 
 #pragma unroll 1
     for (int pass = 0; pass < kTileEdge / 4; pass++) {
       const int x = Tx * kTileEdge + pass * 4 + tx;
-      if (x < p.Dx) cnt += fuse_group<4>(p, f, s_K, s_P, x, y, z0);
+      if (x < p.Dx) cnt += fuse_group<4>(p, f, vw, x, y, z0);
     }
   }
   cnt = warp_sum(cnt);
@@ -393,21 +422,11 @@ extern "C" int sg_auto_bbox(const float *depth, const float *K, const float *R, 
   return SG_OK;
 }
 
-extern "C" int sg_fuse_tsdf(const float *K, const float *RT, const float *color, const float *depth, int B,
-                            int N, int H, int W, int Dx, int Dy, int Dz, const float *vol_bbox,
-                            const float *voxel_size, float obs_weight, float trunc_weight, float th_low,
-                            float th_high, float *tsdf, float *weight, float *colorv, int *occ,
-                            int *count, sg_stream_t stream) {
-  if (!K || !RT || !color || !depth || !vol_bbox || !voxel_size || !tsdf || !weight || !colorv || !occ ||
-      !count)
-    return SG_ERR_INVALID_ARG;
-  if (B <= 0 || N <= 0 || N > kMaxViews || H <= 0 || W <= 0 || Dx <= 0 || Dy <= 0 || Dz <= 0)
-    return SG_ERR_INVALID_ARG;
-  FuseParams p{K, RT, color, depth, vol_bbox, voxel_size, tsdf, weight, colorv, occ, count,
-               N, H, W, Dx, Dy, Dz, obs_weight, trunc_weight, th_low, th_high};
+static int launch_fuse(const FuseParams &p, int B, sg_stream_t stream) {
+  const int Dx = p.Dx, Dy = p.Dy, Dz = p.Dz;
   long vol = (long)Dx * Dy * Dz;
-  const uintptr_t ptrs = ((uintptr_t)tsdf) | ((uintptr_t)weight) | ((uintptr_t)colorv) | ((uintptr_t)occ);
-  if (tune(SG_TUNE_FUSE_TILED) && Dz % 4 == 0 && ptrs % 16 == 0) {
+  const uintptr_t ptrs = ((uintptr_t)p.tsdf) | ((uintptr_t)p.weight) | ((uintptr_t)p.colorv) | ((uintptr_t)p.occ);
+  if (p.view_begin || (tune(SG_TUNE_FUSE_TILED) && Dz % 4 == 0 && ptrs % 16 == 0)) {
     const int ty = ceil_div(Dy, kTileEdge), tz = ceil_div(Dz, kTileEdge);
     const long n_tiles = (long)ceil_div(Dx, kTileEdge) * ty * tz;
     const int gx = n_tiles < 65535L * 16 ? (int)n_tiles : 65535 * 16;
@@ -424,4 +443,36 @@ extern "C" int sg_fuse_tsdf(const float *K, const float *RT, const float *color,
   else fuse_tsdf_kernel<1><<<dim3(gx, B), blk, 0, stream>>>(p);
   SG_LAUNCH_CHECK();
   return SG_OK;
+}
+
+extern "C" int sg_fuse_tsdf(const float *K, const float *RT, const float *color, const float *depth, int B,
+                            int N, int H, int W, int Dx, int Dy, int Dz, const float *vol_bbox,
+                            const float *voxel_size, float obs_weight, float trunc_weight, float th_low,
+                            float th_high, float *tsdf, float *weight, float *colorv, int *occ,
+                            int *count, sg_stream_t stream) {
+  if (!K || !RT || !color || !depth || !vol_bbox || !voxel_size || !tsdf || !weight || !colorv || !occ ||
+      !count)
+    return SG_ERR_INVALID_ARG;
+  if (B <= 0 || N <= 0 || N > kMaxViews || H <= 0 || W <= 0 || Dx <= 0 || Dy <= 0 || Dz <= 0)
+    return SG_ERR_INVALID_ARG;
+  FuseParams p{K, RT, color, depth, vol_bbox, voxel_size, tsdf, weight, colorv, occ, count,
+               N, H, W, Dx, Dy, Dz, obs_weight, trunc_weight, th_low, th_high, nullptr, nullptr, nullptr};
+  return launch_fuse(p, B, stream);
+}
+
+extern "C" int sg_fuse_tsdf_views(const SgViews *views, int B, int D, const float *vol_bbox,
+                                  const float *voxel_size, float obs_weight, float trunc_weight, float th_low,
+                                  float th_high, float *tsdf, float *weight, float *colorv, int *occ, int *count,
+                                  sg_stream_t stream) {
+  if (!views || !views->view_begin || !views->view_hw || !views->view_offset || !views->K || !views->RT ||
+      !views->depth || !views->color || !vol_bbox || !voxel_size || !tsdf || !weight || !colorv || !occ || !count)
+    return SG_ERR_INVALID_ARG;
+  if (B <= 0 || D <= 0 || D % 4 != 0) return SG_ERR_INVALID_ARG;
+  if (views->max_views > kMaxViews) return SG_ERR_UNSUPPORTED;
+  if ((((uintptr_t)tsdf) | ((uintptr_t)weight) | ((uintptr_t)colorv) | ((uintptr_t)occ)) % 16 != 0)
+    return SG_ERR_INVALID_ARG;
+  FuseParams p{views->K, views->RT, views->color, views->depth, vol_bbox, voxel_size, tsdf, weight, colorv, occ,
+               count, 0, 0, 0, D, D, D, obs_weight, trunc_weight, th_low, th_high, views->view_begin,
+               views->view_hw, views->view_offset};
+  return launch_fuse(p, B, stream);
 }

@@ -29,16 +29,19 @@ struct IsectParams {
   float *hit_t0, *hit_t1, *valid_len;
   int *hit_count;
   SgStatus *st;
+  long R;                               // rays of the launch
+  int nseg;                             // 0: frames of N rays; else ray segments
+  const int *seg_begin, *seg_frame;
 };
 
 __global__ void __launch_bounds__(512) intersect_kernel(IsectParams p) {
   const SgTree &t = p.t;
-  const long R = (long)t.B * p.N;
+  const long R = p.R;
   const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
   int cnt = 0;
   bool over = false;
   if (r < R) {
-    const int b = (int)(r / p.N);
+    const int b = p.nseg > 0 ? __ldg(p.seg_frame + segment_of(p.seg_begin, p.nseg, r)) : (int)(r / p.N);
     const float *bb = t.vol_bbox + 6 * b;
     const float bmin[3] = {bb[0], bb[2], bb[4]};
     const float xc = (bb[0] + bb[1]) / 2.0f, yc = (bb[2] + bb[3]) / 2.0f, zc = (bb[4] + bb[5]) / 2.0f;
@@ -251,9 +254,9 @@ extern "C" int sg_intersect(const SgTree *tree, const float *ori, const float *d
   if (padded && !hit_count) return SG_ERR_INVALID_ARG;
   if (padded && (((uintptr_t)hit_idx) | ((uintptr_t)hit_t0) | ((uintptr_t)hit_t1)) % 16 != 0)
     return SG_ERR_INVALID_ARG;
-  IsectParams p{*tree, ori, dir, N, W, th_early_stop, opt_num, is_training,
-                hit_idx, hit_t0, hit_t1, valid_len, hit_count, status};
   long R = (long)tree->B * N;
+  IsectParams p{*tree, ori, dir, N, W, th_early_stop, opt_num, is_training,
+                hit_idx, hit_t0, hit_t1, valid_len, hit_count, status, R, 0, nullptr, nullptr};
   const int blk = tune(SG_TUNE_ISECT_BLOCK);
   intersect_kernel<<<ceil_div(R, blk), blk, 0, stream>>>(p);
   if (padded) {
@@ -261,6 +264,22 @@ extern "C" int sg_intersect(const SgTree *tree, const float *ori, const float *d
     if (g > 152 * 64) g = 152 * 64;
     pad_rows_kernel<<<g, 256, 0, stream>>>(R, W, hit_count, hit_idx, hit_t0, hit_t1);
   }
+  SG_LAUNCH_CHECK();
+  return SG_OK;
+}
+
+extern "C" int sg_intersect_segments(const SgTree *tree, const SgRaySegments *seg, const float *ori,
+                                     const float *dir, int W, int *hit_idx, float *hit_t0, float *hit_t1,
+                                     float *valid_len, int *hit_count, SgStatus *status, sg_stream_t stream) {
+  if (!tree || !seg || !ori || !dir || !hit_idx || !hit_t0 || !hit_t1 || !valid_len || !hit_count)
+    return SG_ERR_INVALID_ARG;
+  if (seg->count <= 0 || seg->total < 0 || !seg->ray_begin || !seg->frame) return SG_ERR_INVALID_ARG;
+  if (W <= 0 || tree->B <= 0 || tree->Dt <= 0 || tree->Db != tree->Dt * tree->rate) return SG_ERR_INVALID_ARG;
+  if (seg->total == 0) return SG_OK;
+  IsectParams p{*tree, ori, dir, 1, W, -1, -1, 0, hit_idx, hit_t0, hit_t1, valid_len, hit_count, status,
+                (long)seg->total, seg->count, seg->ray_begin, seg->frame};
+  const int blk = tune(SG_TUNE_ISECT_BLOCK);
+  intersect_kernel<<<ceil_div((long)seg->total, blk), blk, 0, stream>>>(p);
   SG_LAUNCH_CHECK();
   return SG_OK;
 }

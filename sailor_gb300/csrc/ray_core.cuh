@@ -18,6 +18,7 @@ struct SampleParams {
   int N, W, S, num_levels, start_level;
   int *sampled_idx;
   float *sampled_z;
+  unsigned long long seed;  // rands == NULL and seed != 0: hashed jitter
 };
 
 // Warp-private shared scratch of the sampler.
@@ -42,14 +43,17 @@ __device__ __forceinline__ float sample_z(float mn, float off, int j, float rnd)
 // samples are generated position-parallel: the owner of position q is the
 // last hit whose range starts at or before q (starts are non-decreasing and
 // strictly increasing over hits that get samples).  Returns #samples.
-__device__ __forceinline__ int warp_sample_ray(const SampleParams &p, long r, int nh, float rand_const,
-                                               float *sz, int *si, SampleScratch &sc) {
+// b: the ray's frame; S: its sample count (<= p.S, the row stride of rands).
+__device__ __forceinline__ int warp_sample_ray(const SampleParams &p, long r, int b, int S, int nh,
+                                               float rand_const, float *sz, int *si, SampleScratch &sc) {
   const int lane = lane_id();
-  const int S = p.S;
-  const int b = (int)(r / p.N);
   const int *hi = p.hit_idx + (size_t)r * p.W;
   const float *h0 = p.hit_t0 + (size_t)r * p.W, *h1 = p.hit_t1 + (size_t)r * p.W;
-  const float *rd = p.rands ? p.rands + (size_t)r * S : nullptr;
+  const float *rd = p.rands ? p.rands + (size_t)r * p.S : nullptr;
+  const unsigned long long seed = p.seed;
+  auto jitter = [&](int q) {
+    return rd ? __ldg(rd + q) : (seed ? hash_uniform(seed, r, q) : rand_const);
+  };
   int done = 0;
   if (nh > 0 && __ldg(hi) >= 0) {
     const float vl = p.valid_len[r];
@@ -97,7 +101,7 @@ __device__ __forceinline__ int warp_sample_ray(const SampleParams &p, long r, in
           if (sc.start[mid] <= q) lo = mid;
           else up = mid - 1;
         }
-        sz[q] = sample_z(sc.mn[lo], sc.off[lo], q - sc.start[lo], rd ? __ldg(rd + q) : rand_const);
+        sz[q] = sample_z(sc.mn[lo], sc.off[lo], q - sc.start[lo], jitter(q));
         si[q] = sc.id[lo];
       }
       __syncwarp();
@@ -113,7 +117,7 @@ __device__ __forceinline__ int warp_sample_ray(const SampleParams &p, long r, in
       const float off = (mx - mn) * 0.5f;
       const float base = mn + off;
       const int q = has + i;
-      sz[q] = sum3_rn(base, -(off * 0.5f), off * (rd ? __ldg(rd + q) : rand_const));
+      sz[q] = sum3_rn(base, -(off * 0.5f), off * jitter(q));
       si[q] = id;
     }
     done = has + cnt;
@@ -224,7 +228,7 @@ __device__ __forceinline__ void warp_sort_samples(float *sz, int *spos, int S, i
 // sorted position.  Invalid positions (z < 0) get alpha 0.
 template <int E>
 __device__ __forceinline__ void ray_alpha(const float (&z)[E], const float (&sg)[E], unsigned valid, int S,
-                                          int mode, const float *s_z, float (&al)[E]) {
+                                          int mode, const float *s_z, float (&al)[E], float (&dl)[E]) {
   const int lane = lane_id();
   if (mode == 0) {
     unsigned gtz[E];
@@ -234,6 +238,7 @@ __device__ __forceinline__ void ray_alpha(const float (&z)[E], const float (&sg)
     for (int e = 0; e < E; e++) {
       const int i = e * 32 + lane;
       al[e] = 0.0f;
+      dl[e] = 0.0f;
       if ((valid >> e) & 1u) {
         float delta;
         if (i == S - 1) {
@@ -250,12 +255,16 @@ __device__ __forceinline__ void ray_alpha(const float (&z)[E], const float (&sg)
           }
           delta = s_z[m] - z[e];
         }
+        dl[e] = delta;
         al[e] = 1.0f - __expf(-sg[e] * delta);
       }
     }
   } else {
 #pragma unroll
-    for (int e = 0; e < E; e++) al[e] = ((valid >> e) & 1u) ? sg[e] : 0.0f;
+    for (int e = 0; e < E; e++) {
+      al[e] = ((valid >> e) & 1u) ? sg[e] : 0.0f;
+      dl[e] = 0.0f;
+    }
   }
 }
 
@@ -327,10 +336,10 @@ __device__ __forceinline__ void ray_transmittance(const float (&al)[E], unsigned
 // dense-grid trilinear tap (grid [D,D,D,C] channel-last of one frame, voxel
 // (x,y,z) centred at bbox_min + (x,y,z) * vs, outside corners contribute 0)
 // ---------------------------------------------------------------------------
-template <int C>
-__device__ __forceinline__ void grid_tap(const float *__restrict__ grid, int D, const float bmin[3], float vs,
-                                         const float pt[3], float (&acc)[C]) {
-  int i0[3];
+// Cell (lower corner index) and the eight corner weights of a trilinear tap
+// at pt; corner cr = (dx, dy, dz) = bits (2, 1, 0) of cr.
+__device__ __forceinline__ void tap_cell(const float bmin[3], float vs, const float pt[3], int (&i0)[3],
+                                         float (&w)[8]) {
   float f[3];
 #pragma unroll
   for (int a = 0; a < 3; a++) {
@@ -340,16 +349,34 @@ __device__ __forceinline__ void grid_tap(const float *__restrict__ grid, int D, 
     f[a] = u - fl;
   }
 #pragma unroll
+  for (int cr = 0; cr < 8; cr++) {
+    const int dx = (cr >> 2) & 1, dy = (cr >> 1) & 1, dz = cr & 1;
+    w[cr] = (dx ? f[0] : 1.0f - f[0]) * (dy ? f[1] : 1.0f - f[1]) * (dz ? f[2] : 1.0f - f[2]);
+  }
+}
+
+__device__ __forceinline__ bool corner_inside(const int (&i0)[3], int cr, int D, size_t &off) {
+  const int ix = i0[0] + ((cr >> 2) & 1), iy = i0[1] + ((cr >> 1) & 1), iz = i0[2] + (cr & 1);
+  if (ix < 0 || iy < 0 || iz < 0 || ix >= D || iy >= D || iz >= D) return false;
+  off = ((size_t)ix * D + iy) * D + iz;
+  return true;
+}
+
+template <int C>
+__device__ __forceinline__ void grid_tap(const float *__restrict__ grid, int D, const float bmin[3], float vs,
+                                         const float pt[3], float (&acc)[C]) {
+  int i0[3];
+  float w[8];
+  tap_cell(bmin, vs, pt, i0, w);
+#pragma unroll
   for (int c = 0; c < C; c++) acc[c] = 0.0f;
 #pragma unroll
   for (int cr = 0; cr < 8; cr++) {
-    const int dx = (cr >> 2) & 1, dy = (cr >> 1) & 1, dz = cr & 1;
-    const int ix = i0[0] + dx, iy = i0[1] + dy, iz = i0[2] + dz;
-    if (ix < 0 || iy < 0 || iz < 0 || ix >= D || iy >= D || iz >= D) continue;
-    const float w = (dx ? f[0] : 1.0f - f[0]) * (dy ? f[1] : 1.0f - f[1]) * (dz ? f[2] : 1.0f - f[2]);
-    const float *g = grid + (((size_t)ix * D + iy) * D + iz) * C;
+    size_t off;
+    if (!corner_inside(i0, cr, D, off)) continue;
+    const float *g = grid + off * C;
 #pragma unroll
-    for (int c = 0; c < C; c++) acc[c] = __fmaf_rn(w, __ldg(g + c), acc[c]);
+    for (int c = 0; c < C; c++) acc[c] = __fmaf_rn(w[cr], __ldg(g + c), acc[c]);
   }
 }
 

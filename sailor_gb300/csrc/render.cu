@@ -1,125 +1,181 @@
-// render.cu -- fused per-ray render: sampling -> sort -> field taps -> compositing.
+// render.cu -- fused per-ray render and its adjoint: sampling -> sort -> field
+// taps -> compositing, forward and backward in one kernel each.
 //
 // One warp per ray does, without leaving the SM:
 //   the reference's coarse sampling (ray_voxels_sampling_uniform_kernel,
 //   sampling_kernel.cu:1070-1177) into shared memory, the per-ray sort
 //   (sort_samplings :1308-1329) in registers, per-sample density from the
-//   fused TSDF grid and colour from a dense RGB grid (trilinear taps; the
-//   stand-in for SRONet's MLP), and density compositing of the sorted
-//   samples (volume_rendering_training_forward_kernel, volume_rendering.cu:
-//   17-126, with the transmittance carried in strict sample order).
-// Only 24 bytes per ray are written (rgb, depth, weight sum, alpha); the
-// sorted depths / node ids are written only when requested.  The results
-// equal the unfused chain sg_sample_sorted -> sg_grid_gather (x2) ->
-// sg_composite_fwd on the same inputs (same operations, same order).
+//   fused TSDF grid and colour from a dense feature grid (trilinear taps and
+//   a linear colour head; the stand-in for SRONet's MLP), and density
+//   compositing of the sorted samples (volume_rendering_training_forward_
+//   kernel, volume_rendering.cu:17-126, with the transmittance carried in
+//   strict sample order).
+// The forward writes 24 bytes per ray (rgb, depth, weight sum, alpha); the
+// sorted depths / node ids only when requested.  With a 3-channel colour
+// grid and no head its results equal the unfused chain sg_sample_sorted ->
+// sg_grid_gather (x2) -> sg_composite_fwd on the same inputs.
+//
+// The backward saves nothing from the forward: it re-runs the same per-ray
+// evaluation (same samples, taps, alpha and transmittance, bit for bit),
+// forms the exact adjoint of compositing from in-warp prefix sums, chains
+// it through the density transform and the colour head, and scatters the
+// per-sample gradients into the TSDF and feature grids: lanes own (corner,
+// channel) slots, consecutive samples in one trilinear cell accumulate in
+// registers, and each cell change flushes one atomic add per slot.
+//
+// Launches are persistent grid-stride loops over the rays of all frames and
+// target cameras; a segment table (SgRaySegments) gives each ray its frame
+// and sample count.
+#include <climits>
+
 #include "ray_core.cuh"
 
 namespace sg {
 
 struct RenderParams {
-  SampleParams sp;
+  SampleParams sp;  // tree, hits, jitter, valid_len, N (rays per frame without segments), W, S (row stride)
   const int *hit_count;
   float rand_const;
+  long R;
+  int nseg;  // 0: frames of sp.N rays with sp.S samples each
+  const int *seg_begin, *seg_frame, *seg_samples;
   const float *ori, *dir;
   const float *tsdf;
   int D;
   float sdf_scale, sdf_s;
-  const float *cgrid;
-  int Dc;
-  const float *cbbox, *cvs;
+  const float *feat;
+  int Df;
+  const float *fbbox, *fvs;
+  const float *head;  // [3, C] or null (C == 3)
   float t_thres;
-  float *out_rgb, *out_depth, *out_ws, *out_alpha;
-  float *out_z;
+  float *out_rgb, *out_depth, *out_ws, *out_alpha, *out_z;
   int *out_node;
+  const float *g_rgb, *g_depth, *g_ws, *g_alpha;
+  float *grad_feat, *grad_tsdf, *grad_sigma, *grad_rgb;
 };
 
+__device__ __forceinline__ void ray_frame(const RenderParams &p, long r, int &b, int &S) {
+  if (p.nseg > 0) {
+    const int s = segment_of(p.seg_begin, p.nseg, r);
+    b = __ldg(p.seg_frame + s);
+    S = min(__ldg(p.seg_samples + s), p.sp.S);
+  } else {
+    b = (int)(r / p.sp.N);
+    S = p.sp.S;
+  }
+}
+
 template <int E>
-__global__ void __launch_bounds__(256) render_kernel(RenderParams p) {
-  __shared__ __align__(16) float s_zall[8][32 * E];
-  __shared__ __align__(16) float s_fall[8][32 * E];
-  __shared__ int s_iall[8][32 * E];
-  __shared__ int s_pall[8][32 * E];
-  __shared__ SampleScratch s_sc[8];
-  const int lane = lane_id(), w8 = threadIdx.x >> 5;
-  float *s_z = s_zall[w8];
-  int *s_i = s_iall[w8], *s_p = s_pall[w8];
-  const SampleParams &sp = p.sp;
-  const long R = (long)sp.t.B * sp.N;
-  const int S = sp.S;
-  for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < R;
+struct RayEval {
+  float z[E], sg[E], s01[E], al[E], tb[E], dl[E], rgb[E][3];
+  unsigned valid, proc, post;
+  int done;
+};
+
+// Warp-private shared memory of the render kernels.
+template <int E>
+struct RenderSmem {
+  float *z, *f;
+  int *i, *p;
+  SampleScratch *sc;
+};
+
+// Samples, sort, field taps, alpha and transmittance of ray r (frame b, S
+// samples) into ev; sorted depths stay in sm.z, sorted positions in sm.p.
+template <int E, int C>
+__device__ __forceinline__ void eval_ray(const RenderParams &p, long r, int b, int S, const RenderSmem<E> &sm,
+                                         RayEval<E> &ev) {
+  const int lane = lane_id();
+  const int nh = p.hit_count ? min(__ldg(p.hit_count + r), p.sp.W) : p.sp.W;
+  ev.done = warp_sample_ray(p.sp, r, b, S, nh, p.rand_const, sm.z, sm.i, *sm.sc);
+  ev.valid = ev.proc = ev.post = 0;
+  if (ev.done == 0) return;
+  warp_sort_samples(sm.z, sm.p, S, ev.done);
+  const float *bb = p.sp.t.vol_bbox + 6 * b;
+  const float bmin[3] = {bb[0], bb[2], bb[4]};
+  const float vs = __ldg(p.sp.t.voxel_size + b);
+  const float *fb = p.fbbox + 6 * b;
+  const float fmin[3] = {fb[0], fb[2], fb[4]};
+  const float fvs = __ldg(p.fvs + b);
+  const float *tsdf = p.tsdf + (size_t)b * p.D * p.D * p.D;
+  const float *feat = p.feat + (size_t)b * p.Df * p.Df * p.Df * C;
+  const float o[3] = {__ldg(p.ori + r * 3), __ldg(p.ori + r * 3 + 1), __ldg(p.ori + r * 3 + 2)};
+  const float dr[3] = {__ldg(p.dir + r * 3), __ldg(p.dir + r * 3 + 1), __ldg(p.dir + r * 3 + 2)};
+#pragma unroll
+  for (int e = 0; e < E; e++) {
+    const int i = e * 32 + lane;
+    ev.z[e] = (i < S) ? sm.z[i] : -1.0f;
+    ev.sg[e] = ev.s01[e] = 0.0f;
+    ev.rgb[e][0] = ev.rgb[e][1] = ev.rgb[e][2] = 0.0f;
+    if (ev.z[e] >= 0.0f) {
+      ev.valid |= 1u << e;
+      const float pt[3] = {__fmaf_rn(dr[0], ev.z[e], o[0]), __fmaf_rn(dr[1], ev.z[e], o[1]),
+                           __fmaf_rn(dr[2], ev.z[e], o[2])};
+      float t1[1];
+      grid_tap<1>(tsdf, p.D, bmin, vs, pt, t1);
+      // tsdf_density, with the sigmoid kept for the adjoint
+      ev.s01[e] = 1.0f / (1.0f + __expf(t1[0] * p.sdf_scale / p.sdf_s));
+      ev.sg[e] = ev.s01[e] / p.sdf_s;
+      float fe[C];
+      grid_tap<C>(feat, p.Df, fmin, fvs, pt, fe);
+      if (p.head) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          float a = 0.0f;
+#pragma unroll
+          for (int c = 0; c < C; c++) a = __fmaf_rn(__ldg(p.head + k * C + c), fe[c], a);
+          ev.rgb[e][k] = a;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 3; k++) ev.rgb[e][k] = fe[k < C ? k : 0];
+      }
+    }
+  }
+  ray_alpha<E>(ev.z, ev.sg, ev.valid, S, 0, sm.z, ev.al, ev.dl);
+  ray_transmittance<E>(ev.al, ev.valid, S, p.t_thres, sm.f, ev.tb, ev.proc, ev.post);
+}
+
+#define SG_RENDER_SMEM(E)                         \
+  __shared__ __align__(16) float s_zall[8][32 * E]; \
+  __shared__ __align__(16) float s_fall[8][32 * E]; \
+  __shared__ int s_iall[8][32 * E];                 \
+  __shared__ int s_pall[8][32 * E];                 \
+  __shared__ SampleScratch s_sc[8];                 \
+  const int w8 = threadIdx.x >> 5;                  \
+  const RenderSmem<E> sm{s_zall[w8], s_fall[w8], s_iall[w8], s_pall[w8], &s_sc[w8]};
+
+template <int E, int C>
+__global__ void __launch_bounds__(256) render_fwd_kernel(RenderParams p) {
+  SG_RENDER_SMEM(E)
+  const int lane = lane_id();
+  const int Smax = p.sp.S;
+  for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < p.R;
        r += ((long)gridDim.x * blockDim.x) >> 5) {
-    const int b = (int)(r / sp.N);
-    const int nh = p.hit_count ? min(p.hit_count[r], sp.W) : sp.W;
-    const int done = warp_sample_ray(sp, r, nh, p.rand_const, s_z, s_i, s_sc[w8]);
+    int b, S;
+    ray_frame(p, r, b, S);
+    RayEval<E> ev;
+    eval_ray<E, C>(p, r, b, S, sm, ev);
     float acc_r = 0.0f, acc_g = 0.0f, acc_b = 0.0f, d = 0.0f, ws = 0.0f, aa = 0.0f;
-    if (done == 0) {
-      // no sample: a ray whose largest depth is < 0 renders 0
-      if (p.out_z) {
-        for (int i = lane; i < S; i += 32) {
-          p.out_z[(size_t)r * S + i] = -1.0f;
-          p.out_node[(size_t)r * S + i] = -1;
-        }
+    if (p.out_z) {
+      for (int i = lane; i < Smax; i += 32) {
+        const bool has = ev.done > 0 && i < S;
+        p.out_z[(size_t)r * Smax + i] = has ? sm.z[i] : -1.0f;
+        p.out_node[(size_t)r * Smax + i] = has ? sm.i[sm.p[i]] : -1;
       }
-    } else {
-      warp_sort_samples(s_z, s_p, S, done);
-      float z[E];
-      int node[E];
+    }
+    if (ev.done > 0) {
+      // a ray whose largest depth is < 0 renders 0 (no sample: done == 0)
 #pragma unroll
       for (int e = 0; e < E; e++) {
-        const int i = e * 32 + lane;
-        z[e] = (i < S) ? s_z[i] : -1.0f;
-        node[e] = (i < S) ? s_i[s_p[i]] : -1;
-      }
-      if (p.out_z) {
-#pragma unroll
-        for (int e = 0; e < E; e++) {
-          const int i = e * 32 + lane;
-          if (i < S) {
-            p.out_z[(size_t)r * S + i] = z[e];
-            p.out_node[(size_t)r * S + i] = node[e];
-          }
-        }
-      }
-      const float *bb = sp.t.vol_bbox + 6 * b;
-      const float bmin[3] = {bb[0], bb[2], bb[4]};
-      const float vs = __ldg(sp.t.voxel_size + b);
-      const float *cb = p.cbbox + 6 * b;
-      const float cmin[3] = {cb[0], cb[2], cb[4]};
-      const float cvs = __ldg(p.cvs + b);
-      const float *tsdf = p.tsdf + (size_t)b * p.D * p.D * p.D;
-      const float *cgrid = p.cgrid + (size_t)b * p.Dc * p.Dc * p.Dc * 3;
-      const float o[3] = {__ldg(p.ori + r * 3), __ldg(p.ori + r * 3 + 1), __ldg(p.ori + r * 3 + 2)};
-      const float dr[3] = {__ldg(p.dir + r * 3), __ldg(p.dir + r * 3 + 1), __ldg(p.dir + r * 3 + 2)};
-      unsigned valid = 0;
-      float sg[E], rgb[E][3];
-#pragma unroll
-      for (int e = 0; e < E; e++) {
-        sg[e] = 0.0f;
-        rgb[e][0] = rgb[e][1] = rgb[e][2] = 0.0f;
-        if (z[e] >= 0.0f) {
-          valid |= 1u << e;
-          const float pt[3] = {__fmaf_rn(dr[0], z[e], o[0]), __fmaf_rn(dr[1], z[e], o[1]),
-                               __fmaf_rn(dr[2], z[e], o[2])};
-          float t1[1];
-          grid_tap<1>(tsdf, p.D, bmin, vs, pt, t1);
-          sg[e] = tsdf_density(t1[0], p.sdf_scale, p.sdf_s);
-          grid_tap<3>(cgrid, p.Dc, cmin, cvs, pt, rgb[e]);
-        }
-      }
-      float al[E], tb[E];
-      unsigned proc, post;
-      ray_alpha<E>(z, sg, valid, S, 0, s_z, al);
-      ray_transmittance<E>(al, valid, S, p.t_thres, s_fall[w8], tb, proc, post);
-#pragma unroll
-      for (int e = 0; e < E; e++) {
-        if (((proc & valid) >> e) & 1u) {
-          const float w = al[e] * tb[e];
-          acc_r += w * rgb[e][0];
-          acc_g += w * rgb[e][1];
-          acc_b += w * rgb[e][2];
-          d += w * z[e];
+        if (((ev.proc & ev.valid) >> e) & 1u) {
+          const float w = ev.al[e] * ev.tb[e];
+          acc_r += w * ev.rgb[e][0];
+          acc_g += w * ev.rgb[e][1];
+          acc_b += w * ev.rgb[e][2];
+          d += w * ev.z[e];
           ws += w;
-          aa += w * al[e];
+          aa += w * ev.al[e];
         }
       }
       acc_r = warp_sum(acc_r);
@@ -141,6 +197,283 @@ __global__ void __launch_bounds__(256) render_kernel(RenderParams p) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// backward
+// ---------------------------------------------------------------------------
+// Slots of a lane: feature slots corner * C + channel in [0, 8C), TSDF
+// slots 8C + corner.
+template <int C>
+__device__ __forceinline__ void flush_slots(const RenderParams &p, int b, bool feat_part, const int (&cell)[3],
+                                            float *acc) {
+  constexpr int NF = 8 * C, NSLOT = (NF + 8 + 31) / 32;
+  const int lane = lane_id();
+#pragma unroll
+  for (int q = 0; q < NSLOT; q++) {
+    const int slot = lane + 32 * q;
+    const bool mine = feat_part ? slot < NF : (slot >= NF && slot < NF + 8);
+    if (!mine) continue;
+    if (acc[q] != 0.0f) {
+      size_t off;
+      if (feat_part) {
+        const int cr = slot / C, ch = slot - cr * C;
+        if (corner_inside(cell, cr, p.Df, off))
+          atomicAdd(p.grad_feat + ((size_t)b * p.Df * p.Df * p.Df + off) * C + ch, acc[q]);
+      } else {
+        if (corner_inside(cell, slot - NF, p.D, off)) atomicAdd(p.grad_tsdf + (size_t)b * p.D * p.D * p.D + off, acc[q]);
+      }
+    }
+    acc[q] = 0.0f;
+  }
+}
+
+template <int E, int C>
+__global__ void __launch_bounds__(256) render_bwd_kernel(RenderParams p) {
+  SG_RENDER_SMEM(E)
+  constexpr int NF = 8 * C, NSLOT = (NF + 8 + 31) / 32;
+  __shared__ float s_wf[8][32][9], s_wt[8][32][9];
+  __shared__ float s_g[8][32][C + 2];
+  __shared__ int s_cf[8][32][4], s_ct[8][32][4];
+  const int lane = lane_id();
+  const int Smax = p.sp.S;
+  for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < p.R;
+       r += ((long)gridDim.x * blockDim.x) >> 5) {
+    int b, S;
+    ray_frame(p, r, b, S);
+    RayEval<E> ev;
+    eval_ray<E, C>(p, r, b, S, sm, ev);
+    if (ev.done == 0) {
+      if (p.grad_sigma) {
+        for (int i = lane; i < Smax; i += 32) {
+          p.grad_sigma[(size_t)r * Smax + i] = 0.0f;
+          for (int k = 0; k < 3; k++) p.grad_rgb[((size_t)r * Smax + i) * 3 + k] = 0.0f;
+        }
+      }
+      __syncwarp();
+      continue;
+    }
+    const float gc[3] = {p.g_rgb ? __ldg(p.g_rgb + r * 3) : 0.0f, p.g_rgb ? __ldg(p.g_rgb + r * 3 + 1) : 0.0f,
+                         p.g_rgb ? __ldg(p.g_rgb + r * 3 + 2) : 0.0f};
+    const float gd = p.g_depth ? __ldg(p.g_depth + r) : 0.0f;
+    const float gws = p.g_ws ? __ldg(p.g_ws + r) : 0.0f;
+    const float ga = p.g_alpha ? __ldg(p.g_alpha + r) : 0.0f;
+    // weights and inclusive prefix sums over sorted positions of
+    // w*rgb, w*z, w, w*alpha; totals by carries (the forward's outputs)
+    float w[E], pf[E][3], pd[E], pw[E], pa[E];
+    float cf[3] = {0.0f, 0.0f, 0.0f}, cd = 0.0f, cw = 0.0f, ca = 0.0f;
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      w[e] = (((ev.proc & ev.valid) >> e) & 1u) ? ev.al[e] * ev.tb[e] : 0.0f;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        const float v = warp_incl_scan_f(w[e] * ev.rgb[e][k]);
+        pf[e][k] = cf[k] + v;
+        cf[k] += __shfl_sync(SG_FULL, v, 31);
+      }
+      const float vd = warp_incl_scan_f(w[e] * ev.z[e]);
+      const float vw = warp_incl_scan_f(w[e]);
+      const float va = warp_incl_scan_f(w[e] * ev.al[e]);
+      pd[e] = cd + vd;
+      pw[e] = cw + vw;
+      pa[e] = ca + va;
+      cd += __shfl_sync(SG_FULL, vd, 31);
+      cw += __shfl_sync(SG_FULL, vw, 31);
+      ca += __shfl_sync(SG_FULL, va, 31);
+    }
+    // exact adjoint per sorted position: d out / d sigma_i = delta_i *
+    // (T_{i+1} v_i - sum_{j>i} w_j v_j) (v = rgb, z, 1; 2 alpha T_{i+1} for
+    // the alpha sum); d out / d rgb_i = w_i
+    float gsig[E], grgb[E][3];
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      gsig[e] = 0.0f;
+      grgb[e][0] = grgb[e][1] = grgb[e][2] = 0.0f;
+      if (((ev.proc & ev.valid) >> e) & 1u) {
+        const float Ta = ev.tb[e] * (1.0f - ev.al[e]);
+        float acc = gws * (Ta - (cw - pw[e])) + gd * (Ta * ev.z[e] - (cd - pd[e])) +
+                    ga * (2.0f * ev.al[e] * Ta - (ca - pa[e]));
+#pragma unroll
+        for (int k = 0; k < 3; k++) acc += gc[k] * (Ta * ev.rgb[e][k] - (cf[k] - pf[e][k]));
+        gsig[e] = ev.dl[e] * acc;
+#pragma unroll
+        for (int k = 0; k < 3; k++) grgb[e][k] = w[e] * gc[k];
+      }
+    }
+    if (p.grad_sigma) {
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        const int i = e * 32 + lane;
+        if (i < Smax) {
+          p.grad_sigma[(size_t)r * Smax + i] = i < S ? gsig[e] : 0.0f;
+#pragma unroll
+          for (int k = 0; k < 3; k++) p.grad_rgb[((size_t)r * Smax + i) * 3 + k] = i < S ? grgb[e][k] : 0.0f;
+        }
+      }
+      for (int i = 32 * E + lane; i < Smax; i += 32) {
+        p.grad_sigma[(size_t)r * Smax + i] = 0.0f;
+        for (int k = 0; k < 3; k++) p.grad_rgb[((size_t)r * Smax + i) * 3 + k] = 0.0f;
+      }
+    }
+    if (!p.grad_feat && !p.grad_tsdf) {
+      __syncwarp();
+      continue;
+    }
+    // scatter into the grids, samples in sorted order
+    const float *bb = p.sp.t.vol_bbox + 6 * b;
+    const float bmin[3] = {bb[0], bb[2], bb[4]};
+    const float vs = __ldg(p.sp.t.voxel_size + b);
+    const float *fb = p.fbbox + 6 * b;
+    const float fmin[3] = {fb[0], fb[2], fb[4]};
+    const float fvs = __ldg(p.fvs + b);
+    const float o[3] = {__ldg(p.ori + r * 3), __ldg(p.ori + r * 3 + 1), __ldg(p.ori + r * 3 + 2)};
+    const float dr[3] = {__ldg(p.dir + r * 3), __ldg(p.dir + r * 3 + 1), __ldg(p.dir + r * 3 + 2)};
+    const float dsdt_k = -p.sdf_scale / (p.sdf_s * p.sdf_s);
+    float acc[NSLOT];
+#pragma unroll
+    for (int q = 0; q < NSLOT; q++) acc[q] = 0.0f;
+    int curf[3] = {INT_MIN, 0, 0}, curt[3] = {INT_MIN, 0, 0};
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      const bool use = (((ev.proc & ev.valid) >> e) & 1u) != 0;
+      if (use) {
+        const float pt[3] = {__fmaf_rn(dr[0], ev.z[e], o[0]), __fmaf_rn(dr[1], ev.z[e], o[1]),
+                             __fmaf_rn(dr[2], ev.z[e], o[2])};
+        int i0[3];
+        float wt[8];
+        tap_cell(fmin, fvs, pt, i0, wt);
+#pragma unroll
+        for (int a = 0; a < 3; a++) s_cf[w8][lane][a] = i0[a];
+#pragma unroll
+        for (int cr = 0; cr < 8; cr++) s_wf[w8][lane][cr] = wt[cr];
+        tap_cell(bmin, vs, pt, i0, wt);
+#pragma unroll
+        for (int a = 0; a < 3; a++) s_ct[w8][lane][a] = i0[a];
+#pragma unroll
+        for (int cr = 0; cr < 8; cr++) s_wt[w8][lane][cr] = wt[cr];
+        // feature gradient: head^T d rgb; TSDF gradient: d sigma / d t
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+          float g;
+          if (p.head)
+            g = __fmaf_rn(__ldg(p.head + 2 * C + c), grgb[e][2],
+                          __fmaf_rn(__ldg(p.head + C + c), grgb[e][1], __ldg(p.head + c) * grgb[e][0]));
+          else
+            g = c < 3 ? grgb[e][c] : 0.0f;
+          s_g[w8][lane][c] = g;
+        }
+        s_g[w8][lane][C] = gsig[e] * (ev.s01[e] * (1.0f - ev.s01[e]) * dsdt_k);
+      }
+      s_cf[w8][lane][3] = use;
+      __syncwarp();
+      for (int j = 0; j < 32; j++) {
+        if (!s_cf[w8][j][3]) continue;
+        if (p.grad_feat) {
+          const int c3[3] = {s_cf[w8][j][0], s_cf[w8][j][1], s_cf[w8][j][2]};
+          if (c3[0] != curf[0] || c3[1] != curf[1] || c3[2] != curf[2]) {
+            if (curf[0] != INT_MIN) flush_slots<C>(p, b, true, curf, acc);
+            curf[0] = c3[0];
+            curf[1] = c3[1];
+            curf[2] = c3[2];
+          }
+        }
+        if (p.grad_tsdf) {
+          const int c3[3] = {s_ct[w8][j][0], s_ct[w8][j][1], s_ct[w8][j][2]};
+          if (c3[0] != curt[0] || c3[1] != curt[1] || c3[2] != curt[2]) {
+            if (curt[0] != INT_MIN) flush_slots<C>(p, b, false, curt, acc);
+            curt[0] = c3[0];
+            curt[1] = c3[1];
+            curt[2] = c3[2];
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < NSLOT; q++) {
+          const int slot = lane + 32 * q;
+          if (slot < NF) {
+            if (p.grad_feat) {
+              const int cr = slot / C, ch = slot - cr * C;
+              acc[q] = __fmaf_rn(s_wf[w8][j][cr], s_g[w8][j][ch], acc[q]);
+            }
+          } else if (slot < NF + 8) {
+            if (p.grad_tsdf) acc[q] = __fmaf_rn(s_wt[w8][j][slot - NF], s_g[w8][j][C], acc[q]);
+          }
+        }
+      }
+      __syncwarp();
+    }
+    if (p.grad_feat && curf[0] != INT_MIN) flush_slots<C>(p, b, true, curf, acc);
+    if (p.grad_tsdf && curt[0] != INT_MIN) flush_slots<C>(p, b, false, curt, acc);
+    __syncwarp();
+  }
+}
+
+static int render_grid(long R) {
+  long g = (R * 32 + 255) / 256;
+  const long cap = 152L * tune(SG_TUNE_RENDER_WARPS);
+  return (int)(g < cap ? g : cap);
+}
+
+template <int C>
+static int launch_render(const RenderParams &p, bool bwd, int g, sg_stream_t stream) {
+  const int S = p.sp.S;
+  if (S <= 32) {
+    if (bwd) render_bwd_kernel<1, C><<<g, 256, 0, stream>>>(p);
+    else render_fwd_kernel<1, C><<<g, 256, 0, stream>>>(p);
+  } else if (S <= 64) {
+    if (bwd) render_bwd_kernel<2, C><<<g, 256, 0, stream>>>(p);
+    else render_fwd_kernel<2, C><<<g, 256, 0, stream>>>(p);
+  } else if (S <= 128) {
+    if (bwd) render_bwd_kernel<4, C><<<g, 256, 0, stream>>>(p);
+    else render_fwd_kernel<4, C><<<g, 256, 0, stream>>>(p);
+  } else {
+    return SG_ERR_UNSUPPORTED;
+  }
+  SG_LAUNCH_CHECK();
+  return SG_OK;
+}
+
+static int launch_render_c(const RenderParams &p, int C, bool bwd, sg_stream_t stream) {
+  if (p.R <= 0) return SG_OK;
+  const int g = render_grid(p.R);
+  if (C == 3) return launch_render<3>(p, bwd, g, stream);
+  if (C == 16) return launch_render<16>(p, bwd, g, stream);
+  return SG_ERR_UNSUPPORTED;
+}
+
+// RenderParams of the batched entry points.
+static int segment_params(const SgTree *tree, const SgRaySegments *seg, const SgRenderArgs *a, RenderParams &p) {
+  if (!tree || !seg || !a) return SG_ERR_INVALID_ARG;
+  if (seg->count <= 0 || seg->total < 0 || !seg->ray_begin || !seg->frame || !seg->samples)
+    return SG_ERR_INVALID_ARG;
+  if (!a->ori || !a->dir || !a->hit_idx || !a->hit_t0 || !a->hit_t1 || !a->valid_len || !a->tsdf || !a->feat ||
+      !a->feat_bbox || !a->feat_vs)
+    return SG_ERR_INVALID_ARG;
+  if (a->W <= 0 || a->S <= 0 || a->D <= 0 || a->Df <= 0 || tree->B <= 0 || a->sdf_s == 0.0f)
+    return SG_ERR_INVALID_ARG;
+  if (!a->head && a->C != 3) return SG_ERR_INVALID_ARG;
+  p = RenderParams{};
+  p.sp = SampleParams{*tree, a->hit_idx, a->hit_t0, a->hit_t1, a->rands, a->valid_len, 1, a->W, a->S, 2, 0,
+                      nullptr, nullptr, a->rand_seed};
+  p.hit_count = a->hit_count;
+  p.rand_const = a->rand_const;
+  p.R = seg->total;
+  p.nseg = seg->count;
+  p.seg_begin = seg->ray_begin;
+  p.seg_frame = seg->frame;
+  p.seg_samples = seg->samples;
+  p.ori = a->ori;
+  p.dir = a->dir;
+  p.tsdf = a->tsdf;
+  p.D = a->D;
+  p.sdf_scale = a->sdf_scale;
+  p.sdf_s = a->sdf_s;
+  p.feat = a->feat;
+  p.Df = a->Df;
+  p.fbbox = a->feat_bbox;
+  p.fvs = a->feat_vs;
+  p.head = a->head;
+  p.t_thres = a->t_thres;
+  return SG_OK;
+}
+
 }  // namespace sg
 
 using namespace sg;
@@ -159,21 +492,24 @@ extern "C" int sg_render_fused(const SgTree *tree, const int *hit_idx, const flo
   if ((out_z == nullptr) != (out_node == nullptr)) return SG_ERR_INVALID_ARG;
   if (N <= 0 || W <= 0 || S <= 0 || D <= 0 || Dc <= 0 || tree->B <= 0 || sdf_s == 0.0f)
     return SG_ERR_INVALID_ARG;
-  RenderParams p;
+  RenderParams p{};
   p.sp = SampleParams{*tree, hit_idx, hit_t0, hit_t1, rands, valid_len, N, W, S, num_levels, start_level,
-                      nullptr, nullptr};
+                      nullptr, nullptr, 0ull};
   p.hit_count = hit_count;
   p.rand_const = rand_const;
+  p.R = (long)tree->B * N;
+  p.nseg = 0;
   p.ori = ori;
   p.dir = dir;
   p.tsdf = tsdf;
   p.D = D;
   p.sdf_scale = sdf_scale;
   p.sdf_s = sdf_s;
-  p.cgrid = color_grid;
-  p.Dc = Dc;
-  p.cbbox = color_bbox;
-  p.cvs = color_vs;
+  p.feat = color_grid;
+  p.Df = Dc;
+  p.fbbox = color_bbox;
+  p.fvs = color_vs;
+  p.head = nullptr;
   p.t_thres = t_thres;
   p.out_rgb = out_rgb;
   p.out_depth = out_depth;
@@ -181,13 +517,41 @@ extern "C" int sg_render_fused(const SgTree *tree, const int *hit_idx, const flo
   p.out_alpha = out_alpha;
   p.out_z = out_z;
   p.out_node = out_node;
-  long R = (long)tree->B * N;
-  int g = ceil_div(R * 32, 256);
-  if (g > 152 * tune(SG_TUNE_RENDER_WARPS)) g = 152 * tune(SG_TUNE_RENDER_WARPS);
-  if (S <= 32) render_kernel<1><<<g, 256, 0, stream>>>(p);
-  else if (S <= 64) render_kernel<2><<<g, 256, 0, stream>>>(p);
-  else if (S <= 128) render_kernel<4><<<g, 256, 0, stream>>>(p);
-  else return SG_ERR_UNSUPPORTED;
-  SG_LAUNCH_CHECK();
-  return SG_OK;
+  return launch_render_c(p, 3, false, stream);
+}
+
+extern "C" int sg_render_segments_fwd(const SgTree *tree, const SgRaySegments *seg, const SgRenderArgs *args,
+                                      float *out_rgb, float *out_depth, float *out_ws, float *out_alpha,
+                                      float *out_z, int *out_node, sg_stream_t stream) {
+  RenderParams p;
+  int rc = segment_params(tree, seg, args, p);
+  if (rc != SG_OK) return rc;
+  if (!out_rgb || !out_depth || !out_ws || !out_alpha || (out_z == nullptr) != (out_node == nullptr))
+    return SG_ERR_INVALID_ARG;
+  p.out_rgb = out_rgb;
+  p.out_depth = out_depth;
+  p.out_ws = out_ws;
+  p.out_alpha = out_alpha;
+  p.out_z = out_z;
+  p.out_node = out_node;
+  return launch_render_c(p, args->C, false, stream);
+}
+
+extern "C" int sg_render_segments_bwd(const SgTree *tree, const SgRaySegments *seg, const SgRenderArgs *args,
+                                      const float *g_rgb, const float *g_depth, const float *g_ws,
+                                      const float *g_alpha, float *grad_feat, float *grad_tsdf,
+                                      float *grad_sigma, float *grad_rgb, sg_stream_t stream) {
+  RenderParams p;
+  int rc = segment_params(tree, seg, args, p);
+  if (rc != SG_OK) return rc;
+  if ((grad_sigma == nullptr) != (grad_rgb == nullptr)) return SG_ERR_INVALID_ARG;
+  p.g_rgb = g_rgb;
+  p.g_depth = g_depth;
+  p.g_ws = g_ws;
+  p.g_alpha = g_alpha;
+  p.grad_feat = grad_feat;
+  p.grad_tsdf = grad_tsdf;
+  p.grad_sigma = grad_sigma;
+  p.grad_rgb = grad_rgb;
+  return launch_render_c(p, args->C, true, stream);
 }

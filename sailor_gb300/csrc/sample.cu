@@ -26,7 +26,7 @@ __global__ void __launch_bounds__(256) sample_coarse_kernel(SampleParams p) {
   const long R = (long)p.t.B * p.N;
   for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < R;
        r += ((long)gridDim.x * blockDim.x) >> 5) {
-    warp_sample_ray(p, r, p.W, 0.5f, s_z[w8], s_i[w8], s_sc[w8]);
+    warp_sample_ray(p, r, (int)(r / p.N), p.S, p.W, 0.5f, s_z[w8], s_i[w8], s_sc[w8]);
     for (int q = lane; q < p.S; q += 32) {
       p.sampled_z[(size_t)r * p.S + q] = s_z[w8][q];
       p.sampled_idx[(size_t)r * p.S + q] = s_i[w8][q];
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(256) sample_sorted_kernel(SampleParams p, cons
   for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < R;
        r += ((long)gridDim.x * blockDim.x) >> 5) {
     const int nh = hit_count ? min(hit_count[r], p.W) : p.W;
-    const int done = warp_sample_ray(p, r, nh, rand_const, s_z[w8], s_i[w8], s_sc[w8]);
+    const int done = warp_sample_ray(p, r, (int)(r / p.N), S, nh, rand_const, s_z[w8], s_i[w8], s_sc[w8]);
     warp_sort_samples(s_z[w8], s_p[w8], S, done);
     for (int i = lane; i < S; i += 32) {
       out_z[(size_t)r * S + i] = s_z[w8][i];
@@ -108,7 +108,7 @@ extern "C" int sg_sample_sorted(const SgTree *tree, const int *hit_idx, const fl
     return SG_ERR_INVALID_ARG;
   if (N <= 0 || W <= 0 || S <= 0 || tree->B <= 0) return SG_ERR_INVALID_ARG;
   SampleParams p{*tree, hit_idx, hit_t0, hit_t1, rands, valid_len, N, W, S, num_levels, start_level,
-                 nullptr, nullptr};
+                 nullptr, nullptr, 0ull};
   int g = grid_for((long)tree->B * N);
   if (S <= 32) sample_sorted_kernel<1><<<g, 256, 0, stream>>>(p, hit_count, rand_const, sorted_z, sorted_idx);
   else if (S <= 64) sample_sorted_kernel<2><<<g, 256, 0, stream>>>(p, hit_count, rand_const, sorted_z, sorted_idx);
@@ -126,7 +126,7 @@ extern "C" int sg_sample_coarse(const SgTree *tree, const int *hit_idx, const fl
     return SG_ERR_INVALID_ARG;
   if (N <= 0 || W <= 0 || S <= 0 || tree->B <= 0) return SG_ERR_INVALID_ARG;
   SampleParams p{*tree, hit_idx, hit_t0, hit_t1, rands, valid_len, N, W, S, num_levels, start_level,
-                 sampled_idx, sampled_z};
+                 sampled_idx, sampled_z, 0ull};
   int g = grid_for((long)tree->B * N);
   if (S <= 32) launch_sample_coarse<1>(p, g, stream);
   else if (S <= 64) launch_sample_coarse<2>(p, g, stream);

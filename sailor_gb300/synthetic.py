@@ -195,3 +195,59 @@ def random_rays(seed, n, radius=3.0):
     d = tgt - o
     d /= np.linalg.norm(d, axis=1, keepdims=True)
     return o.astype(np.float32), d.astype(np.float32)
+
+
+def _view_images(rng, prims, K, R, T, res, noise, dropout):
+    z = cast_depth(prims, K, R, T, res)
+    hit = z > 0
+    z = z + rng.normal(0.0, noise, z.shape) * hit
+    z[rng.random(z.shape) < dropout] = 0.0
+    u16 = np.clip(np.round(z * 10000.0), 0, 65535).astype(np.uint16)
+    depth = (u16 / 10000.0).astype(np.float32)
+    rgb = rng.integers(0, 256, (res, res, 3))
+    color = np.floor(rgb[..., 2] * 65536.0 + rgb[..., 1] * 256.0 + rgb[..., 0]).astype(np.float32)
+    return depth, color
+
+
+def make_batch_workload(seed=0, n_frames=8, views=(4, 8), view_res=(512, 768, 1024), n_prims=12, D=256,
+                        trunc=0.03, n_targets=16, target_res=(256, 1024), target_S=(32, 48, 64, 96, 128),
+                        noise=0.005, dropout=0.02):
+    """Frames of uneven view counts and resolutions, each with its own seeded
+    scene, and target cameras of uneven sizes and sample counts.
+
+    Returns dict(frames=[dict(K, RT, depth, color) lists per view],
+    vol_bbox [B,3,2], voxel_size [B], trunc_weight, D,
+    targets=[dict(frame, res, S, ori [res*res,3], dir [res*res,3])])."""
+    rng = np.random.default_rng(seed)
+    frames = []
+    for b in range(n_frames):
+        frng = np.random.default_rng(seed * 1000 + 17 * b + 1)
+        prims = random_primitives(frng, n_prims)
+        nv = int(frng.integers(views[0], views[1] + 1))
+        cams = ring_cameras(nv, phase=frng.uniform(0, 2 * math.pi))
+        fr = dict(K=[], RT=[], depth=[], color=[])
+        for R, T in cams:
+            res = int(frng.choice(view_res))
+            K = intrinsics(res)
+            depth, color = _view_images(frng, prims, K, R, T, res, noise, dropout)
+            fr["K"].append(K.astype(np.float32))
+            fr["RT"].append(np.concatenate([R, T[:, None]], 1).astype(np.float32))
+            fr["depth"].append(depth)
+            fr["color"].append(color)
+        frames.append(fr)
+    lo, hi = target_res
+    sizes = np.linspace(lo, hi, n_targets)
+    sizes = (np.round(sizes / 32.0) * 32).astype(int)
+    rng.shuffle(sizes)
+    targets = []
+    for t in range(n_targets):
+        res = int(sizes[t])
+        a = rng.uniform(0, 2 * math.pi)
+        R, T = look_at((2.5 * math.cos(a), 2.5 * math.sin(a), rng.uniform(0.6, 1.6)))
+        o, d = camera_rays(intrinsics(res), R, T, res)
+        targets.append(dict(frame=t % n_frames, res=res, S=int(target_S[t % len(target_S)]), ori=o, dir=d))
+    vs = np.float32(2.0) / np.float32(D - 1)
+    return dict(frames=frames, D=D,
+                vol_bbox=np.tile(np.array([[-1.0, 1.0]] * 3, np.float32), (n_frames, 1, 1)),
+                voxel_size=np.full((n_frames,), vs, np.float32),
+                trunc_weight=float(np.float32(trunc) / vs), targets=targets)
