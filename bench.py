@@ -1,19 +1,30 @@
 """Benchmark of the VoxelEncoding hot path on one GB300 (or N replicas).
 
-Workload (the full-resolution plain-forward configuration): one frame of 4
-synthetic RGBD views at 1024x1024 (24 capsules/ellipsoids, 5 mm depth noise,
-2 % dropout, uint16 depth), fused into a 512^3 TSDF grid (2 m cube, 2 cm
-truncation), 8^3 bricks (64^3 top grid), then a 1024x1024 target view
-rendered with up to 96 adaptive samples per ray: intersection, sampling and
-per-ray sort, per-sample density (sigmoid of the fused TSDF, s = 5 mm) and
-colour (trilinear from a seeded 256^3 x 3 grid), front-to-back compositing.
+Default workload (--workload batch, the batched training step): 8 frames of
+4-8 synthetic RGBD views each at uneven resolutions from {512, 768,
+1024}^2, each frame its own seeded scene (12 capsules/ellipsoids, 5 mm depth
+noise, 2 % dropout, uint16 depth) fused into its own 256^3 TSDF grid (2 m
+cube, 3 cm truncation, 8^3 bricks); 16 target cameras of uneven sizes (256^2
+to 1024^2, 7.4 M rays in all) with 32-128 adaptive samples per ray.  One
+step = fusion + tree build of all frames, intersection, forward render
+(density from the fused TSDF, colour = a linear head over a seeded
+256^3 x 16 feature grid per frame), the gradient of an L2 colour loss, and
+the backward (exact compositing adjoint, gradients scattered into the
+feature and TSDF grids) -- one launch per stage over all frames and targets,
+replayed from a CUDA graph.  value = rays of all targets / step time.  The
+plain per-frame forward-only launch sequence (the reference's call order
+through the drop-in API: integrate, build_multi_res_volumes, octree, and per
+target traversal with 128-wide padded hit rows, coarse sampling, sort, field
+gathers, compositing) runs on the same inputs for the ratio.
 
-One step = fusion + tree build + rendering of the target view, all inputs
-resident in HBM (value); e2e = the same step through the public pipeline API
-from pinned host buffers (images, cameras, rays copied in; the rendered image
-read back).  The per-step working set (>10 GB) is far larger than L2.
+--workload plain: one frame of 4 views at 1024^2 fused into a 512^3 grid,
+a 1024^2 target with up to 96 samples, forward only.
 
-  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+e2e = the same step through the public API from pinned host buffers (images,
+cameras, rays and target colours copied in; the rendered colours read
+back).  The per-step working set (> 10 GB) is far larger than L2.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--workload batch|plain]
 """
 import argparse
 import json
@@ -31,6 +42,10 @@ sys.path.insert(0, ROOT)
 METRIC = "rays/s fwd+bwd batched vs plain per-frame, ≤1e-5 err; TSDF Gvox/s; 1 GB300"
 UNIT = "rays/s"
 CFG = dict(views=4, res=1024, prims=24, D=512, rate=8, trunc=0.02, target=1024, S=96, color_D=256, seed=7)
+BATCH = dict(frames=8, views=(4, 8), view_res=(512, 768, 1024), prims=12, D=256, rate=8, trunc=0.03, C=16,
+             targets=16, target_res=(256, 1024), target_S=(32, 48, 64, 96, 128), W_hits=256, sdf_s=0.005,
+             seed=11)
+BATCH_SMALL = dict(BATCH, frames=3, views=(2, 4), view_res=(256, 384), D=128, targets=5, target_res=(128, 256))
 
 
 def parse():
@@ -42,6 +57,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="small configuration (256^3, 512^2) for profiling")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--workload", default="batch", choices=["batch", "plain"])
     ap.add_argument("--unfused", action="store_true",
                     help="render with four kernels (sample+sort, two field gathers, composite) instead of one")
     return ap.parse_args()
@@ -203,10 +219,351 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# batched training step (default workload)
+# ---------------------------------------------------------------------------
+def batch_workload(bcfg, rank=0):
+    from sailor_gb300 import synthetic as syn
+    return syn.make_batch_workload(seed=bcfg["seed"] + 1000 * rank, n_frames=bcfg["frames"], views=bcfg["views"],
+                                   view_res=bcfg["view_res"], n_prims=bcfg["prims"], D=bcfg["D"],
+                                   trunc=bcfg["trunc"], n_targets=bcfg["targets"], target_res=bcfg["target_res"],
+                                   target_S=bcfg["target_S"], workers=min(8, os.cpu_count() or 1))
+
+
+def batch_fields(bcfg, R, feat, rank=0):
+    """Seeded feature grids ~ N(0, 0.1) written into feat [B, D, D, D, C] on
+    the device; colour head [3, C] ~ N(0, 0.25); target colours U(0, 1)."""
+    import torch
+    gen = torch.Generator(device=feat.device)
+    gen.manual_seed(bcfg["seed"] + 1000 * rank + 5)
+    feat.normal_(0.0, 0.1, generator=gen)
+    rng = np.random.default_rng(bcfg["seed"] + 1000 * rank + 5)
+    head = rng.standard_normal((3, bcfg["C"]), dtype=np.float32) * np.float32(0.5)
+    target = rng.random((R, 3), dtype=np.float32)
+    return head, target
+
+
+def padded_views(fr):
+    """A frame's views zero-padded to its largest resolution (depth 0 =
+    no measurement, so the padding changes nothing)."""
+    hm = max(d.shape[0] for d in fr["depth"])
+    nv = len(fr["depth"])
+    dep = np.zeros((1, nv, hm, hm), np.float32)
+    col = np.zeros((1, nv, hm, hm), np.float32)
+    for v in range(nv):
+        h, w_ = fr["depth"][v].shape
+        dep[0, v, :h, :w_] = fr["depth"][v]
+        col[0, v, :h, :w_] = fr["color"][v]
+    return np.stack(fr["K"])[None], np.stack(fr["RT"])[None], dep, col
+
+
+def batch_algorithmic_bytes(bcfg, w, n_hits, R, n_samples):
+    """Per-launch algorithmic HBM bytes of each batched stage."""
+    B, D, C = bcfg["frames"], bcfg["D"], bcfg["C"]
+    V, Vt = B * D ** 3, B * (D // bcfg["rate"]) ** 3
+    n_pix = sum(d.size for fr in w["frames"] for d in fr["depth"])
+    return dict(
+        fusion=16 * V + 8 * n_pix,
+        tree=4 * V + 4 * Vt,
+        intersect=24 * R + 12 * n_hits + 8 * R,
+        # hit rows + per-ray count / valid length + ray + 24 B/ray out
+        forward=12 * n_hits + 8 * R + 24 * R + 24 * R,
+        # as forward, upstream gradient in, and the gradient grids zeroed and
+        # written (the dense grids are the contract of the adjoint)
+        backward=12 * n_hits + 8 * R + 24 * R + 12 * R + 2 * 4 * V * (C + 1),
+    )
+
+
+def cpu_baseline_batch(w, bcfg, feat, head, ray_sample=2048, fusion_slab=8):
+    """The oracle (a C port of the reference kernels, OpenMP on all host
+    cores) on a bounded sample of the batched step, scaled to the whole step:
+    fusion of an x-slab of frame 0, coarse occupancy + tree of frame 0 (x
+    frames), and forward + backward of a ray subset of target 0."""
+    from oracle import oracle as orc
+    D, rate, B = bcfg["D"], bcfg["rate"], bcfg["frames"]
+    fr = w["frames"][0]
+    K, RT, dep, col = padded_views(fr)
+    bb, vs = w["vol_bbox"][:1], w["voxel_size"][:1].reshape(1, 1)
+    n_views_all = sum(len(f["K"]) for f in w["frames"])
+    t0 = time.perf_counter()
+    orc.integrate_slab(K, RT, col, dep, D, bb, vs, 0, fusion_slab, trunc_weight=w["trunc_weight"])
+    t_fuse = (time.perf_counter() - t0) * (D / fusion_slab) * (n_views_all / len(fr["K"]))
+    fz = orc.integrate(K, RT, col, dep, D, bb, vs, trunc_weight=w["trunc_weight"])
+    t0 = time.perf_counter()
+    top, _ = orc.merge(fz["occ"], rate)
+    tree = orc.build_tree(top, fz["occ"])
+    t_tree = (time.perf_counter() - t0) * B
+    tg = w["targets"][0]
+    sel = np.linspace(0, tg["ori"].shape[0] - 1, ray_sample).astype(np.int64)
+    o, d = tg["ori"][sel][None], tg["dir"][sel][None]
+    S = tg["S"]
+    R = sum(t["ori"].shape[0] for t in w["targets"])
+    t0 = time.perf_counter()
+    hits = orc.voxel_traversal(tree, o, d, vs, bb, W=bcfg["W_hits"])
+    _, sz, _ = orc.sample_coarse(tree, hits, np.full((1, ray_sample, S), 0.5, np.float32), vs, S)
+    srt, _ = orc.sort(sz)
+    pts = (o[0][:, None, :] + d[0][:, None, :] * np.maximum(srt[0], 0)[..., None]).reshape(-1, 3)
+    t = orc.grid_gather(pts, fz["tsdf"][..., None], bb[:, :, 0], vs[:, 0])[:, 0]
+    sdf = t * float(vs[0, 0]) * w["trunc_weight"]
+    sigma = (1.0 / (1.0 + np.exp(sdf / bcfg["sdf_s"])) / bcfg["sdf_s"]).astype(np.float32)
+    fe = orc.grid_gather(pts, feat[:1], bb[:, :, 0], vs[:, 0])
+    rgb = (fe @ head.T.astype(np.float64)).astype(np.float32)
+    sig4 = sigma.reshape(1, ray_sample, S, 1)
+    rgb4 = rgb.reshape(1, ray_sample, S, 3)
+    fo = orc.composite_fwd(srt, None, sig4, rgb4, 1e-4, False)[:4]
+    g = [np.ones(x.shape, np.float32) for x in fo]
+    ident = np.broadcast_to(np.arange(S, dtype=np.int32), srt.shape)
+    gf, gs = orc.composite_bwd_ref(*g, *fo, srt, ident, sig4, rgb4, 1e-4, False)
+    gfe = (gf.reshape(-1, 3).astype(np.float64) @ head.astype(np.float64)).astype(np.float32)
+    orc.grid_scatter(pts, gfe, 1, D, bb[:, :, 0], vs[:, 0])
+    t_render = (time.perf_counter() - t0) * R / ray_sample
+    t_step = t_fuse + t_tree + t_render
+    return dict(value=R / t_step, unit=UNIT, cores=orc.num_threads(), kind="port",
+                sample=(f"oracle (C port, OpenMP) on host cores: fusion of x-slab {fusion_slab}/{D} of frame 0 "
+                        f"scaled to all {n_views_all} views, coarse occupancy + tree of frame 0 x{B}, "
+                        f"traversal/sampling/sort/field taps/compositing forward and backward + grid scatter "
+                        f"of {ray_sample} rays of target 0 scaled to {R} rays"),
+                stage_s=dict(fusion=t_fuse, tree=t_tree, render=t_render))
+
+
+def plain_per_frame_forward(VE, fields, w, bcfg, dev, feat, head_t, vbb, vvs, W_hits=256):
+    """The reference's per-frame call order through the drop-in API, forward
+    only: per frame integrate -> build_multi_res_volumes -> octree, then per
+    target of the frame traversal (padded rows) -> coarse sampling -> sort ->
+    TSDF density and feature gathers -> colour head -> compositing."""
+    import torch
+    D, rate = bcfg["D"], bcfg["rate"]
+    Dt = D // rate
+    trunc_m = float(w["voxel_size"][0]) * w["trunc_weight"]
+    outs = []
+    for b, fr in enumerate(w["frames"]):
+        K, RT, dep, col = fr["_dev"]
+        occ0 = torch.full((1, D, D, D), -1, dtype=torch.int32, device=dev)
+        occ1 = torch.full((1, Dt, Dt, Dt), -1, dtype=torch.int32, device=dev)
+        cnt0 = torch.zeros((1, 1), dtype=torch.int32, device=dev)
+        cnt1 = torch.zeros((1, 1), dtype=torch.int32, device=dev)
+        bb, vs = vbb[b:b + 1], vvs[b:b + 1]
+        tsdf, _, _ = VE.integrate_in_box(occ0, cnt0, K, RT, col, dep, bb, vs, 1.0, w["trunc_weight"], 13.5, 13.5,
+                                         dev.index or 0)
+        VE.build_multi_res_volumes([occ0, occ1], [cnt0, cnt1], 2, rate, dev.index or 0)
+        tot = [int(cnt0.sum()), int(cnt1.sum())]
+        octree = VE.MultiLayerOctree(2, 1, rate, dev.index or 0)
+        octree.init_octree([occ0, occ1], tot, [cnt0, cnt1], [0, tot[0]], vs, bb)
+        octree.build_octree()
+        for t in w["targets"]:
+            if t["frame"] != b:
+                continue
+            o, d = t["_dev"]
+            S = t["S"]
+            n = o.shape[1]
+            idx, t0, t1, vl = octree.voxel_traversal(o, d, W_hits, 0, -1, False, -1)
+            rands = torch.full((1, n, S), 0.5, device=dev)
+            _, sz = octree.ray_voxels_points_sampling_coarse(idx, t0, t1, rands, vl, 0, S)
+            _, sidx = octree.sort_samplings(sz)
+            sig = fields.tsdf_density(tsdf, o, d, sz, bb, vs, trunc_m, bcfg["sdf_s"])
+            rgb = fields.grid_gather(feat[b:b + 1], o, d, sz, bb, vs) @ head_t
+            outs.append(VE.volume_rendering_training_forward(sz, sidx, sig[..., None].contiguous(),
+                                                             rgb.contiguous(), dev.index or 0, 1e-4, False))
+    return outs
+
+
+def run_batch(args):
+    import torch
+    import torch.distributed as dist
+
+    from sailor_gb300 import fields
+    from sailor_gb300.batch import BatchPipeline
+    from sailor_gb300.dist import VoxelEncoding as VE
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    bcfg = dict(BATCH_SMALL if args.small else BATCH)
+    w = batch_workload(bcfg, rank)
+    view_hw = [[d.shape for d in fr["depth"]] for fr in w["frames"]]
+    targets = [(t["frame"], t["ori"].shape[0], t["S"]) for t in w["targets"]]
+    bp = BatchPipeline(view_hw, targets, D=bcfg["D"], rate=bcfg["rate"], C=bcfg["C"], W_hits=bcfg["W_hits"],
+                       device=dev)
+    bp.load_views(w["frames"], w["vol_bbox"], w["voxel_size"], w["trunc_weight"])
+    bp.load_rays([(t["ori"], t["dir"]) for t in w["targets"]])
+    head, target = batch_fields(bcfg, bp.R, bp.feat, rank)
+    bp.set_fields(head=torch.as_tensor(head).to(dev), target_rgb=torch.as_tensor(target).to(dev))
+    trunc_m = float(w["voxel_size"][0]) * w["trunc_weight"]
+    bp.render_args(trunc_m, sdf_s=bcfg["sdf_s"], t_thres=1e-4, rand_seed=bcfg["seed"] + 1)
+    R = bp.R
+
+    tuned = None
+    bp.train_step()
+    if not args.no_autotune:
+        from sailor_gb300 import autotune
+        autotune.set_knob("fuse_tiled", 1)
+        tuned = autotune.tune({"isect_block": bp.intersect,
+                               "render_warps": lambda: (bp.forward(), bp.backward(bp.g_rgb))},
+                              verbose=True)
+        tuned.update(fuse_tiled=1)
+    for _ in range(max(args.warmup - 1, 0)):
+        bp.train_step()
+    torch.cuda.synchronize()
+    st = bp.status.tolist()
+    if st[0] & 1:
+        raise RuntimeError(f"hit rows overflowed: a ray has {st[1]} hits, rows hold {bp.W}")
+    n_hits = int(bp.hit_count.sum().item())
+    graph = bp.capture(warmup=1)
+    for _ in range(args.warmup):
+        graph.replay()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    import tempfile
+    clk = ClockSampler(os.path.join(tempfile.gettempdir(), f"sg_clocks_rank{rank}.csv"))
+    with clk:
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            graph.replay()
+        e1.record()
+        barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    t = torch.tensor([ms], device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * R / (ms_max / 1000.0)
+
+    # per-stage times (eager pass with events on the launching stream)
+    stage_sum = {}
+    for _ in range(args.steps):
+        bp.events = []
+        bp.train_step()
+        for k, v in bp.stage_times().items():
+            stage_sum[k] = stage_sum.get(k, 0.0) + v
+    bp.events = None
+    stages = {k: v / args.steps for k, v in stage_sum.items()}
+    peak_mem = torch.cuda.max_memory_allocated(dev)
+
+    # plain per-frame forward-only launch sequence on the same inputs
+    vbb = torch.as_tensor(w["vol_bbox"]).to(dev)
+    vvs = torch.as_tensor(w["voxel_size"]).reshape(-1, 1).to(dev)
+    for fr in w["frames"]:
+        fr["_dev"] = [torch.as_tensor(a).to(dev) for a in padded_views(fr)]
+    for t in w["targets"]:
+        t["_dev"] = (torch.as_tensor(t["ori"])[None].to(dev), torch.as_tensor(t["dir"])[None].to(dev))
+    feat_t, head_t = bp.feat, bp.head.T.contiguous()
+    plain_forward = lambda: plain_per_frame_forward(VE, fields, w, bcfg, dev, feat_t, head_t, vbb, vvs)  # noqa
+    for _ in range(2):
+        plain_forward()
+    barrier()
+    p0 = time.perf_counter()
+    n_plain = max(1, min(args.steps, 5))
+    for _ in range(n_plain):
+        plain_forward()
+    barrier()
+    plain_ms = (time.perf_counter() - p0) * 1000.0 / n_plain
+    plain_value = R / (plain_ms / 1000.0)
+    for fr in w["frames"]:
+        fr.pop("_dev")
+    for t in w["targets"]:
+        t.pop("_dev")
+
+    # e2e: the same step through the public API from pinned host buffers
+    host = dict(depth=torch.as_tensor(np.concatenate([d.reshape(-1) for fr in w["frames"] for d in fr["depth"]])),
+                color=torch.as_tensor(np.concatenate([c.reshape(-1) for fr in w["frames"] for c in fr["color"]])),
+                K=torch.as_tensor(np.stack([k for fr in w["frames"] for k in fr["K"]])),
+                RT=torch.as_tensor(np.stack([k for fr in w["frames"] for k in fr["RT"]])),
+                ori=torch.as_tensor(np.concatenate([t["ori"] for t in w["targets"]])),
+                dirs=torch.as_tensor(np.concatenate([t["dir"] for t in w["targets"]])),
+                target_rgb=torch.as_tensor(target))
+    host = {k: v.contiguous().pin_memory() for k, v in host.items()}
+    dst = dict(depth=bp.depth, color=bp.color, K=bp.K, RT=bp.RT, ori=bp.ori, dirs=bp.dirs,
+               target_rgb=bp.target_rgb)
+    out_host = torch.empty((R, 3), dtype=torch.float32).pin_memory()
+    h2d = sum(v.numel() * v.element_size() for v in host.values())
+    d2h = out_host.numel() * 4
+
+    def e2e_step():
+        for k in host:
+            dst[k].copy_(host[k], non_blocking=True)
+        graph.replay()
+        out_host.copy_(bp.out_rgb, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    barrier()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record()
+    for _ in range(args.steps):
+        e2e_step()
+    f1.record()
+    barrier()
+    t = torch.tensor([f0.elapsed_time(f1) / args.steps], device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    e2e_value = world * R / (float(t.item()) / 1000.0)
+
+    if rank == 0:
+        pk, pk_kind = peaks()
+        S_all = sum(n * s for _, n, s in targets)
+        ab = batch_algorithmic_bytes(bcfg, w, n_hits, R, S_all)
+        rl = {k: ab[k] / (stages[k] / 1000.0) / 1e9 for k in ab if stages.get(k)}
+        dom = max(rl, key=lambda k: stages[k])
+        traffic = None
+        tpath = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tpath):
+            traffic = json.load(open(tpath)).get("batch_" + dom)
+        render_ms = sum(stages.get(k, 0.0) for k in ("intersect", "forward", "backward"))
+        out = dict(
+            metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=args.steps, warmup=args.warmup,
+            ms_per_step=ms_max, higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32",
+            data="synthetic (seeded capsule/ellipsoid scenes per frame, see DESIGN.md)",
+            config=dict(workload=("batched training step: %d frames x 4-8 views at {512,768,1024}^2, 256^3 TSDF "
+                                  "+ 256^3x16 feature grid per frame, 8^3 bricks, %d targets 256^2-1024^2 "
+                                  "(%d rays), S 32-128, forward + adjoint, CUDA graph" %
+                                  (bcfg["frames"], bcfg["targets"], R)) if not args.small else "batch small",
+                        frames_per_rank=bcfg["frames"], rays_per_step=R, l2="per-step working set > 10 GB >> L2",
+                        parallelism=f"replicas x{world}", launch_shapes=tuned),
+            stages_ms=stages,
+            render_rays_s=R / (render_ms / 1000.0),
+            plain_per_frame_fwd=dict(value=plain_value, unit=UNIT, ms_per_step=plain_ms,
+                                     ratio_batched_fwd_bwd=value / plain_value),
+            tsdf_gvox_s=bcfg["frames"] * bcfg["D"] ** 3 / (stages["fusion"] / 1000.0) / 1e9,
+            hits_per_ray=n_hits / R, peak_hbm_bytes=peak_mem,
+            roofline=dict(bound="hbm", kernel=dom, achieved=rl[dom], peak=pk["hbm_gbs"], unit="GB/s",
+                          frac=rl[dom] / pk["hbm_gbs"], traffic=traffic, peak_kind=pk_kind,
+                          algorithmic_bytes=ab[dom]),
+            rooflines={k: dict(achieved=v, frac=v / pk["hbm_gbs"], algorithmic_bytes=ab[k]) for k, v in rl.items()},
+            e2e=dict(value=e2e_value, unit=UNIT, h2d_bytes_per_step=h2d, d2h_bytes_per_step=d2h),
+            gpu_launches=10 * args.steps,
+            clocks=clk.summary(),
+        )
+        if not args.no_cpu_baseline:
+            cb = cpu_baseline_batch(w, bcfg, bp.feat[:1].cpu().numpy(), head)
+            out["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch":
+        return run_batch(args)
+    return run_plain(args)
+
+
+def run_plain(args):
     import torch
     import torch.distributed as dist
 

@@ -35,11 +35,13 @@ from . import _native as N
 
 
 class BatchPipeline:
-    def __init__(self, view_hw, targets, D=256, rate=8, C=16, W_hits=64, device="cuda"):
+    def __init__(self, view_hw, targets, D=256, rate=8, C=16, W_hits=64, train_tsdf=False, device="cuda"):
         """view_hw: per frame, a list of (H, W) per view.  targets: list of
-        (frame, n_rays, S)."""
+        (frame, n_rays, S).  train_tsdf: train_step also scatters the gradient
+        of the TSDF grid (the feature grid is always trained)."""
         self.B = B = len(view_hw)
         self.D, self.rate, self.C, self.W = D, rate, C, W_hits
+        self.train_tsdf = bool(train_tsdf)
         self.Dt = D // rate
         if self.Dt * rate != D or D % 4:
             raise ValueError("D must be a multiple of rate and of 4")
@@ -229,7 +231,7 @@ class BatchPipeline:
         self.forward()
         torch.sub(self.out_rgb, self.target_rgb, out=self.g_rgb)
         self.g_rgb.mul_(2.0 / (3.0 * self.R))
-        self.backward(self.g_rgb)
+        self.backward(self.g_rgb, tsdf_grad=self.train_tsdf)
 
     def capture(self, warmup=2):
         """CUDA graph of train_step (run it a few times first, then capture)."""

@@ -213,6 +213,13 @@ __device__ __forceinline__ float hash_uniform(unsigned long long seed, long r, i
   return (float)(x >> 40) * (1.0f / 16777216.0f);
 }
 
+// Fire-and-forget vector reduction of four consecutive floats (PTX
+// red.global.add.v4.f32, sm_90 and later); addr must be 16-byte aligned.
+__device__ __forceinline__ void red_add_f32x4(float *addr, float a, float b, float c, float d) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(a), "f"(b), "f"(c), "f"(d)
+               : "memory");
+}
+
 #define SG_LAUNCH_CHECK()                           \
   do {                                              \
     cudaError_t _e = cudaGetLastError();            \

@@ -60,8 +60,8 @@ __global__ void __launch_bounds__(256) grid_gather_kernel(GatherParams p) {
       float pt[3];
 #pragma unroll
       for (int a = 0; a < 3; a++) pt[a] = __fmaf_rn(__ldg(p.dir + r * 3 + a), zz, __ldg(p.ori + r * 3 + a));
-      grid_tap<C>(p.grid + (size_t)b * p.D * p.D * p.D * C, p.D, bmin, __ldg(p.voxel_size + b), pt, acc);
-      if (p.mode == 1) acc[0] = tsdf_density(acc[0], p.scale, p.s);
+      grid_tap<C>(p.grid + (size_t)b * p.D * p.D * p.D * C, p.D, bmin, 1.0f / __ldg(p.voxel_size + b), pt, acc);
+      if (p.mode == 1) acc[0] = tsdf_density(acc[0], p.scale / p.s, 1.0f / p.s);
     }
 #pragma unroll
     for (int c = 0; c < C; c++) p.out[k * C + c] = acc[c];
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(256) grid_scatter_kernel(ScatterParams p) {
     const int b = (int)(r / p.N);
     const float *bb = p.vol_bbox + 6 * b;
     const float bmin[3] = {bb[0], bb[2], bb[4]};
-    const float vs = __ldg(p.voxel_size + b);
+    const float inv_vs = 1.0f / __ldg(p.voxel_size + b);
     float acc[NSLOT];
 #pragma unroll
     for (int q = 0; q < NSLOT; q++) acc[q] = 0.0f;
@@ -121,21 +121,13 @@ __global__ void __launch_bounds__(256) grid_scatter_kernel(ScatterParams p) {
       const float zz = i < p.S ? __ldg(p.z + r * p.S + i) : -1.0f;
       int valid = 0;
       if (zz >= 0.0f) {
-        float pt[3], f[3];
+        float pt[3], wc[8];
         int i0[3];
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-          pt[a] = __fmaf_rn(__ldg(p.dir + r * 3 + a), zz, __ldg(p.ori + r * 3 + a));
-          const float u = (pt[a] - bmin[a]) / vs;
-          const float fl = floorf(u);
-          i0[a] = (int)fl;
-          f[a] = u - fl;
-        }
+        for (int a = 0; a < 3; a++) pt[a] = __fmaf_rn(__ldg(p.dir + r * 3 + a), zz, __ldg(p.ori + r * 3 + a));
+        tap_cell(bmin, inv_vs, pt, i0, wc);
 #pragma unroll
-        for (int cr = 0; cr < 8; cr++) {
-          const int dx = (cr >> 2) & 1, dy = (cr >> 1) & 1, dz = cr & 1;
-          s_w[w8][lane][cr] = (dx ? f[0] : 1.0f - f[0]) * (dy ? f[1] : 1.0f - f[1]) * (dz ? f[2] : 1.0f - f[2]);
-        }
+        for (int cr = 0; cr < 8; cr++) s_w[w8][lane][cr] = wc[cr];
         s_cell[w8][lane][0] = i0[0];
         s_cell[w8][lane][1] = i0[1];
         s_cell[w8][lane][2] = i0[2];
@@ -143,9 +135,10 @@ __global__ void __launch_bounds__(256) grid_scatter_kernel(ScatterParams p) {
         if (p.mode == 1) {
           // d sigma / d t of sigma = sigmoid(-t scale / s) / s at the gathered t
           float t1[1];
-          grid_tap<1>(p.grid + (size_t)b * p.D * p.D * p.D, p.D, bmin, vs, pt, t1);
-          const float sg = 1.0f / (1.0f + __expf(t1[0] * p.scale / p.s));
-          s_g[w8][lane][0] = __ldg(g) * (-sg * (1.0f - sg) * p.scale / (p.s * p.s));
+          grid_tap_cell<1>(p.grid + (size_t)b * p.D * p.D * p.D, p.D, i0, wc, t1);
+          const float k = p.scale / p.s;
+          const float sg = tsdf_sigmoid(t1[0], k);
+          s_g[w8][lane][0] = __ldg(g) * (-sg * (1.0f - sg) * (k * (1.0f / p.s)));
         } else {
 #pragma unroll
           for (int c = 0; c < C; c++) s_g[w8][lane][c] = __ldg(g + c);

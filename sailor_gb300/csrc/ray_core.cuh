@@ -337,13 +337,14 @@ __device__ __forceinline__ void ray_transmittance(const float (&al)[E], unsigned
 // (x,y,z) centred at bbox_min + (x,y,z) * vs, outside corners contribute 0)
 // ---------------------------------------------------------------------------
 // Cell (lower corner index) and the eight corner weights of a trilinear tap
-// at pt; corner cr = (dx, dy, dz) = bits (2, 1, 0) of cr.
-__device__ __forceinline__ void tap_cell(const float bmin[3], float vs, const float pt[3], int (&i0)[3],
+// at pt (u = (pt - bmin) * inv_vs in voxel units); corner cr = (dx, dy, dz)
+// = bits (2, 1, 0) of cr.
+__device__ __forceinline__ void tap_cell(const float bmin[3], float inv_vs, const float pt[3], int (&i0)[3],
                                          float (&w)[8]) {
   float f[3];
 #pragma unroll
   for (int a = 0; a < 3; a++) {
-    const float u = (pt[a] - bmin[a]) / vs;
+    const float u = (pt[a] - bmin[a]) * inv_vs;
     const float fl = floorf(u);
     i0[a] = (int)fl;
     f[a] = u - fl;
@@ -362,12 +363,11 @@ __device__ __forceinline__ bool corner_inside(const int (&i0)[3], int cr, int D,
   return true;
 }
 
+// Trilinear interpolation of a channel-last grid [D, D, D, C] for a given
+// cell and weights; corners outside the grid contribute 0.
 template <int C>
-__device__ __forceinline__ void grid_tap(const float *__restrict__ grid, int D, const float bmin[3], float vs,
-                                         const float pt[3], float (&acc)[C]) {
-  int i0[3];
-  float w[8];
-  tap_cell(bmin, vs, pt, i0, w);
+__device__ __forceinline__ void grid_tap_cell(const float *__restrict__ grid, int D, const int (&i0)[3],
+                                              const float (&w)[8], float (&acc)[C]) {
 #pragma unroll
   for (int c = 0; c < C; c++) acc[c] = 0.0f;
 #pragma unroll
@@ -375,15 +375,37 @@ __device__ __forceinline__ void grid_tap(const float *__restrict__ grid, int D, 
     size_t off;
     if (!corner_inside(i0, cr, D, off)) continue;
     const float *g = grid + off * C;
+    if constexpr (C % 4 == 0) {
 #pragma unroll
-    for (int c = 0; c < C; c++) acc[c] = __fmaf_rn(w[cr], __ldg(g + c), acc[c]);
+      for (int c4 = 0; c4 < C / 4; c4++) {
+        const float4 v = __ldg(reinterpret_cast<const float4 *>(g) + c4);
+        acc[4 * c4 + 0] = __fmaf_rn(w[cr], v.x, acc[4 * c4 + 0]);
+        acc[4 * c4 + 1] = __fmaf_rn(w[cr], v.y, acc[4 * c4 + 1]);
+        acc[4 * c4 + 2] = __fmaf_rn(w[cr], v.z, acc[4 * c4 + 2]);
+        acc[4 * c4 + 3] = __fmaf_rn(w[cr], v.w, acc[4 * c4 + 3]);
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < C; c++) acc[c] = __fmaf_rn(w[cr], __ldg(g + c), acc[c]);
+    }
   }
 }
 
-// density of a normalised TSDF value t: sigmoid(-t * scale / s) / s
-__device__ __forceinline__ float tsdf_density(float t, float scale, float s) {
-  const float v = t * scale / s;
-  return (1.0f / (1.0f + __expf(v))) / s;
+template <int C>
+__device__ __forceinline__ void grid_tap(const float *__restrict__ grid, int D, const float bmin[3], float inv_vs,
+                                         const float pt[3], float (&acc)[C]) {
+  int i0[3];
+  float w[8];
+  tap_cell(bmin, inv_vs, pt, i0, w);
+  grid_tap_cell<C>(grid, D, i0, w, acc);
 }
+
+// Density of a normalised TSDF value t: sigmoid(-t * scale / s) / s, with
+// k = scale / s and inv_s = 1 / s folded by the caller.  tsdf_sigmoid is
+// the sigmoid factor (kept by the adjoint: d sigma / d t = -k inv_s sg (1 - sg)).
+__device__ __forceinline__ float tsdf_sigmoid(float t, float k) {
+  return __fdividef(1.0f, 1.0f + __expf(t * k));
+}
+__device__ __forceinline__ float tsdf_density(float t, float k, float inv_s) { return tsdf_sigmoid(t, k) * inv_s; }
 
 }  // namespace sg

@@ -48,6 +48,8 @@ struct RenderParams {
   const float *fbbox, *fvs;
   const float *head;  // [3, C] or null (C == 3)
   float t_thres;
+  float dk, inv_s;    // density constants: sdf_scale / sdf_s, 1 / sdf_s
+  bool shared;        // feature grid on the TSDF grid's geometry (one tap cell)
   float *out_rgb, *out_depth, *out_ws, *out_alpha, *out_z;
   int *out_node;
   const float *g_rgb, *g_depth, *g_ws, *g_alpha;
@@ -93,10 +95,10 @@ __device__ __forceinline__ void eval_ray(const RenderParams &p, long r, int b, i
   warp_sort_samples(sm.z, sm.p, S, ev.done);
   const float *bb = p.sp.t.vol_bbox + 6 * b;
   const float bmin[3] = {bb[0], bb[2], bb[4]};
-  const float vs = __ldg(p.sp.t.voxel_size + b);
+  const float inv_vs = 1.0f / __ldg(p.sp.t.voxel_size + b);
   const float *fb = p.fbbox + 6 * b;
   const float fmin[3] = {fb[0], fb[2], fb[4]};
-  const float fvs = __ldg(p.fvs + b);
+  const float inv_fvs = 1.0f / __ldg(p.fvs + b);
   const float *tsdf = p.tsdf + (size_t)b * p.D * p.D * p.D;
   const float *feat = p.feat + (size_t)b * p.Df * p.Df * p.Df * C;
   const float o[3] = {__ldg(p.ori + r * 3), __ldg(p.ori + r * 3 + 1), __ldg(p.ori + r * 3 + 2)};
@@ -111,13 +113,16 @@ __device__ __forceinline__ void eval_ray(const RenderParams &p, long r, int b, i
       ev.valid |= 1u << e;
       const float pt[3] = {__fmaf_rn(dr[0], ev.z[e], o[0]), __fmaf_rn(dr[1], ev.z[e], o[1]),
                            __fmaf_rn(dr[2], ev.z[e], o[2])};
+      int i0[3];
+      float wc[8];
+      tap_cell(bmin, inv_vs, pt, i0, wc);
       float t1[1];
-      grid_tap<1>(tsdf, p.D, bmin, vs, pt, t1);
-      // tsdf_density, with the sigmoid kept for the adjoint
-      ev.s01[e] = 1.0f / (1.0f + __expf(t1[0] * p.sdf_scale / p.sdf_s));
-      ev.sg[e] = ev.s01[e] / p.sdf_s;
+      grid_tap_cell<1>(tsdf, p.D, i0, wc, t1);
+      ev.s01[e] = tsdf_sigmoid(t1[0], p.dk);  // kept for the adjoint
+      ev.sg[e] = ev.s01[e] * p.inv_s;
+      if (!p.shared) tap_cell(fmin, inv_fvs, pt, i0, wc);
       float fe[C];
-      grid_tap<C>(feat, p.Df, fmin, fvs, pt, fe);
+      grid_tap_cell<C>(feat, p.Df, i0, wc, fe);
       if (p.head) {
 #pragma unroll
         for (int k = 0; k < 3; k++) {
@@ -200,39 +205,62 @@ __global__ void __launch_bounds__(256) render_fwd_kernel(RenderParams p) {
 // ---------------------------------------------------------------------------
 // backward
 // ---------------------------------------------------------------------------
-// Slots of a lane: feature slots corner * C + channel in [0, 8C), TSDF
-// slots 8C + corner.
+// Scatter layout of the backward.  Feature gradient: with C == 16, lane l
+// owns corner l / 4, channels 4 (l % 4) .. 4 (l % 4) + 3 (one float4, flushed
+// with one vector reduction); with C == 3, lane l < 24 owns corner l / 3,
+// channel l % 3.  TSDF gradient: lane l owns corner l - kTsdfLane0<C> when
+// that is in [0, 8).
+// A trilinear cell (lower corner i0, each axis in [-1, D-1] when any corner
+// is inside the grid) packed into one non-negative key of 21 bits per axis;
+// -1 when no corner is inside (the sample contributes nothing).
+__device__ __forceinline__ long long cell_key(const int (&i0)[3], int D) {
+  if (i0[0] < -1 || i0[1] < -1 || i0[2] < -1 || i0[0] >= D || i0[1] >= D || i0[2] >= D) return -1;
+  return ((long long)(i0[0] + 1) << 42) | ((long long)(i0[1] + 1) << 21) | (long long)(i0[2] + 1);
+}
+
+struct Cell3 {
+  int v[3];
+};
+__device__ __forceinline__ Cell3 cell_of(long long k) {
+  return Cell3{{(int)(k >> 42) - 1, (int)((k >> 21) & 0x1fffff) - 1, (int)(k & 0x1fffff) - 1}};
+}
+
 template <int C>
-__device__ __forceinline__ void flush_slots(const RenderParams &p, int b, bool feat_part, const int (&cell)[3],
-                                            float *acc) {
-  constexpr int NF = 8 * C, NSLOT = (NF + 8 + 31) / 32;
+constexpr int kTsdfLane0 = (C == 3) ? 24 : 0;
+
+template <int C>
+__device__ __forceinline__ void flush_feat(const RenderParams &p, int b, const Cell3 &c3, float4 &acc) {
+  const int(&cell)[3] = c3.v;
   const int lane = lane_id();
-#pragma unroll
-  for (int q = 0; q < NSLOT; q++) {
-    const int slot = lane + 32 * q;
-    const bool mine = feat_part ? slot < NF : (slot >= NF && slot < NF + 8);
-    if (!mine) continue;
-    if (acc[q] != 0.0f) {
-      size_t off;
-      if (feat_part) {
-        const int cr = slot / C, ch = slot - cr * C;
-        if (corner_inside(cell, cr, p.Df, off))
-          atomicAdd(p.grad_feat + ((size_t)b * p.Df * p.Df * p.Df + off) * C + ch, acc[q]);
-      } else {
-        if (corner_inside(cell, slot - NF, p.D, off)) atomicAdd(p.grad_tsdf + (size_t)b * p.D * p.D * p.D + off, acc[q]);
-      }
-    }
-    acc[q] = 0.0f;
+  size_t off;
+  if constexpr (C == 16) {
+    if ((acc.x != 0.0f || acc.y != 0.0f || acc.z != 0.0f || acc.w != 0.0f) && corner_inside(cell, lane >> 2, p.Df, off))
+      red_add_f32x4(p.grad_feat + ((size_t)b * p.Df * p.Df * p.Df + off) * C + 4 * (lane & 3), acc.x, acc.y, acc.z,
+                    acc.w);
+  } else {
+    if (lane < 8 * C && acc.x != 0.0f && corner_inside(cell, lane / C, p.Df, off))
+      atomicAdd(p.grad_feat + ((size_t)b * p.Df * p.Df * p.Df + off) * C + lane % C, acc.x);
   }
+  acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+template <int C>
+__device__ __forceinline__ void flush_tsdf(const RenderParams &p, int b, const Cell3 &c3, float &acc) {
+  const int(&cell)[3] = c3.v;
+  const int cr = lane_id() - kTsdfLane0<C>;
+  size_t off;
+  if (cr >= 0 && cr < 8 && acc != 0.0f && corner_inside(cell, cr, p.D, off))
+    atomicAdd(p.grad_tsdf + (size_t)b * p.D * p.D * p.D + off, acc);
+  acc = 0.0f;
 }
 
 template <int E, int C>
 __global__ void __launch_bounds__(256) render_bwd_kernel(RenderParams p) {
+  static_assert(C == 3 || C == 16, "feature grids of 3 or 16 channels");
   SG_RENDER_SMEM(E)
-  constexpr int NF = 8 * C, NSLOT = (NF + 8 + 31) / 32;
   __shared__ float s_wf[8][32][9], s_wt[8][32][9];
-  __shared__ float s_g[8][32][C + 2];
-  __shared__ int s_cf[8][32][4], s_ct[8][32][4];
+  __shared__ __align__(16) float s_g[8][32][C == 16 ? 20 : 4];
+  __shared__ long long s_kf[8][32], s_kt[8][32];  // packed cell keys, -1: no contribution
   const int lane = lane_id();
   const int Smax = p.sp.S;
   for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < p.R;
@@ -320,87 +348,94 @@ __global__ void __launch_bounds__(256) render_bwd_kernel(RenderParams p) {
     // scatter into the grids, samples in sorted order
     const float *bb = p.sp.t.vol_bbox + 6 * b;
     const float bmin[3] = {bb[0], bb[2], bb[4]};
-    const float vs = __ldg(p.sp.t.voxel_size + b);
+    const float inv_vs = 1.0f / __ldg(p.sp.t.voxel_size + b);
     const float *fb = p.fbbox + 6 * b;
     const float fmin[3] = {fb[0], fb[2], fb[4]};
-    const float fvs = __ldg(p.fvs + b);
+    const float inv_fvs = 1.0f / __ldg(p.fvs + b);
     const float o[3] = {__ldg(p.ori + r * 3), __ldg(p.ori + r * 3 + 1), __ldg(p.ori + r * 3 + 2)};
     const float dr[3] = {__ldg(p.dir + r * 3), __ldg(p.dir + r * 3 + 1), __ldg(p.dir + r * 3 + 2)};
-    const float dsdt_k = -p.sdf_scale / (p.sdf_s * p.sdf_s);
-    float acc[NSLOT];
-#pragma unroll
-    for (int q = 0; q < NSLOT; q++) acc[q] = 0.0f;
-    int curf[3] = {INT_MIN, 0, 0}, curt[3] = {INT_MIN, 0, 0};
+    const float dsdt_k = -p.dk * p.inv_s;
+    // lane-owned accumulators: feature (corner, channels) and TSDF corner
+    float4 accf = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float acct = 0.0f;
+    const int fcr = (C == 16) ? (lane >> 2) : (lane < 8 * C ? lane / C : 0);
+    const int fch = (C == 16) ? 4 * (lane & 3) : (lane < 8 * C ? lane % C : 0);
+    const int tcr = lane - kTsdfLane0<C>;
+    const bool town = tcr >= 0 && tcr < 8;
+    long long curf = -1, curt = -1;
+    const bool want_t = p.grad_tsdf != nullptr, want_f = p.grad_feat != nullptr;
 #pragma unroll
     for (int e = 0; e < E; e++) {
       const bool use = (((ev.proc & ev.valid) >> e) & 1u) != 0;
+      long long kf = -1, kt = -1;
       if (use) {
         const float pt[3] = {__fmaf_rn(dr[0], ev.z[e], o[0]), __fmaf_rn(dr[1], ev.z[e], o[1]),
                              __fmaf_rn(dr[2], ev.z[e], o[2])};
         int i0[3];
         float wt[8];
-        tap_cell(fmin, fvs, pt, i0, wt);
+        tap_cell(bmin, inv_vs, pt, i0, wt);
+        if (want_t) {
+          kt = cell_key(i0, p.D);
 #pragma unroll
-        for (int a = 0; a < 3; a++) s_cf[w8][lane][a] = i0[a];
-#pragma unroll
-        for (int cr = 0; cr < 8; cr++) s_wf[w8][lane][cr] = wt[cr];
-        tap_cell(bmin, vs, pt, i0, wt);
-#pragma unroll
-        for (int a = 0; a < 3; a++) s_ct[w8][lane][a] = i0[a];
-#pragma unroll
-        for (int cr = 0; cr < 8; cr++) s_wt[w8][lane][cr] = wt[cr];
-        // feature gradient: head^T d rgb; TSDF gradient: d sigma / d t
-#pragma unroll
-        for (int c = 0; c < C; c++) {
-          float g;
-          if (p.head)
-            g = __fmaf_rn(__ldg(p.head + 2 * C + c), grgb[e][2],
-                          __fmaf_rn(__ldg(p.head + C + c), grgb[e][1], __ldg(p.head + c) * grgb[e][0]));
-          else
-            g = c < 3 ? grgb[e][c] : 0.0f;
-          s_g[w8][lane][c] = g;
+          for (int cr = 0; cr < 8; cr++) s_wt[w8][lane][cr] = wt[cr];
+          s_g[w8][lane][C == 16 ? 16 : 3] = gsig[e] * (ev.s01[e] * (1.0f - ev.s01[e]) * dsdt_k);
         }
-        s_g[w8][lane][C] = gsig[e] * (ev.s01[e] * (1.0f - ev.s01[e]) * dsdt_k);
+        if (want_f) {
+          if (!p.shared) tap_cell(fmin, inv_fvs, pt, i0, wt);
+          kf = cell_key(i0, p.Df);
+#pragma unroll
+          for (int cr = 0; cr < 8; cr++) s_wf[w8][lane][cr] = wt[cr];
+          // feature gradient: head^T d rgb
+#pragma unroll
+          for (int c = 0; c < C; c++) {
+            float g;
+            if (p.head)
+              g = __fmaf_rn(__ldg(p.head + 2 * C + c), grgb[e][2],
+                            __fmaf_rn(__ldg(p.head + C + c), grgb[e][1], __ldg(p.head + c) * grgb[e][0]));
+            else
+              g = c < 3 ? grgb[e][c] : 0.0f;
+            s_g[w8][lane][c] = g;
+          }
+        }
       }
-      s_cf[w8][lane][3] = use;
+      s_kf[w8][lane] = kf;
+      s_kt[w8][lane] = kt;
       __syncwarp();
-      for (int j = 0; j < 32; j++) {
-        if (!s_cf[w8][j][3]) continue;
-        if (p.grad_feat) {
-          const int c3[3] = {s_cf[w8][j][0], s_cf[w8][j][1], s_cf[w8][j][2]};
-          if (c3[0] != curf[0] || c3[1] != curf[1] || c3[2] != curf[2]) {
-            if (curf[0] != INT_MIN) flush_slots<C>(p, b, true, curf, acc);
-            curf[0] = c3[0];
-            curf[1] = c3[1];
-            curf[2] = c3[2];
+      if (want_f) {
+        for (int j = 0; j < 32; j++) {
+          const long long k = s_kf[w8][j];
+          if (k < 0) continue;
+          if (k != curf) {
+            if (curf >= 0) flush_feat<C>(p, b, cell_of(curf), accf);
+            curf = k;
+          }
+          const float wf = s_wf[w8][j][fcr];
+          if constexpr (C == 16) {
+            const float4 g4 = *reinterpret_cast<const float4 *>(&s_g[w8][j][fch]);
+            accf.x = __fmaf_rn(wf, g4.x, accf.x);
+            accf.y = __fmaf_rn(wf, g4.y, accf.y);
+            accf.z = __fmaf_rn(wf, g4.z, accf.z);
+            accf.w = __fmaf_rn(wf, g4.w, accf.w);
+          } else {
+            accf.x = __fmaf_rn(wf, s_g[w8][j][fch], accf.x);
           }
         }
-        if (p.grad_tsdf) {
-          const int c3[3] = {s_ct[w8][j][0], s_ct[w8][j][1], s_ct[w8][j][2]};
-          if (c3[0] != curt[0] || c3[1] != curt[1] || c3[2] != curt[2]) {
-            if (curt[0] != INT_MIN) flush_slots<C>(p, b, false, curt, acc);
-            curt[0] = c3[0];
-            curt[1] = c3[1];
-            curt[2] = c3[2];
+      }
+      if (want_t) {
+        for (int j = 0; j < 32; j++) {
+          const long long k = s_kt[w8][j];
+          if (k < 0) continue;
+          if (k != curt) {
+            if (curt >= 0) flush_tsdf<C>(p, b, cell_of(curt), acct);
+            curt = k;
           }
-        }
-#pragma unroll
-        for (int q = 0; q < NSLOT; q++) {
-          const int slot = lane + 32 * q;
-          if (slot < NF) {
-            if (p.grad_feat) {
-              const int cr = slot / C, ch = slot - cr * C;
-              acc[q] = __fmaf_rn(s_wf[w8][j][cr], s_g[w8][j][ch], acc[q]);
-            }
-          } else if (slot < NF + 8) {
-            if (p.grad_tsdf) acc[q] = __fmaf_rn(s_wt[w8][j][slot - NF], s_g[w8][j][C], acc[q]);
-          }
+          if (town) acct = __fmaf_rn(s_wt[w8][j][tcr], s_g[w8][j][C == 16 ? 16 : 3], acct);
         }
       }
       __syncwarp();
     }
-    if (p.grad_feat && curf[0] != INT_MIN) flush_slots<C>(p, b, true, curf, acc);
-    if (p.grad_tsdf && curt[0] != INT_MIN) flush_slots<C>(p, b, false, curt, acc);
+    if (curf >= 0) flush_feat<C>(p, b, cell_of(curf), accf);
+    if (curt >= 0) flush_tsdf<C>(p, b, cell_of(curt), acct);
     __syncwarp();
   }
 }
@@ -471,6 +506,10 @@ static int segment_params(const SgTree *tree, const SgRaySegments *seg, const Sg
   p.fvs = a->feat_vs;
   p.head = a->head;
   p.t_thres = a->t_thres;
+  p.dk = a->sdf_scale / a->sdf_s;
+  p.inv_s = 1.0f / a->sdf_s;
+  p.shared = a->Df == a->D && a->feat_bbox == tree->vol_bbox && a->feat_vs == tree->voxel_size;
+  if (a->C == 16 && (((uintptr_t)a->feat) % 16 != 0)) return SG_ERR_INVALID_ARG;
   return SG_OK;
 }
 
@@ -511,6 +550,9 @@ extern "C" int sg_render_fused(const SgTree *tree, const int *hit_idx, const flo
   p.fvs = color_vs;
   p.head = nullptr;
   p.t_thres = t_thres;
+  p.dk = sdf_scale / sdf_s;
+  p.inv_s = 1.0f / sdf_s;
+  p.shared = Dc == D && color_bbox == tree->vol_bbox && color_vs == tree->voxel_size;
   p.out_rgb = out_rgb;
   p.out_depth = out_depth;
   p.out_ws = out_ws;

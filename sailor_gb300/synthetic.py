@@ -117,11 +117,25 @@ def cast_depth(prims, K, R, T, res):
     dw = dcam @ R                              # R^T dcam
     ow = np.broadcast_to(-R.T @ T, dw.shape)
     t = np.full(dw.shape[0], np.inf)
+    o0 = -R.T @ T
+    dn = np.sqrt(np.einsum("ij,ij->i", dw, dw))
     for p in prims:
+        # only rays that pass the primitive's bounding sphere can hit it
         if p[0] == "capsule":
-            t = np.minimum(t, _hit_capsule(ow, dw, p[1], p[2], p[3]))
+            c, rb = 0.5 * (p[1] + p[2]), 0.5 * np.linalg.norm(p[2] - p[1]) + p[3]
         else:
-            t = np.minimum(t, _hit_ellipsoid(ow, dw, p[1], p[2], p[3]))
+            c, rb = p[1], float(np.max(p[2]))
+        oc = c - o0
+        cr = np.cross(dw, oc)
+        near = np.sqrt(np.einsum("ij,ij->i", cr, cr)) <= (rb * 1.001 + 1e-6) * dn
+        if not near.any():
+            continue
+        sel = np.nonzero(near)[0]
+        if p[0] == "capsule":
+            th = _hit_capsule(ow[sel], dw[sel], p[1], p[2], p[3])
+        else:
+            th = _hit_ellipsoid(ow[sel], dw[sel], p[1], p[2], p[3])
+        t[sel] = np.minimum(t[sel], th)
     z = np.where(np.isfinite(t), t, 0.0)       # dcam.z == 1, so t is z-depth
     return z.reshape(res, res)
 
@@ -209,32 +223,43 @@ def _view_images(rng, prims, K, R, T, res, noise, dropout):
     return depth, color
 
 
+def _batch_frame(job):
+    seed, b, n_prims, views, view_res, noise, dropout = job
+    frng = np.random.default_rng(seed * 1000 + 17 * b + 1)
+    prims = random_primitives(frng, n_prims)
+    nv = int(frng.integers(views[0], views[1] + 1))
+    cams = ring_cameras(nv, phase=frng.uniform(0, 2 * math.pi))
+    fr = dict(K=[], RT=[], depth=[], color=[])
+    for R, T in cams:
+        res = int(frng.choice(view_res))
+        K = intrinsics(res)
+        depth, color = _view_images(frng, prims, K, R, T, res, noise, dropout)
+        fr["K"].append(K.astype(np.float32))
+        fr["RT"].append(np.concatenate([R, T[:, None]], 1).astype(np.float32))
+        fr["depth"].append(depth)
+        fr["color"].append(color)
+    return fr
+
+
 def make_batch_workload(seed=0, n_frames=8, views=(4, 8), view_res=(512, 768, 1024), n_prims=12, D=256,
                         trunc=0.03, n_targets=16, target_res=(256, 1024), target_S=(32, 48, 64, 96, 128),
-                        noise=0.005, dropout=0.02):
+                        noise=0.005, dropout=0.02, workers=1):
     """Frames of uneven view counts and resolutions, each with its own seeded
-    scene, and target cameras of uneven sizes and sample counts.
+    scene, and target cameras of uneven sizes and sample counts.  workers > 1
+    generates the frames in that many spawned processes (same result).
 
     Returns dict(frames=[dict(K, RT, depth, color) lists per view],
     vol_bbox [B,3,2], voxel_size [B], trunc_weight, D,
     targets=[dict(frame, res, S, ori [res*res,3], dir [res*res,3])])."""
+    jobs = [(seed, b, n_prims, views, view_res, noise, dropout) for b in range(n_frames)]
+    if workers > 1:
+        import concurrent.futures as cf
+        import multiprocessing as mp
+        with cf.ProcessPoolExecutor(min(workers, n_frames), mp_context=mp.get_context("spawn")) as ex:
+            frames = list(ex.map(_batch_frame, jobs))
+    else:
+        frames = [_batch_frame(j) for j in jobs]
     rng = np.random.default_rng(seed)
-    frames = []
-    for b in range(n_frames):
-        frng = np.random.default_rng(seed * 1000 + 17 * b + 1)
-        prims = random_primitives(frng, n_prims)
-        nv = int(frng.integers(views[0], views[1] + 1))
-        cams = ring_cameras(nv, phase=frng.uniform(0, 2 * math.pi))
-        fr = dict(K=[], RT=[], depth=[], color=[])
-        for R, T in cams:
-            res = int(frng.choice(view_res))
-            K = intrinsics(res)
-            depth, color = _view_images(frng, prims, K, R, T, res, noise, dropout)
-            fr["K"].append(K.astype(np.float32))
-            fr["RT"].append(np.concatenate([R, T[:, None]], 1).astype(np.float32))
-            fr["depth"].append(depth)
-            fr["color"].append(color)
-        frames.append(fr)
     lo, hi = target_res
     sizes = np.linspace(lo, hi, n_targets)
     sizes = (np.round(sizes / 32.0) * 32).astype(int)
