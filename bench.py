@@ -268,9 +268,11 @@ def batch_algorithmic_bytes(bcfg, w, n_hits, R, n_samples):
         intersect=24 * R + 12 * n_hits + 8 * R,
         # hit rows + per-ray count / valid length + ray + 24 B/ray out
         forward=12 * n_hits + 8 * R + 24 * R + 24 * R,
-        # as forward, upstream gradient in, and the gradient grids zeroed and
-        # written (the dense grids are the contract of the adjoint)
-        backward=12 * n_hits + 8 * R + 24 * R + 12 * R + 2 * 4 * V * (C + 1),
+        # as forward, with the upstream colour gradient in; the atomic adds
+        # into the feature-gradient grid are not counted
+        backward=12 * n_hits + 8 * R + 24 * R + 12 * R,
+        # loss gradient and the zeroing of the feature-gradient grid
+        grad_prep=4 * V * C + 36 * R,
     )
 
 
@@ -521,7 +523,7 @@ def run_batch(args):
         tpath = os.path.join(ROOT, "profiles", "traffic.json")
         if os.path.exists(tpath):
             traffic = json.load(open(tpath)).get("batch_" + dom)
-        render_ms = sum(stages.get(k, 0.0) for k in ("intersect", "forward", "backward"))
+        render_ms = sum(stages.get(k, 0.0) for k in ("intersect", "forward", "grad_prep", "backward"))
         out = dict(
             metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=args.steps, warmup=args.warmup,
             ms_per_step=ms_max, higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32",

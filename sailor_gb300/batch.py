@@ -217,6 +217,7 @@ class BatchPipeline:
             self.grad_feat.zero_()
             if tsdf_grad:
                 self.grad_tsdf.zero_()
+        self._mark("grad_prep")
         N.check(N.lib.sg_render_segments_bwd(C.byref(self.tree), C.byref(self.seg), C.byref(self.args),
                                              N.ptr(g_rgb), N.ptr(g_depth), N.ptr(g_ws), N.ptr(g_alpha),
                                              N.ptr(self.grad_feat), N.ptr(self.grad_tsdf) if tsdf_grad else None,
