@@ -268,11 +268,12 @@ def batch_algorithmic_bytes(bcfg, w, n_hits, R, n_samples):
         intersect=24 * R + 12 * n_hits + 8 * R,
         # hit rows + per-ray count / valid length + ray + 24 B/ray out
         forward=12 * n_hits + 8 * R + 24 * R + 24 * R,
-        # as forward, with the upstream colour gradient in; the atomic adds
-        # into the feature-gradient grid are not counted
-        backward=12 * n_hits + 8 * R + 24 * R + 12 * R,
-        # loss gradient and the zeroing of the feature-gradient grid
-        grad_prep=4 * V * C + 36 * R,
+        # fused training pass: as forward, with the target colour in and the
+        # per-ray loss out; the atomic adds into the feature-gradient grid
+        # are not counted
+        train=12 * n_hits + 8 * R + 24 * R + 12 * R + 24 * R + 4 * R,
+        # zeroing of the feature-gradient grid
+        grad_prep=4 * V * C,
     )
 
 
@@ -403,9 +404,7 @@ def run_batch(args):
     if not args.no_autotune:
         from sailor_gb300 import autotune
         autotune.set_knob("fuse_tiled", 1)
-        tuned = autotune.tune({"isect_block": bp.intersect,
-                               "render_warps": lambda: (bp.forward(), bp.backward(bp.g_rgb))},
-                              verbose=True)
+        tuned = autotune.tune({"isect_block": bp.intersect, "render_warps": bp.train_step}, verbose=True)
         tuned.update(fuse_tiled=1)
     for _ in range(max(args.warmup - 1, 0)):
         bp.train_step()
@@ -523,7 +522,7 @@ def run_batch(args):
         tpath = os.path.join(ROOT, "profiles", "traffic.json")
         if os.path.exists(tpath):
             traffic = json.load(open(tpath)).get("batch_" + dom)
-        render_ms = sum(stages.get(k, 0.0) for k in ("intersect", "forward", "grad_prep", "backward"))
+        render_ms = sum(stages.get(k, 0.0) for k in ("intersect", "grad_prep", "train"))
         out = dict(
             metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=args.steps, warmup=args.warmup,
             ms_per_step=ms_max, higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32",

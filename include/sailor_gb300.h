@@ -416,6 +416,21 @@ int sg_render_segments_bwd(const SgTree *tree, const SgRaySegments *seg,
                            float *grad_tsdf, float *grad_sigma,
                            float *grad_rgb, sg_stream_t stream);
 
+/* Training step of the batched render in one pass per ray: the forward
+ * (outputs written as by sg_render_segments_fwd), the per-ray loss
+ * loss_scale / 2 * |rgb - target_rgb|^2 (out_loss [R], may be NULL), and
+ * the backward for the upstream gradient loss_scale * (rgb - target_rgb)
+ * (as sg_render_segments_bwd: gradients accumulated into grad_feat and, if
+ * not NULL, grad_tsdf).  Nothing is recomputed and nothing per sample is
+ * stored.  With loss_scale = 2 / (3 R) the loss summed over rays is the mean
+ * squared colour error. */
+int sg_render_segments_train(const SgTree *tree, const SgRaySegments *seg,
+                             const SgRenderArgs *args, const float *target_rgb,
+                             float loss_scale, float *out_rgb, float *out_depth,
+                             float *out_ws, float *out_alpha, float *out_loss,
+                             float *grad_feat, float *grad_tsdf,
+                             sg_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -22,7 +22,7 @@ EXPORTS = (
     "sg_trilerp_nodes_fwd", "sg_trilerp_nodes_bwd", "sg_sample_sorted", "sg_grid_gather",
     "sg_render_fused", "sg_tune_set", "sg_tune_get", "sg_tree_build_static",
     "sg_grid_scatter", "sg_fuse_tsdf_views", "sg_intersect_segments", "sg_render_segments_fwd",
-    "sg_render_segments_bwd",
+    "sg_render_segments_bwd", "sg_render_segments_train",
 )
 
 
@@ -90,6 +90,7 @@ def _load():
     lib.sg_intersect_segments.argtypes = [T, G, p, p, i, p, p, p, p, p, p, p]
     lib.sg_render_segments_fwd.argtypes = [T, G, A, p, p, p, p, p, p, p]
     lib.sg_render_segments_bwd.argtypes = [T, G, A, p, p, p, p, p, p, p, p, p]
+    lib.sg_render_segments_train.argtypes = [T, G, A, p, f, p, p, p, p, p, p, p, p]
     lib.sg_tune_set.argtypes = [i, i]
     lib.sg_tune_get.argtypes = [i]
     lib.sg_trilerp_nodes_fwd.argtypes = [C.POINTER(SgTree), p, p, p, p, p, i, i, i, p, p]

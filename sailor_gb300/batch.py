@@ -123,6 +123,7 @@ class BatchPipeline:
         self.out_alpha = torch.empty(R, **f32)
         self.target_rgb = torch.zeros((R, 3), **f32)
         self.g_rgb = torch.empty((R, 3), **f32)
+        self.out_loss = torch.empty(R, **f32)
         self.args = None
         self.trunc_weight = None
         self.events = None
@@ -225,8 +226,27 @@ class BatchPipeline:
         self._mark("backward")
 
     def train_step(self):
-        """Build, intersect, forward, gradient of the mean squared colour error
-        against target_rgb, backward.  Allocates nothing."""
+        """Build, intersect, then one fused pass per ray: forward, the mean
+        squared colour error against target_rgb (per-ray terms in out_loss)
+        and its backward into grad_feat (and grad_tsdf when train_tsdf).
+        Allocates nothing."""
+        self.build()
+        self.intersect()
+        self.grad_feat.zero_()
+        if self.train_tsdf:
+            self.grad_tsdf.zero_()
+        self._mark("grad_prep")
+        N.check(N.lib.sg_render_segments_train(
+            C.byref(self.tree), C.byref(self.seg), C.byref(self.args), N.ptr(self.target_rgb),
+            2.0 / (3.0 * self.R), N.ptr(self.out_rgb), N.ptr(self.out_depth), N.ptr(self.out_ws),
+            N.ptr(self.out_alpha), N.ptr(self.out_loss), N.ptr(self.grad_feat),
+            N.ptr(self.grad_tsdf) if self.train_tsdf else None, N.stream()), "render_train")
+        self._mark("train")
+
+    def train_step_unfused(self):
+        """The same step with separate forward and backward launches (the
+        backward recomputes each ray) and the loss gradient formed between
+        them."""
         self.build()
         self.intersect()
         self.forward()

@@ -54,6 +54,10 @@ struct RenderParams {
   int *out_node;
   const float *g_rgb, *g_depth, *g_ws, *g_alpha;
   float *grad_feat, *grad_tsdf, *grad_sigma, *grad_rgb;
+  // training step: upstream gradient of loss_scale / 2 * |rgb - target|^2
+  const float *target_rgb;
+  float loss_scale;
+  float *out_loss;
 };
 
 __device__ __forceinline__ void ray_frame(const RenderParams &p, long r, int &b, int &S) {
@@ -254,7 +258,11 @@ __device__ __forceinline__ void flush_tsdf(const RenderParams &p, int b, const C
   acc = 0.0f;
 }
 
-template <int E, int C>
+// TRAIN: the upstream gradient is formed in the kernel from the ray's own
+// outputs (loss = loss_scale / 2 * |rgb - target|^2 per ray, so d loss /
+// d rgb = loss_scale * (rgb - target)); the outputs and per-ray loss are
+// written, and nothing is recomputed.
+template <int E, int C, bool TRAIN>
 __global__ void __launch_bounds__(256) render_bwd_kernel(RenderParams p) {
   static_assert(C == 3 || C == 16, "feature grids of 3 or 16 channels");
   SG_RENDER_SMEM(E)
@@ -276,14 +284,31 @@ __global__ void __launch_bounds__(256) render_bwd_kernel(RenderParams p) {
           for (int k = 0; k < 3; k++) p.grad_rgb[((size_t)r * Smax + i) * 3 + k] = 0.0f;
         }
       }
+      if (TRAIN && lane == 0) {
+        // no sample: zero outputs, loss of the target alone, no gradient
+        float l = 0.0f;
+        for (int k = 0; k < 3; k++) {
+          const float t = __ldg(p.target_rgb + r * 3 + k);
+          p.out_rgb[r * 3 + k] = 0.0f;
+          l += t * t;
+        }
+        p.out_depth[r] = p.out_ws[r] = p.out_alpha[r] = 0.0f;
+        if (p.out_loss) p.out_loss[r] = 0.5f * p.loss_scale * l;
+      }
       __syncwarp();
       continue;
     }
-    const float gc[3] = {p.g_rgb ? __ldg(p.g_rgb + r * 3) : 0.0f, p.g_rgb ? __ldg(p.g_rgb + r * 3 + 1) : 0.0f,
-                         p.g_rgb ? __ldg(p.g_rgb + r * 3 + 2) : 0.0f};
-    const float gd = p.g_depth ? __ldg(p.g_depth + r) : 0.0f;
-    const float gws = p.g_ws ? __ldg(p.g_ws + r) : 0.0f;
-    const float ga = p.g_alpha ? __ldg(p.g_alpha + r) : 0.0f;
+    float gc[3] = {0.0f, 0.0f, 0.0f}, gd = 0.0f, gws = 0.0f, ga = 0.0f;
+    if (!TRAIN) {
+      if (p.g_rgb) {
+        gc[0] = __ldg(p.g_rgb + r * 3);
+        gc[1] = __ldg(p.g_rgb + r * 3 + 1);
+        gc[2] = __ldg(p.g_rgb + r * 3 + 2);
+      }
+      gd = p.g_depth ? __ldg(p.g_depth + r) : 0.0f;
+      gws = p.g_ws ? __ldg(p.g_ws + r) : 0.0f;
+      ga = p.g_alpha ? __ldg(p.g_alpha + r) : 0.0f;
+    }
     // weights and inclusive prefix sums over sorted positions of
     // w*rgb, w*z, w, w*alpha; totals by carries (the forward's outputs)
     float w[E], pf[E][3], pd[E], pw[E], pa[E];
@@ -306,6 +331,25 @@ __global__ void __launch_bounds__(256) render_bwd_kernel(RenderParams p) {
       cd += __shfl_sync(SG_FULL, vd, 31);
       cw += __shfl_sync(SG_FULL, vw, 31);
       ca += __shfl_sync(SG_FULL, va, 31);
+    }
+    if (TRAIN) {
+      // forward outputs = the totals; upstream gradient of the per-ray loss
+      float l = 0.0f;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        const float d = cf[k] - __ldg(p.target_rgb + r * 3 + k);
+        gc[k] = p.loss_scale * d;
+        l += d * d;
+      }
+      if (lane == 0) {
+        p.out_rgb[r * 3 + 0] = cf[0];
+        p.out_rgb[r * 3 + 1] = cf[1];
+        p.out_rgb[r * 3 + 2] = cf[2];
+        p.out_depth[r] = cd;
+        p.out_ws[r] = cw;
+        p.out_alpha[r] = ca;
+        if (p.out_loss) p.out_loss[r] = 0.5f * p.loss_scale * l;
+      }
     }
     // exact adjoint per sorted position: d out / d sigma_i = delta_i *
     // (T_{i+1} v_i - sum_{j>i} w_j v_j) (v = rgb, z, 1; 2 alpha T_{i+1} for
@@ -446,30 +490,30 @@ static int render_grid(long R) {
   return (int)(g < cap ? g : cap);
 }
 
+// mode 0: forward, 1: backward, 2: training step (forward + loss + backward)
+template <int E, int C>
+static void launch_render_e(const RenderParams &p, int mode, int g, sg_stream_t stream) {
+  if (mode == 0) render_fwd_kernel<E, C><<<g, 256, 0, stream>>>(p);
+  else if (mode == 1) render_bwd_kernel<E, C, false><<<g, 256, 0, stream>>>(p);
+  else render_bwd_kernel<E, C, true><<<g, 256, 0, stream>>>(p);
+}
+
 template <int C>
-static int launch_render(const RenderParams &p, bool bwd, int g, sg_stream_t stream) {
+static int launch_render(const RenderParams &p, int mode, int g, sg_stream_t stream) {
   const int S = p.sp.S;
-  if (S <= 32) {
-    if (bwd) render_bwd_kernel<1, C><<<g, 256, 0, stream>>>(p);
-    else render_fwd_kernel<1, C><<<g, 256, 0, stream>>>(p);
-  } else if (S <= 64) {
-    if (bwd) render_bwd_kernel<2, C><<<g, 256, 0, stream>>>(p);
-    else render_fwd_kernel<2, C><<<g, 256, 0, stream>>>(p);
-  } else if (S <= 128) {
-    if (bwd) render_bwd_kernel<4, C><<<g, 256, 0, stream>>>(p);
-    else render_fwd_kernel<4, C><<<g, 256, 0, stream>>>(p);
-  } else {
-    return SG_ERR_UNSUPPORTED;
-  }
+  if (S <= 32) launch_render_e<1, C>(p, mode, g, stream);
+  else if (S <= 64) launch_render_e<2, C>(p, mode, g, stream);
+  else if (S <= 128) launch_render_e<4, C>(p, mode, g, stream);
+  else return SG_ERR_UNSUPPORTED;
   SG_LAUNCH_CHECK();
   return SG_OK;
 }
 
-static int launch_render_c(const RenderParams &p, int C, bool bwd, sg_stream_t stream) {
+static int launch_render_c(const RenderParams &p, int C, int mode, sg_stream_t stream) {
   if (p.R <= 0) return SG_OK;
   const int g = render_grid(p.R);
-  if (C == 3) return launch_render<3>(p, bwd, g, stream);
-  if (C == 16) return launch_render<16>(p, bwd, g, stream);
+  if (C == 3) return launch_render<3>(p, mode, g, stream);
+  if (C == 16) return launch_render<16>(p, mode, g, stream);
   return SG_ERR_UNSUPPORTED;
 }
 
@@ -559,7 +603,7 @@ extern "C" int sg_render_fused(const SgTree *tree, const int *hit_idx, const flo
   p.out_alpha = out_alpha;
   p.out_z = out_z;
   p.out_node = out_node;
-  return launch_render_c(p, 3, false, stream);
+  return launch_render_c(p, 3, 0, stream);
 }
 
 extern "C" int sg_render_segments_fwd(const SgTree *tree, const SgRaySegments *seg, const SgRenderArgs *args,
@@ -576,7 +620,7 @@ extern "C" int sg_render_segments_fwd(const SgTree *tree, const SgRaySegments *s
   p.out_alpha = out_alpha;
   p.out_z = out_z;
   p.out_node = out_node;
-  return launch_render_c(p, args->C, false, stream);
+  return launch_render_c(p, args->C, 0, stream);
 }
 
 extern "C" int sg_render_segments_bwd(const SgTree *tree, const SgRaySegments *seg, const SgRenderArgs *args,
@@ -595,5 +639,25 @@ extern "C" int sg_render_segments_bwd(const SgTree *tree, const SgRaySegments *s
   p.grad_tsdf = grad_tsdf;
   p.grad_sigma = grad_sigma;
   p.grad_rgb = grad_rgb;
-  return launch_render_c(p, args->C, true, stream);
+  return launch_render_c(p, args->C, 1, stream);
+}
+
+extern "C" int sg_render_segments_train(const SgTree *tree, const SgRaySegments *seg, const SgRenderArgs *args,
+                                        const float *target_rgb, float loss_scale, float *out_rgb,
+                                        float *out_depth, float *out_ws, float *out_alpha, float *out_loss,
+                                        float *grad_feat, float *grad_tsdf, sg_stream_t stream) {
+  RenderParams p;
+  int rc = segment_params(tree, seg, args, p);
+  if (rc != SG_OK) return rc;
+  if (!target_rgb || !out_rgb || !out_depth || !out_ws || !out_alpha) return SG_ERR_INVALID_ARG;
+  p.target_rgb = target_rgb;
+  p.loss_scale = loss_scale;
+  p.out_loss = out_loss;
+  p.out_rgb = out_rgb;
+  p.out_depth = out_depth;
+  p.out_ws = out_ws;
+  p.out_alpha = out_alpha;
+  p.grad_feat = grad_feat;
+  p.grad_tsdf = grad_tsdf;
+  return launch_render_c(p, args->C, 2, stream);
 }

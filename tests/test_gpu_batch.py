@@ -226,3 +226,23 @@ def test_train_step_graph_replay(work):
         assert torch.equal(bp.tsdf, ref[2])
         for got, r in ((bp.grad_feat, ref[3]), (bp.grad_tsdf, ref[4])):
             assert (got - r).abs().max().item() <= 1e-5 * max(r.abs().max().item(), 1e-12)
+
+
+def test_fused_train_step_matches_unfused(work):
+    """sg_render_segments_train (forward + per-ray loss + backward in one
+    pass) against the forward kernel, the loss gradient formed in torch, and
+    the backward kernel: outputs within 1e-5 (only the summation order of
+    the colour sums differs), loss = mean squared colour error, feature-grid
+    gradient within 1e-5 of its largest value."""
+    bp = _pipeline(work)
+    bp.train_step_unfused()
+    torch.cuda.synchronize()
+    ref = [t.clone() for t in (bp.out_rgb, bp.out_depth, bp.out_ws, bp.out_alpha, bp.grad_feat)]
+    mse = ((bp.out_rgb - bp.target_rgb) ** 2).mean().item()
+    bp.train_step()
+    torch.cuda.synchronize()
+    for got, r in zip((bp.out_rgb, bp.out_depth, bp.out_ws, bp.out_alpha), ref[:4]):
+        assert (got - r).abs().max().item() <= 1e-5 * max(1.0, r.abs().max().item())
+    assert abs(bp.out_loss.sum().item() - mse) <= 1e-5 * max(mse, 1e-12) + 1e-9
+    m = ref[4].abs().max().item()
+    assert m > 0 and (bp.grad_feat - ref[4]).abs().max().item() <= 1e-5 * m
