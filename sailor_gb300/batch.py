@@ -127,6 +127,7 @@ class BatchPipeline:
         self.args = None
         self.trunc_weight = None
         self.events = None
+        self.side = torch.cuda.Stream(device=dev)  # zeroing of the gradient grids beside the build
 
     # ------------------------------------------------------------------ inputs
     def load_views(self, frames, vol_bbox, voxel_size, trunc_weight):
@@ -229,12 +230,18 @@ class BatchPipeline:
         """Build, intersect, then one fused pass per ray: forward, the mean
         squared colour error against target_rgb (per-ray terms in out_loss)
         and its backward into grad_feat (and grad_tsdf when train_tsdf).
-        Allocates nothing."""
+        Allocates nothing.  The gradient grids are zeroed on a side stream
+        while fusion, tree build and intersection run (a memory-bound fill
+        beside compute-bound stages); the training pass waits for both."""
+        main = torch.cuda.current_stream()
+        self.side.wait_stream(main)  # the previous step's users of the grids come first
+        with torch.cuda.stream(self.side):
+            self.grad_feat.zero_()
+            if self.train_tsdf:
+                self.grad_tsdf.zero_()
         self.build()
         self.intersect()
-        self.grad_feat.zero_()
-        if self.train_tsdf:
-            self.grad_tsdf.zero_()
+        main.wait_stream(self.side)
         self._mark("grad_prep")
         N.check(N.lib.sg_render_segments_train(
             C.byref(self.tree), C.byref(self.seg), C.byref(self.args), N.ptr(self.target_rgb),
