@@ -63,6 +63,26 @@ def parse():
     return ap.parse_args()
 
 
+
+def dist_env():
+    """(world size, rank, local rank) of a torchrun launch; (1, 0, 0) alone."""
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def whole_job(ms_per_step, units_per_rank, world, device):
+    """Replicas: every rank processes its own units_per_rank per step; the
+    job's step time is the slowest rank's (max over ranks), and the job's
+    throughput is world * units_per_rank over that time.  Returns (ms_max,
+    units per second)."""
+    import torch
+    t = torch.tensor([float(ms_per_step)], device=device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    return ms_max, world * units_per_rank / (ms_max / 1000.0)
+
 def workload(cfg, rank=0):
     from sailor_gb300 import synthetic as syn
     seed = cfg["seed"] + 1000 * rank
@@ -193,27 +213,47 @@ def cpu_baseline(sc, ori, dirs, cfg, color_grid, color_vs, ray_sample=16384, fus
 
 def run_reference(args):
     """--impl reference: the reference's CPU implementation of the path (the
-    oracle port of its kernels), all host threads, bounded sample per step."""
-    rank = int(os.environ.get("RANK", 0))
+    oracle port of its kernels), all host threads, on a bounded sample of
+    the same workload as this arm per step.  Rank 0 alone runs and prints."""
+    world, rank, _ = dist_env()
     if rank != 0:
         return
-    cfg = dict(CFG)
-    if args.small:
-        cfg.update(res=512, D=256, trunc=0.03, target=512, S=64, prims=12)
-    sc, ori, dirs, color_grid, color_vs = workload(cfg)
-    fz = cpu_fused_grid(sc, cfg)
+    if args.workload == "batch":
+        from oracle import oracle as orc
+        bcfg = dict(BATCH_SMALL if args.small else BATCH)
+        w = batch_workload(bcfg)
+        rng = np.random.default_rng(bcfg["seed"] + 5)
+        D, C = bcfg["D"], bcfg["C"]
+        feat0 = rng.standard_normal((1, D, D, D, C), dtype=np.float32) * np.float32(0.1)
+        head = rng.standard_normal((3, C), dtype=np.float32) * np.float32(0.5)
+        K, RT, dep, col = padded_views(w["frames"][0])
+        fz = orc.integrate(K, RT, col, dep, D, w["vol_bbox"][:1], w["voxel_size"][:1].reshape(1, 1),
+                           trunc_weight=w["trunc_weight"])
+        run = lambda: cpu_baseline_batch(w, bcfg, feat0, head, fz=fz)  # noqa: E731
+        R = sum(t["ori"].shape[0] for t in w["targets"])
+        workload = ("batched training step (CPU port, bounded sample): %d frames, %d targets (%d rays)" %
+                    (bcfg["frames"], bcfg["targets"], R))
+    else:
+        cfg = dict(CFG)
+        if args.small:
+            cfg.update(res=512, D=256, trunc=0.03, target=512, S=64, prims=12)
+        sc, ori, dirs, color_grid, color_vs = workload(cfg)
+        fz = cpu_fused_grid(sc, cfg)
+        run = lambda: cpu_baseline(sc, ori, dirs, cfg, color_grid, color_vs, ray_sample=4096, fusion_slab=8,  # noqa
+                                   fz=fz)
+        R = ori.shape[1]
+        workload = "full-resolution plain forward: 4x1024^2 views, 512^3 TSDF, 8^3 bricks, 1024^2 target, S=96"
     vals = []
     cb = None
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(sc, ori, dirs, cfg, color_grid, color_vs, ray_sample=4096, fusion_slab=8, fz=fz)
+        cb = run()
         if i >= args.warmup:
             vals.append(cb["value"])
     v = float(np.median(vals)) if vals else cb["value"]
     out = dict(metric=METRIC, value=v, unit=UNIT, impl="reference", n_gpus=args.gpus, steps=args.steps,
-               warmup=args.warmup, ms_per_step=1000.0 * ori.shape[1] / v, higher_is_better=True,
+               warmup=args.warmup, ms_per_step=1000.0 * R / v, higher_is_better=True,
                scaling="weak", vs_baseline=None, dtype="f32", data="synthetic",
-               config=dict(workload="full-resolution plain forward: 4x1024^2 views, 512^3 TSDF, 8^3 bricks, "
-                                    "1024^2 target, S=96" if not args.small else "small", l2="inputs > L2"),
+               config=dict(workload=workload, l2="inputs > L2"),
                cpu_baseline=dict(value=v, unit=UNIT, cores=cb["cores"], kind="port", sample=cb["sample"]),
                e2e=dict(value=v, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0))
     print(json.dumps(out), flush=True)
@@ -277,7 +317,7 @@ def batch_algorithmic_bytes(bcfg, w, n_hits, R, n_samples):
     )
 
 
-def cpu_baseline_batch(w, bcfg, feat, head, ray_sample=2048, fusion_slab=8):
+def cpu_baseline_batch(w, bcfg, feat, head, ray_sample=2048, fusion_slab=8, fz=None):
     """The oracle (a C port of the reference kernels, OpenMP on all host
     cores) on a bounded sample of the batched step, scaled to the whole step:
     fusion of an x-slab of frame 0, coarse occupancy + tree of frame 0 (x
@@ -291,7 +331,8 @@ def cpu_baseline_batch(w, bcfg, feat, head, ray_sample=2048, fusion_slab=8):
     t0 = time.perf_counter()
     orc.integrate_slab(K, RT, col, dep, D, bb, vs, 0, fusion_slab, trunc_weight=w["trunc_weight"])
     t_fuse = (time.perf_counter() - t0) * (D / fusion_slab) * (n_views_all / len(fr["K"]))
-    fz = orc.integrate(K, RT, col, dep, D, bb, vs, trunc_weight=w["trunc_weight"])
+    if fz is None:
+        fz = orc.integrate(K, RT, col, dep, D, bb, vs, trunc_weight=w["trunc_weight"])
     t0 = time.perf_counter()
     top, _ = orc.merge(fz["occ"], rate)
     tree = orc.build_tree(top, fz["occ"])
@@ -378,9 +419,7 @@ def run_batch(args):
     from sailor_gb300.batch import BatchPipeline
     from sailor_gb300.dist import VoxelEncoding as VE
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    world, rank, local = dist_env()
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl")
@@ -434,12 +473,7 @@ def run_batch(args):
             graph.replay()
         e1.record()
         barrier()
-    ms = e0.elapsed_time(e1) / args.steps
-    t = torch.tensor([ms], device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = world * R / (ms_max / 1000.0)
+    ms_max, value = whole_job(e0.elapsed_time(e1) / args.steps, R, world, dev)
 
     # per-stage times (eager pass with events on the launching stream)
     stage_sum = {}
@@ -507,10 +541,7 @@ def run_batch(args):
         e2e_step()
     f1.record()
     barrier()
-    t = torch.tensor([f0.elapsed_time(f1) / args.steps], device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    e2e_value = world * R / (float(t.item()) / 1000.0)
+    _, e2e_value = whole_job(f0.elapsed_time(f1) / args.steps, R, world, dev)
 
     if rank == 0:
         pk, pk_kind = peaks()
@@ -570,9 +601,7 @@ def run_plain(args):
 
     from sailor_gb300.pipeline import FramePipeline
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    world, rank, local = dist_env()
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl")
@@ -641,12 +670,7 @@ def run_plain(args):
             stage_sum[k] = stage_sum.get(k, 0.0) + v
     pipe.events = None
     stages = {k: v / args.steps for k, v in stage_sum.items()}
-    ms = ms_total / args.steps
-    t = torch.tensor([ms], device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = world * n_rays / (ms_max / 1000.0)
+    ms_max, value = whole_job(ms_total / args.steps, n_rays, world, dev)
 
     # ---- e2e through the public pipeline API from pinned host buffers -------
     host = {k: torch.as_tensor(np.ascontiguousarray(v)).pin_memory() for k, v in
@@ -674,11 +698,7 @@ def run_plain(args):
         e2e_step()
     f1.record()
     barrier()
-    e2e_ms = f0.elapsed_time(f1) / args.steps
-    t = torch.tensor([e2e_ms], device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    e2e_value = world * n_rays / (float(t.item()) / 1000.0)
+    _, e2e_value = whole_job(f0.elapsed_time(f1) / args.steps, n_rays, world, dev)
 
     if rank == 0:
         pk, pk_kind = peaks()
