@@ -305,13 +305,12 @@ def batch_algorithmic_bytes(bcfg, w, n_hits, R, n_samples):
     return dict(
         fusion=16 * V + 8 * n_pix,
         tree=4 * V + 4 * Vt,
-        intersect=24 * R + 12 * n_hits + 8 * R,
-        # hit rows + per-ray count / valid length + ray + 24 B/ray out
-        forward=12 * n_hits + 8 * R + 24 * R + 24 * R,
+        intersect=12 * n_hits + 8 * R,  # rays generated from the target cameras
+        forward=12 * n_hits + 8 * R + 24 * R,  # hit rows, count + valid length in; 24 B/ray out
         # fused training pass: as forward, with the target colour in and the
         # per-ray loss out; the atomic adds into the feature-gradient grid
         # are not counted
-        train=12 * n_hits + 8 * R + 24 * R + 12 * R + 24 * R + 4 * R,
+        train=12 * n_hits + 8 * R + 12 * R + 24 * R + 4 * R,
         # zeroing of the feature-gradient grid
         grad_prep=4 * V * C,
     )
@@ -373,8 +372,9 @@ def cpu_baseline_batch(w, bcfg, feat, head, ray_sample=2048, fusion_slab=8, fz=N
 def plain_per_frame_forward(VE, fields, w, bcfg, dev, feat, head_t, vbb, vvs, W_hits=256):
     """The reference's per-frame call order through the drop-in API, forward
     only: per frame integrate -> build_multi_res_volumes -> octree, then per
-    target of the frame traversal (padded rows) -> coarse sampling -> sort ->
-    TSDF density and feature gathers -> colour head -> compositing."""
+    target of the frame rays_calculating -> traversal (padded rows) -> coarse
+    sampling -> sort -> TSDF density and feature gathers -> colour head ->
+    compositing."""
     import torch
     D, rate = bcfg["D"], bcfg["rate"]
     Dt = D // rate
@@ -397,7 +397,9 @@ def plain_per_frame_forward(VE, fields, w, bcfg, dev, feat, head_t, vbb, vvs, W_
         for t in w["targets"]:
             if t["frame"] != b:
                 continue
-            o, d = t["_dev"]
+            Kt, Rt, Tt = t["_dev"]
+            rays = VE.rays_calculating(Kt, Rt, Tt, t["res"], dev.index or 0).view(1, -1, 6)
+            o, d = rays[..., :3].contiguous(), rays[..., 3:].contiguous()
             S = t["S"]
             n = o.shape[1]
             idx, t0, t1, vl = octree.voxel_traversal(o, d, W_hits, 0, -1, False, -1)
@@ -429,9 +431,9 @@ def run_batch(args):
     view_hw = [[d.shape for d in fr["depth"]] for fr in w["frames"]]
     targets = [(t["frame"], t["ori"].shape[0], t["S"]) for t in w["targets"]]
     bp = BatchPipeline(view_hw, targets, D=bcfg["D"], rate=bcfg["rate"], C=bcfg["C"], W_hits=bcfg["W_hits"],
-                       device=dev)
+                       target_widths=[t["res"] for t in w["targets"]], device=dev)
     bp.load_views(w["frames"], w["vol_bbox"], w["voxel_size"], w["trunc_weight"])
-    bp.load_rays([(t["ori"], t["dir"]) for t in w["targets"]])
+    bp.load_cameras([t["K"] for t in w["targets"]], [t["R"] for t in w["targets"]], [t["T"] for t in w["targets"]])
     head, target = batch_fields(bcfg, bp.R, bp.feat, rank)
     bp.set_fields(head=torch.as_tensor(head).to(dev), target_rgb=torch.as_tensor(target).to(dev))
     trunc_m = float(w["voxel_size"][0]) * w["trunc_weight"]
@@ -492,7 +494,7 @@ def run_batch(args):
     for fr in w["frames"]:
         fr["_dev"] = [torch.as_tensor(a).to(dev) for a in padded_views(fr)]
     for t in w["targets"]:
-        t["_dev"] = (torch.as_tensor(t["ori"])[None].to(dev), torch.as_tensor(t["dir"])[None].to(dev))
+        t["_dev"] = tuple(torch.as_tensor(t[k]).reshape(1, 1, *np.shape(t[k])).to(dev) for k in ("K", "R", "T"))
     feat_t, head_t = bp.feat, bp.head.T.contiguous()
     plain_forward = lambda: plain_per_frame_forward(VE, fields, w, bcfg, dev, feat_t, head_t, vbb, vvs)  # noqa
     for _ in range(2):
@@ -515,11 +517,12 @@ def run_batch(args):
                 color=torch.as_tensor(np.concatenate([c.reshape(-1) for fr in w["frames"] for c in fr["color"]])),
                 K=torch.as_tensor(np.stack([k for fr in w["frames"] for k in fr["K"]])),
                 RT=torch.as_tensor(np.stack([k for fr in w["frames"] for k in fr["RT"]])),
-                ori=torch.as_tensor(np.concatenate([t["ori"] for t in w["targets"]])),
-                dirs=torch.as_tensor(np.concatenate([t["dir"] for t in w["targets"]])),
+                tK=torch.as_tensor(np.stack([t["K"] for t in w["targets"]])),
+                tR=torch.as_tensor(np.stack([t["R"] for t in w["targets"]])),
+                tT=torch.as_tensor(np.stack([t["T"] for t in w["targets"]])),
                 target_rgb=torch.as_tensor(target))
     host = {k: v.contiguous().pin_memory() for k, v in host.items()}
-    dst = dict(depth=bp.depth, color=bp.color, K=bp.K, RT=bp.RT, ori=bp.ori, dirs=bp.dirs,
+    dst = dict(depth=bp.depth, color=bp.color, K=bp.K, RT=bp.RT, tK=bp.tK, tR=bp.tR, tT=bp.tT,
                target_rgb=bp.target_rgb)
     out_host = torch.empty((R, 3), dtype=torch.float32).pin_memory()
     h2d = sum(v.numel() * v.element_size() for v in host.values())

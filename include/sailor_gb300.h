@@ -312,6 +312,24 @@ int sg_render_fused(const SgTree *tree, const int *hit_idx,
                     float *out_ws, float *out_alpha, float *out_z,
                     int *out_node, sg_stream_t stream);
 
+/* ---- rays ----------------------------------------------------------------- */
+
+/* Camera table: per camera i, K^-1 (9), R^-1 (9) and the centre -R^-1 T (3)
+ * into cams [n, 21], with the reference's inverse_mat3x3
+ * (sampling_kernel.cu:18-48) and centre arithmetic (:441-447).
+ * K, R [n, 3, 3], T [n, 3]. */
+int sg_camera_params(const float *K, const float *R, const float *T, int n,
+                     float *cams, sg_stream_t stream);
+
+/* Per-pixel rays of B x N cameras: out [B, N, H, W, 6] = (origin -R^-1 T,
+ * direction R^-1 K^-1 [w, h, 1] normalised).  Replaces rays_calculating
+ * (sampling_kernel.cu:674-731, kernel :411-486; square H = W = load_size
+ * there).  Origins are bit-identical to the reference; directions are
+ * within one ulp (the reference normalises in double precision, this
+ * library in single). */
+int sg_rays_from_cameras(const float *K, const float *R, const float *T, int B,
+                         int N, int H, int W, float *out, sg_stream_t stream);
+
 /* ---- batched launches over segment tables -------------------------------- */
 /* Many frames, views and target cameras of uneven sizes go through one
  * launch per stage.  No reference counterpart: the reference runs one frame
@@ -343,6 +361,14 @@ typedef struct SgRaySegments {
   const int *ray_begin; /* [count+1] */
   const int *frame;     /* [count]   */
   const int *samples;   /* [count]   */
+  /* Optional (both NULL or both set): each segment is a camera image of
+   * widths[s] pixels per row; ray r of segment s is pixel p = r -
+   * ray_begin[s] (row p / width, column p % width) of camera cameras[s]
+   * (sg_camera_params).  sg_intersect_segments then generates each ray
+   * itself instead of reading ori / dir; sg_segment_rays writes the rays
+   * for the render entry points, which always read ori / dir. */
+  const float *cameras; /* [count, 21] */
+  const int *widths;    /* [count]     */
 } SgRaySegments;
 
 /* Inputs of the batched render.  Rays ori/dir [R,3]; hit rows [R,W] with
@@ -382,6 +408,13 @@ int sg_fuse_tsdf_views(const SgViews *views, int B, int D,
                        float th_high, float *tsdf, float *weight,
                        float *colorv, int *occ, int *count,
                        sg_stream_t stream);
+
+/* The rays of camera-defined segments (SgRaySegments.cameras / widths set)
+ * written to ori / dir [total, 3]: one thread per ray, the same rays the
+ * kernels generate from the cameras.  Cheaper than generating them inside
+ * the warp-per-ray render, which repeats the camera arithmetic per warp. */
+int sg_segment_rays(const SgRaySegments *seg, float *ori, float *dir,
+                    sg_stream_t stream);
 
 /* sg_intersect (compact rows, inference mode) over ray segments: ray r of
  * segment s traverses frame frame[s] of the tree. */

@@ -28,6 +28,7 @@ def lib():
         L = C.CDLL(path)
         i, f, l = C.c_int, C.c_float, C.c_long
         L.orc_inverse3x3.argtypes = [_f32p, i, _f32p]
+        L.orc_rays.argtypes = [_f32p, _f32p, _f32p, i, i, i, i, _f32p]
         L.orc_origin_bbox.argtypes = [_f32p, _f32p, _f32p, _f32p, i, i, i, i, f, _f32p]
         L.orc_resized_bbox.argtypes = [_f32p, i, i, _f32p, _f32p]
         L.orc_integrate.argtypes = [i, i, i, i, i, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p,
@@ -84,6 +85,17 @@ def inverse3x3(M):
     M = _f(M)
     out = np.zeros_like(M)
     lib().orc_inverse3x3(M.reshape(-1), M.size // 9, out.reshape(-1))
+    return out
+
+
+def rays(K, R, T, H, W=None):
+    """rays_calculating (sampling_kernel.cu:674-731): K, R [B,N,3,3], T
+    [B,N,3] -> [B,N,H,W,6] (ori, dir) per pixel (h, w)."""
+    W = H if W is None else W
+    K, R, T = _f(K), _f(R), _f(np.reshape(T, np.shape(K)[:2] + (3,)))
+    B, N = K.shape[:2]
+    out = np.zeros((B, N, H, W, 6), np.float32)
+    lib().orc_rays(K.reshape(-1), R.reshape(-1), T.reshape(-1), B, N, H, W, out.reshape(-1))
     return out
 
 

@@ -13,6 +13,7 @@ as device memory:
   ray_voxels_points_sampling_coarse sampling_kernel.cu:1251-1304
   sort_samplings          sampling_kernel.cu:1308-1329 (torch.sort)
   volume_rendering_*      volume_rendering.cu:525-787
+  rays_calculating        sampling_kernel.cu:674-731
 
 It is used only to generate golden vectors (tests/golden/make_golden.py) and
 by optional GPU tests that skip when the cubins are absent.
@@ -48,6 +49,8 @@ _NAMES = {
     "vr_bwd": ("volume_rendering", "volume_rendering_training_backward_kernelIfE"),
     "vr_occ_bwd": ("volume_rendering", "volume_rendering_occ_training_backward_kernelIfE"),
     "vr_occ": ("volume_rendering", "volume_rendering_occ_kernelIfE"),
+    "rays_inverse": ("sampling_kernel", "14inverse_mat3x3IfE"),
+    "rays": ("sampling_kernel", "23rays_calculating_kernelIfE"),
 }
 
 
@@ -307,3 +310,20 @@ def volume_rendering_occ_forward(z, occ_, feats, t_thres):
     d.launch("vr_occ", B * N, [z, occ_, feats, of, od, ws, oa, u32(B), u32(N), u32(S), f32(t_thres)])
     torch.cuda.synchronize()
     return of, od, ws, oa
+
+
+def rays_calculating(K, R, T, load_size):
+    """rays_calculating (sampling_kernel.cu:674-731): inverse_mat3x3 of K and
+    R, then rays_calculating_kernel (:411-486) -> [B, N, H, W, 6] (ori, dir)."""
+    d = driver()
+    B, N = K.shape[0], K.shape[1]
+    Kt, Rt, Tt = _dev(K, torch.float32), _dev(R, torch.float32), _dev(np.reshape(T, (B, N, 3)), torch.float32)
+    kinv = torch.zeros((B, N, 3, 3), device="cuda")
+    rinv = torch.zeros((B, N, 3, 3), device="cuda")
+    out = torch.zeros((B, N, load_size, load_size, 6), device="cuda")
+    d.launch("rays_inverse", B * N, [Kt, u32(B), u32(N), kinv])
+    d.launch("rays_inverse", B * N, [Rt, u32(B), u32(N), rinv])
+    d.launch("rays", B * N * load_size * load_size, [kinv, rinv, Tt, out, u32(B), u32(N), u32(load_size),
+                                                     u32(load_size)])
+    torch.cuda.synchronize()
+    return dict(rays=out, Kinv=kinv, Rinv=rinv)

@@ -98,6 +98,40 @@ void orc_inverse3x3(const float *M, int n, float *inv) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* Ray generation: rays_calculating (sampling_kernel.cu:674-731) and           */
+/* rays_calculating_kernel (:411-486).  K^-1 and R^-1 by inverse_mat3x3        */
+/* (:18-48, the same arithmetic as orc_inverse3x3); per pixel (h, w):          */
+/* ori = -R^-1 T, dir = R^-1 K^-1 [w, h, 1] / (|.| + 1e-10).  nvcc contracts   */
+/* the sums as written below; the normalising division is in double (the       */
+/* literal 1e-10 is a double) and rounded to float, as the reference computes. */
+/* out [B, N, H, W, 6].                                                        */
+/* ------------------------------------------------------------------------ */
+void orc_rays(const float *K, const float *R, const float *T, int B, int N, int H, int W, float *out) {
+  for (int bv = 0; bv < B * N; bv++) {
+    float ki[9], ri[9], c[3];
+    orc_inverse3x3(K + 9 * bv, 1, ki);
+    orc_inverse3x3(R + 9 * bv, 1, ri);
+    const float *t = T + 3 * bv;
+    for (int k = 0; k < 3; k++)
+      c[k] = fmaf(-ri[3 * k + 2], t[2], fmaf(-ri[3 * k + 1], t[1], -(ri[3 * k] * t[0])));
+#pragma omp parallel for schedule(static)
+    for (int h = 0; h < H; h++)
+      for (int w = 0; w < W; w++) {
+        float cd[3], wd[3];
+        for (int k = 0; k < 3; k++) cd[k] = fmaf((float)w, ki[3 * k], (float)h * ki[3 * k + 1]) + ki[3 * k + 2];
+        for (int k = 0; k < 3; k++)
+          wd[k] = fmaf(cd[2], ri[3 * k + 2], fmaf(cd[0], ri[3 * k], cd[1] * ri[3 * k + 1]));
+        const float nd = sqrtf(fmaf(wd[2], wd[2], fmaf(wd[0], wd[0], wd[1] * wd[1])));
+        float *o = out + (((size_t)bv * H + h) * W + w) * 6;
+        for (int k = 0; k < 3; k++) {
+          o[k] = c[k];
+          o[3 + k] = (float)((double)wd[k] / ((double)nd + 1e-10));
+        }
+      }
+  }
+}
+
+/* ------------------------------------------------------------------------ */
 /* Data-driven bounding box: obtain_origin_bbox fusion_kernel.cu:137-184.     */
 /* vol_origin [B,3,2] must hold 99999 / -99999 on entry (reference host code  */
 /* fusion_kernel.cu:655-662).                                                */

@@ -23,6 +23,7 @@ EXPORTS = (
     "sg_render_fused", "sg_tune_set", "sg_tune_get", "sg_tree_build_static",
     "sg_grid_scatter", "sg_fuse_tsdf_views", "sg_intersect_segments", "sg_render_segments_fwd",
     "sg_render_segments_bwd", "sg_render_segments_train",
+    "sg_camera_params", "sg_rays_from_cameras", "sg_segment_rays",
 )
 
 
@@ -42,7 +43,7 @@ class SgViews(C.Structure):
 
 class SgRaySegments(C.Structure):
     _fields_ = [("count", C.c_int), ("total", C.c_int), ("ray_begin", C.c_void_p), ("frame", C.c_void_p),
-                ("samples", C.c_void_p)]
+                ("samples", C.c_void_p), ("cameras", C.c_void_p), ("widths", C.c_void_p)]
 
 
 class SgRenderArgs(C.Structure):
@@ -91,6 +92,9 @@ def _load():
     lib.sg_render_segments_fwd.argtypes = [T, G, A, p, p, p, p, p, p, p]
     lib.sg_render_segments_bwd.argtypes = [T, G, A, p, p, p, p, p, p, p, p, p]
     lib.sg_render_segments_train.argtypes = [T, G, A, p, f, p, p, p, p, p, p, p, p]
+    lib.sg_camera_params.argtypes = [p, p, p, i, p, p]
+    lib.sg_rays_from_cameras.argtypes = [p, p, p, i, i, i, i, p, p]
+    lib.sg_segment_rays.argtypes = [C.POINTER(SgRaySegments), p, p, p]
     lib.sg_tune_set.argtypes = [i, i]
     lib.sg_tune_get.argtypes = [i]
     lib.sg_trilerp_nodes_fwd.argtypes = [C.POINTER(SgTree), p, p, p, p, p, i, i, i, p, p]

@@ -11,7 +11,9 @@ over all frames / all rays, indexed by segment tables:
 * coarse occupancy and tree: ``sg_brick_occupancy`` / ``sg_tree_build`` over
   the frame axis;
 * intersection: ``sg_intersect_segments`` (each ray's frame from its target's
-  segment);
+  segment); with ``target_widths`` the targets are cameras (``load_cameras``)
+  whose rays are generated on the device each step (``sg_camera_params``,
+  ``sg_segment_rays``), so no ray crosses from the host;
 * render: ``sg_render_segments_fwd`` (per-ray outputs only) and
   ``sg_render_segments_bwd`` (recomputes each ray, exact compositing adjoint,
   gradients scattered into the per-frame feature and TSDF grids).
@@ -35,10 +37,14 @@ from . import _native as N
 
 
 class BatchPipeline:
-    def __init__(self, view_hw, targets, D=256, rate=8, C=16, W_hits=64, train_tsdf=False, device="cuda"):
+    def __init__(self, view_hw, targets, D=256, rate=8, C=16, W_hits=64, train_tsdf=False, target_widths=None,
+                 device="cuda"):
         """view_hw: per frame, a list of (H, W) per view.  targets: list of
         (frame, n_rays, S).  train_tsdf: train_step also scatters the gradient
-        of the TSDF grid (the feature grid is always trained)."""
+        of the TSDF grid (the feature grid is always trained).  target_widths:
+        per target the image width in pixels -- the targets are then cameras
+        (n_rays = width x height, ray = pixel in row-major order) given by
+        load_cameras instead of ray buffers given by load_rays."""
         self.B = B = len(view_hw)
         self.D, self.rate, self.C, self.W = D, rate, C, W_hits
         self.train_tsdf = bool(train_tsdf)
@@ -104,9 +110,25 @@ class BatchPipeline:
         self.seg_begin = torch.tensor(rb.astype(np.int32), **i32)
         self.seg_frame = torch.tensor([f for f, _, _ in self.targets], **i32)
         self.seg_samples = torch.tensor([s for _, _, s in self.targets], **i32)
-        self.seg = N.SgRaySegments(T, R, N.ptr(self.seg_begin), N.ptr(self.seg_frame), N.ptr(self.seg_samples))
+        self.cameras = target_widths is not None
+        if self.cameras:
+            if len(target_widths) != T or any(n % int(w) for (_, n, _), w in zip(self.targets, target_widths)):
+                raise ValueError("one width per target, dividing its ray count")
+            self.tK = torch.zeros((T, 3, 3), **f32)
+            self.tR = torch.zeros((T, 3, 3), **f32)
+            self.tT = torch.zeros((T, 3), **f32)
+            self.cams = torch.zeros((T, 21), **f32)
+            self.cam_w = torch.tensor([int(w) for w in target_widths], **i32)
+            self.cam_seg = N.SgRaySegments(T, R, N.ptr(self.seg_begin), N.ptr(self.seg_frame),
+                                           N.ptr(self.seg_samples), N.ptr(self.cams), N.ptr(self.cam_w))
+        else:
+            self.cams = self.cam_w = self.cam_seg = None
+        # ray buffers: loaded (load_rays), or written from the cameras once per
+        # step (sg_segment_rays) -- cheaper than generating each ray inside the
+        # warp-per-ray render kernels
         self.ori = torch.zeros((R, 3), **f32)
         self.dirs = torch.zeros((R, 3), **f32)
+        self.seg = N.SgRaySegments(T, R, N.ptr(self.seg_begin), N.ptr(self.seg_frame), N.ptr(self.seg_samples))
         self.hit_idx = torch.empty((R, W_hits), **i32)
         self.hit_t0 = torch.empty((R, W_hits), **f32)
         self.hit_t1 = torch.empty((R, W_hits), **f32)
@@ -151,9 +173,20 @@ class BatchPipeline:
 
     def load_rays(self, rays):
         """rays: per target (ori [n,3], dir [n,3])."""
+        if self.cameras:
+            raise RuntimeError("this pipeline takes target cameras (load_cameras)")
         for (a, b), (o, d) in zip(self.ray_slices, rays):
             self.ori[a:b].copy_(torch.as_tensor(o))
             self.dirs[a:b].copy_(torch.as_tensor(d))
+
+    def load_cameras(self, K, R, T):
+        """Target cameras (K [T,3,3], R [T,3,3], T [T,3]); rays follow
+        rays_calculating (origin -R^-1 T, direction R^-1 K^-1 [w, h, 1])."""
+        if not self.cameras:
+            raise RuntimeError("this pipeline takes ray buffers (load_rays)")
+        self.tK.copy_(torch.as_tensor(np.asarray(K, np.float32)).reshape(self.tK.shape))
+        self.tR.copy_(torch.as_tensor(np.asarray(R, np.float32)).reshape(self.tR.shape))
+        self.tT.copy_(torch.as_tensor(np.asarray(T, np.float32)).reshape(self.tT.shape))
 
     def set_fields(self, feat=None, head=None, target_rgb=None):
         if feat is not None:
@@ -199,6 +232,11 @@ class BatchPipeline:
         self._mark("tree")
 
     def intersect(self):
+        if self.cameras:
+            N.check(N.lib.sg_camera_params(N.ptr(self.tK), N.ptr(self.tR), N.ptr(self.tT), len(self.targets),
+                                           N.ptr(self.cams), N.stream()), "camera_params")
+            N.check(N.lib.sg_segment_rays(C.byref(self.cam_seg), N.ptr(self.ori), N.ptr(self.dirs), N.stream()),
+                    "segment_rays")
         N.check(N.lib.sg_intersect_segments(C.byref(self.tree), C.byref(self.seg), N.ptr(self.ori),
                                             N.ptr(self.dirs), self.W, N.ptr(self.hit_idx), N.ptr(self.hit_t0),
                                             N.ptr(self.hit_t1), N.ptr(self.valid_len), N.ptr(self.hit_count),

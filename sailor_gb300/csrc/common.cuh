@@ -187,6 +187,62 @@ __device__ __forceinline__ void status_or(SgStatus *st, int f) {
 // launch-shape knobs (sg_tune_set / sg_tune_get, capi.cu)
 int tune(int knob);
 
+// ---------------------------------------------------------------------------
+// ray generation (rays_calculating_kernel, sampling_kernel.cu:411-486)
+// ---------------------------------------------------------------------------
+constexpr int kCamFloats = 21;  // K^-1 (9), R^-1 (9), centre (3)
+
+// Camera table entry from K, R, T: the reference's inverses and centre.
+__device__ __forceinline__ void camera_params(const float *K, const float *R, const float *T, float *cam) {
+  inverse3x3(K, cam);
+  inverse3x3(R, cam + 9);
+  const float *ri = cam + 9;
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    cam[18 + k] = __fmaf_rn(-ri[3 * k + 2], T[2], __fmaf_rn(-ri[3 * k + 1], T[1], -(ri[3 * k] * T[0])));
+}
+
+// Ray of pixel (h, w): direction R^-1 K^-1 [w, h, 1] / (|.| + 1e-10), with the
+// multiply-adds of the reference kernel; the reference divides in double,
+// the single-precision quotient here is within one ulp of it.  cam: a
+// camera table entry in shared memory or (GLOBAL) read-only global memory.
+template <bool GLOBAL>
+__device__ __forceinline__ void pixel_ray(const float *cam, int h, int w, float o[3], float d[3]) {
+  auto c = [&](int k) { return GLOBAL ? __ldg(cam + k) : cam[k]; };
+  float cd[3], wd[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) cd[k] = __fmaf_rn((float)w, c(3 * k), (float)h * c(3 * k + 1)) + c(3 * k + 2);
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    wd[k] = __fmaf_rn(cd[2], c(9 + 3 * k + 2), __fmaf_rn(cd[0], c(9 + 3 * k), cd[1] * c(9 + 3 * k + 1)));
+  const float nd = sqrtf(__fmaf_rn(wd[2], wd[2], __fmaf_rn(wd[0], wd[0], wd[1] * wd[1]))) + 1e-10f;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    o[k] = c(18 + k);
+    d[k] = wd[k] / nd;
+  }
+}
+
+// Origin and direction of ray r of segment s: generated from the segment's
+// camera (cams != NULL) or read from ori / dir.
+__device__ __forceinline__ void segment_ray(const float *__restrict__ ori, const float *__restrict__ dir,
+                                            const float *__restrict__ cams, const int *__restrict__ widths,
+                                            const int *__restrict__ seg_begin, int s, long r, float o[3],
+                                            float d[3]) {
+  if (cams) {
+    const int p = (int)(r - __ldg(seg_begin + s));
+    const int W = __ldg(widths + s);
+    const int h = p / W;
+    pixel_ray<true>(cams + (size_t)s * kCamFloats, h, p - h * W, o, d);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      o[k] = __ldg(ori + r * 3 + k);
+      d[k] = __ldg(dir + r * 3 + k);
+    }
+  }
+}
+
 }  // namespace sg
 
 // launch-error check used by every entry point

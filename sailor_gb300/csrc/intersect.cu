@@ -32,6 +32,8 @@ struct IsectParams {
   long R;                               // rays of the launch
   int nseg;                             // 0: frames of N rays; else ray segments
   const int *seg_begin, *seg_frame;
+  const float *cams;                    // segments given as cameras (rays generated here)
+  const int *cam_w;
 };
 
 __global__ void __launch_bounds__(512) intersect_kernel(IsectParams p) {
@@ -41,15 +43,16 @@ __global__ void __launch_bounds__(512) intersect_kernel(IsectParams p) {
   int cnt = 0;
   bool over = false;
   if (r < R) {
-    const int b = p.nseg > 0 ? __ldg(p.seg_frame + segment_of(p.seg_begin, p.nseg, r)) : (int)(r / p.N);
+    const int sgm = p.nseg > 0 ? segment_of(p.seg_begin, p.nseg, r) : 0;
+    const int b = p.nseg > 0 ? __ldg(p.seg_frame + sgm) : (int)(r / p.N);
     const float *bb = t.vol_bbox + 6 * b;
     const float bmin[3] = {bb[0], bb[2], bb[4]};
     const float xc = (bb[0] + bb[1]) / 2.0f, yc = (bb[2] + bb[3]) / 2.0f, zc = (bb[4] + bb[5]) / 2.0f;
     const float vs = t.voxel_size[b];
     const float vs_top = vs * (float)(t.Db / t.Dt);
     const float bst[3] = {bb[0] - vs / 2.0f, bb[2] - vs / 2.0f, bb[4] - vs / 2.0f};
-    const float o[3] = {p.ori[r * 3 + 0], p.ori[r * 3 + 1], p.ori[r * 3 + 2]};
-    const float d[3] = {p.dir[r * 3 + 0], p.dir[r * 3 + 1], p.dir[r * 3 + 2]};
+    float o[3], d[3];
+    segment_ray(p.ori, p.dir, p.cams, p.cam_w, p.seg_begin, sgm, r, o, d);
     const float inv[3] = {__fdividef(1.0f, d[0]), __fdividef(1.0f, d[1]), __fdividef(1.0f, d[2])};
     const LevelGeom gt = level_geom(vs, t.Db / t.Dt);
     const LevelGeom gb = level_geom(vs, 1);
@@ -256,7 +259,7 @@ extern "C" int sg_intersect(const SgTree *tree, const float *ori, const float *d
     return SG_ERR_INVALID_ARG;
   long R = (long)tree->B * N;
   IsectParams p{*tree, ori, dir, N, W, th_early_stop, opt_num, is_training,
-                hit_idx, hit_t0, hit_t1, valid_len, hit_count, status, R, 0, nullptr, nullptr};
+                hit_idx, hit_t0, hit_t1, valid_len, hit_count, status, R, 0, nullptr, nullptr, nullptr, nullptr};
   const int blk = tune(SG_TUNE_ISECT_BLOCK);
   intersect_kernel<<<ceil_div(R, blk), blk, 0, stream>>>(p);
   if (padded) {
@@ -271,13 +274,14 @@ extern "C" int sg_intersect(const SgTree *tree, const float *ori, const float *d
 extern "C" int sg_intersect_segments(const SgTree *tree, const SgRaySegments *seg, const float *ori,
                                      const float *dir, int W, int *hit_idx, float *hit_t0, float *hit_t1,
                                      float *valid_len, int *hit_count, SgStatus *status, sg_stream_t stream) {
-  if (!tree || !seg || !ori || !dir || !hit_idx || !hit_t0 || !hit_t1 || !valid_len || !hit_count)
-    return SG_ERR_INVALID_ARG;
+  if (!tree || !seg || !hit_idx || !hit_t0 || !hit_t1 || !valid_len || !hit_count) return SG_ERR_INVALID_ARG;
+  if ((seg->cameras == nullptr) != (seg->widths == nullptr)) return SG_ERR_INVALID_ARG;
+  if (!seg->cameras && (!ori || !dir)) return SG_ERR_INVALID_ARG;
   if (seg->count <= 0 || seg->total < 0 || !seg->ray_begin || !seg->frame) return SG_ERR_INVALID_ARG;
   if (W <= 0 || tree->B <= 0 || tree->Dt <= 0 || tree->Db != tree->Dt * tree->rate) return SG_ERR_INVALID_ARG;
   if (seg->total == 0) return SG_OK;
   IsectParams p{*tree, ori, dir, 1, W, -1, -1, 0, hit_idx, hit_t0, hit_t1, valid_len, hit_count, status,
-                (long)seg->total, seg->count, seg->ray_begin, seg->frame};
+                (long)seg->total, seg->count, seg->ray_begin, seg->frame, seg->cameras, seg->widths};
   const int blk = tune(SG_TUNE_ISECT_BLOCK);
   intersect_kernel<<<ceil_div((long)seg->total, blk), blk, 0, stream>>>(p);
   SG_LAUNCH_CHECK();

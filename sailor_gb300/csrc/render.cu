@@ -60,12 +60,13 @@ struct RenderParams {
   float *out_loss;
 };
 
-__device__ __forceinline__ void ray_frame(const RenderParams &p, long r, int &b, int &S) {
+__device__ __forceinline__ void ray_frame(const RenderParams &p, long r, int &b, int &S, int &s) {
   if (p.nseg > 0) {
-    const int s = segment_of(p.seg_begin, p.nseg, r);
+    s = segment_of(p.seg_begin, p.nseg, r);
     b = __ldg(p.seg_frame + s);
     S = min(__ldg(p.seg_samples + s), p.sp.S);
   } else {
+    s = 0;
     b = (int)(r / p.sp.N);
     S = p.sp.S;
   }
@@ -89,8 +90,8 @@ struct RenderSmem {
 // Samples, sort, field taps, alpha and transmittance of ray r (frame b, S
 // samples) into ev; sorted depths stay in sm.z, sorted positions in sm.p.
 template <int E, int C>
-__device__ __forceinline__ void eval_ray(const RenderParams &p, long r, int b, int S, const RenderSmem<E> &sm,
-                                         RayEval<E> &ev) {
+__device__ __forceinline__ void eval_ray(const RenderParams &p, long r, int b, int S, int sgm,
+                                         const RenderSmem<E> &sm, RayEval<E> &ev) {
   const int lane = lane_id();
   const int nh = p.hit_count ? min(__ldg(p.hit_count + r), p.sp.W) : p.sp.W;
   ev.done = warp_sample_ray(p.sp, r, b, S, nh, p.rand_const, sm.z, sm.i, *sm.sc);
@@ -161,10 +162,10 @@ __global__ void __launch_bounds__(256) render_fwd_kernel(RenderParams p) {
   const int Smax = p.sp.S;
   for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < p.R;
        r += ((long)gridDim.x * blockDim.x) >> 5) {
-    int b, S;
-    ray_frame(p, r, b, S);
+    int b, S, sgm;
+    ray_frame(p, r, b, S, sgm);
     RayEval<E> ev;
-    eval_ray<E, C>(p, r, b, S, sm, ev);
+    eval_ray<E, C>(p, r, b, S, sgm, sm, ev);
     float acc_r = 0.0f, acc_g = 0.0f, acc_b = 0.0f, d = 0.0f, ws = 0.0f, aa = 0.0f;
     if (p.out_z) {
       for (int i = lane; i < Smax; i += 32) {
@@ -273,10 +274,10 @@ __global__ void __launch_bounds__(256) render_bwd_kernel(RenderParams p) {
   const int Smax = p.sp.S;
   for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < p.R;
        r += ((long)gridDim.x * blockDim.x) >> 5) {
-    int b, S;
-    ray_frame(p, r, b, S);
+    int b, S, sgm;
+    ray_frame(p, r, b, S, sgm);
     RayEval<E> ev;
-    eval_ray<E, C>(p, r, b, S, sm, ev);
+    eval_ray<E, C>(p, r, b, S, sgm, sm, ev);
     if (ev.done == 0) {
       if (p.grad_sigma) {
         for (int i = lane; i < Smax; i += 32) {
@@ -522,9 +523,11 @@ static int segment_params(const SgTree *tree, const SgRaySegments *seg, const Sg
   if (!tree || !seg || !a) return SG_ERR_INVALID_ARG;
   if (seg->count <= 0 || seg->total < 0 || !seg->ray_begin || !seg->frame || !seg->samples)
     return SG_ERR_INVALID_ARG;
-  if (!a->ori || !a->dir || !a->hit_idx || !a->hit_t0 || !a->hit_t1 || !a->valid_len || !a->tsdf || !a->feat ||
-      !a->feat_bbox || !a->feat_vs)
+  if (!a->hit_idx || !a->hit_t0 || !a->hit_t1 || !a->valid_len || !a->tsdf || !a->feat || !a->feat_bbox ||
+      !a->feat_vs)
     return SG_ERR_INVALID_ARG;
+  // the render reads ray buffers (for camera segments: sg_segment_rays)
+  if (!a->ori || !a->dir) return SG_ERR_INVALID_ARG;
   if (a->W <= 0 || a->S <= 0 || a->D <= 0 || a->Df <= 0 || tree->B <= 0 || a->sdf_s == 0.0f)
     return SG_ERR_INVALID_ARG;
   if (!a->head && a->C != 3) return SG_ERR_INVALID_ARG;

@@ -270,7 +270,8 @@ def make_batch_workload(seed=0, n_frames=8, views=(4, 8), view_res=(512, 768, 10
         a = rng.uniform(0, 2 * math.pi)
         R, T = look_at((2.5 * math.cos(a), 2.5 * math.sin(a), rng.uniform(0.6, 1.6)))
         o, d = camera_rays(intrinsics(res), R, T, res)
-        targets.append(dict(frame=t % n_frames, res=res, S=int(target_S[t % len(target_S)]), ori=o, dir=d))
+        targets.append(dict(frame=t % n_frames, res=res, S=int(target_S[t % len(target_S)]), ori=o, dir=d,
+                            K=intrinsics(res).astype(np.float32), R=R.astype(np.float32), T=T.astype(np.float32)))
     vs = np.float32(2.0) / np.float32(D - 1)
     return dict(frames=frames, D=D,
                 vol_bbox=np.tile(np.array([[-1.0, 1.0]] * 3, np.float32), (n_frames, 1, 1)),

@@ -20,7 +20,7 @@ import torch
 
 from . import _native as N
 
-__all__ = ["integrate", "integrate_in_box", "build_multi_res_volumes", "volume_rendering_training_forward",
+__all__ = ["rays_calculating", "integrate", "integrate_in_box", "build_multi_res_volumes", "volume_rendering_training_forward",
            "volume_rendering_training_backward", "volume_rendering_occ_forward", "MultiLayerOctree"]
 
 
@@ -68,6 +68,22 @@ class _Dev:
 # --------------------------------------------------------------------------
 # fusion: fusion_cuda_integrate (fusion_kernel.cu:600-727)
 # --------------------------------------------------------------------------
+def rays_calculating(cam_intr, cam_R, cam_T, load_size, device):
+    """Per-pixel rays [B, N, load_size, load_size, 6] (origin, unit
+    direction) of cameras K [B,N,3,3], R [B,N,3,3], T [B,N,3]
+    (sampling_kernel.cu:674-731)."""
+    with _Dev(device, cam_intr, cam_R, cam_T):
+        K = _in(cam_intr, "cam_intr")
+        R = _in(cam_R, "cam_R")
+        T = _in(cam_T, "cam_T")
+        B, Nv = K.shape[0], K.shape[1]
+        H = int(load_size)
+        out = torch.empty((B, Nv, H, H, 6), dtype=torch.float32, device=K.device)
+        N.check(N.lib.sg_rays_from_cameras(N.ptr(K), N.ptr(R), N.ptr(T), B, Nv, H, H, N.ptr(out), N.stream()),
+                "rays_calculating")
+        return out
+
+
 def integrate(occupied_vol, num_occ_voxel, cam_intr, cam_pose, cam_R, cam_T, color_ims, depth_ims, mask_ims,
               obs_weight, th_bbox, trunc_weight, tsdf_th_low, tsdf_th_high, device):
     """TSDF fusion over the data-driven cubic box of the depth points.

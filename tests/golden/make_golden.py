@@ -6,8 +6,8 @@ they lie; this script only loads the cubins):
 
     python tests/golden/make_golden.py --out <dir>
 
-It writes ``ref_chain_explicit.npz``, ``ref_chain_auto.npz`` and
-``ref_composite.npz``.  Each holds the seeded inputs
+It writes ``ref_chain_explicit.npz``, ``ref_chain_auto.npz``,
+``ref_composite.npz`` and ``ref_rays.npz`` (``--only rays``: that one alone).  Each holds the seeded inputs
 and the reference outputs of fusion, coarse occupancy, the two-level tree
 (as canonical node keys, since the reference's node ids depend on atomic
 ordering), the voxel traversal, the coarse sampling, the sort, compositing
@@ -105,12 +105,44 @@ def chain(scene, ori, dirs, rands_list, explicit, trunc_weight, th_bbox=0.025):
     return res, tree
 
 
+def rays(out_dir):
+    """Ray generation: two frames of two cameras each (ring cameras with the
+    synthetic pinhole, and cameras with an off-centre principal point, unequal
+    focal lengths and skew), 48 x 48 pixels."""
+    rng = np.random.default_rng(21)
+    Ks, Rs, Ts = [], [], []
+    for b in range(2):
+        for v in range(2):
+            if v == 0:
+                K = syn.intrinsics(48)
+                R, T = syn.ring_cameras(1, phase=rng.uniform(0, 2 * math.pi))[0]
+            else:
+                K = np.array([[rng.uniform(40, 70), rng.uniform(-2, 2), rng.uniform(18, 30)],
+                              [0.0, rng.uniform(40, 70), rng.uniform(18, 30)], [0.0, 0.0, 1.0]])
+                R, T = syn.look_at(rng.uniform(-3, 3, 3) + np.array([0.0, 0.0, 3.5]), rng.uniform(-0.3, 0.3, 3))
+            Ks.append(K)
+            Rs.append(R)
+            Ts.append(T)
+    K = np.array(Ks, np.float32).reshape(2, 2, 3, 3)
+    R = np.array(Rs, np.float32).reshape(2, 2, 3, 3)
+    T = np.array(Ts, np.float32).reshape(2, 2, 3)
+    res = rc.rays_calculating(K, R, T, 48)
+    np.savez_compressed(os.path.join(out_dir, "ref_rays.npz"), K=K, R=R, T=T, load_size=np.array(48),
+                        rays=res["rays"].cpu().numpy(), Kinv=res["Kinv"].cpu().numpy(),
+                        Rinv=res["Rinv"].cpu().numpy())
+    print("rays done", flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
+    ap.add_argument("--only", choices=["rays"])
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
     assert rc.available(), "reference cubins or GPU missing"
+    rays(args.out)
+    if args.only == "rays":
+        return
     scene = syn.make_scene(seed=11, n_views=VIEWS, res=RES, n_prims=PRIMS, D=D, trunc=0.03)
     ori, dirs = syn.target_rays(seed=11, res=TRES)
     rng = np.random.default_rng(5)
