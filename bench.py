@@ -305,14 +305,16 @@ def batch_algorithmic_bytes(bcfg, w, n_hits, R, n_samples):
     return dict(
         fusion=16 * V + 8 * n_pix,
         tree=4 * V + 4 * Vt,
-        intersect=12 * n_hits + 8 * R,  # rays generated from the target cameras
-        forward=12 * n_hits + 8 * R + 24 * R,  # hit rows, count + valid length in; 24 B/ray out
+        # camera table, ray generation (24 B/ray written), intersection (rays
+        # read back, hit rows + count + valid length written)
+        intersect=24 * R + 24 * R + 12 * n_hits + 8 * R,
+        forward=24 * R + 12 * n_hits + 8 * R + 24 * R,  # rays, hit rows, count + valid length in; 24 B/ray out
         # fused training pass: as forward, with the target colour in and the
         # per-ray loss out; the atomic adds into the feature-gradient grid
         # are not counted
-        train=12 * n_hits + 8 * R + 12 * R + 24 * R + 4 * R,
-        # zeroing of the feature-gradient grid
-        grad_prep=4 * V * C,
+        train=24 * R + 12 * n_hits + 8 * R + 12 * R + 24 * R + 4 * R,
+        # zeroing of the feature-gradient grid (side stream, overlapped)
+        zero_grad=4 * V * C,
     )
 
 
@@ -554,7 +556,7 @@ def run_batch(args):
         dom = max(rl, key=lambda k: stages[k])
         traffic = None
         tpath = os.path.join(ROOT, "profiles", "traffic.json")
-        if os.path.exists(tpath):
+        if os.path.exists(tpath) and not args.small:  # figures scaled to the full batch
             traffic = json.load(open(tpath)).get("batch_" + dom)
         render_ms = sum(stages.get(k, 0.0) for k in ("intersect", "grad_prep", "train"))
         out = dict(
@@ -578,7 +580,9 @@ def run_batch(args):
                           algorithmic_bytes=ab[dom]),
             rooflines={k: dict(achieved=v, frac=v / pk["hbm_gbs"], algorithmic_bytes=ab[k]) for k, v in rl.items()},
             e2e=dict(value=e2e_value, unit=UNIT, h2d_bytes_per_step=h2d, d2h_bytes_per_step=d2h),
-            gpu_launches=10 * args.steps,
+            # per step: fusion 1, coarse occupancy 1, tree 5, camera table 1,
+            # ray generation 1, intersection 1, training pass 1
+            gpu_launches=11 * args.steps,
             clocks=clk.summary(),
         )
         if not args.no_cpu_baseline:

@@ -149,6 +149,7 @@ class BatchPipeline:
         self.args = None
         self.trunc_weight = None
         self.events = None
+        self.side_events = None
         self.side = torch.cuda.Stream(device=dev)  # zeroing of the gradient grids beside the build
 
     # ------------------------------------------------------------------ inputs
@@ -213,6 +214,13 @@ class BatchPipeline:
             ev.record()
             self.events.append((name, ev))
 
+    def _side_event(self):
+        if self.events is None:
+            return None
+        ev = torch.cuda.Event(enable_timing=True)
+        ev.record()
+        return ev
+
     # ------------------------------------------------------------------ stages
     def build(self, obs_weight=1.0, th_low=13.5, th_high=13.5):
         st = N.stream()
@@ -274,9 +282,12 @@ class BatchPipeline:
         main = torch.cuda.current_stream()
         self.side.wait_stream(main)  # the previous step's users of the grids come first
         with torch.cuda.stream(self.side):
+            z0 = self._side_event()
             self.grad_feat.zero_()
             if self.train_tsdf:
                 self.grad_tsdf.zero_()
+            if z0 is not None:
+                self.side_events = (z0, self._side_event())
         self.build()
         self.intersect()
         main.wait_stream(self.side)
@@ -320,6 +331,11 @@ class BatchPipeline:
             if prev is not None:
                 out[name] = out.get(name, 0.0) + prev.elapsed_time(ev)
             prev = ev
+        if self.events and self.side_events is not None:
+            # zeroing of the gradient grids, timed on the side stream where it
+            # overlaps fusion, tree build and intersection
+            out["zero_grad"] = self.side_events[0].elapsed_time(self.side_events[1])
+        self.side_events = None
         return out
 
     def frame_rays(self, t):
