@@ -141,9 +141,10 @@ __device__ __forceinline__ float from_ordered(uint32_t k) {
   return __uint_as_float((k >> 31) ? (k ^ 0x80000000u) : ~k);
 }
 
-// E keys per lane, element i = e*32 + lane, P = 32*E (power of two)
-template <int E>
-__device__ __forceinline__ void bitonic_warp(unsigned long long (&key)[E]) {
+// E keys per lane, element i = e*32 + lane, P = 32*E (power of two); K is
+// a 64-bit (depth, position) key or a 32-bit depth key
+template <int E, typename K>
+__device__ __forceinline__ void bitonic_warp(K (&key)[E]) {
   const int lane = lane_id();
   constexpr int P = 32 * E;
 #pragma unroll
@@ -157,7 +158,7 @@ __device__ __forceinline__ void bitonic_warp(unsigned long long (&key)[E]) {
           if ((e & m) == 0) {
             const int i = e * 32 + lane;
             const bool asc = (i & k) == 0;
-            unsigned long long a = key[e], c = key[e ^ m];
+            K a = key[e], c = key[e ^ m];
             bool sw = asc ? (a > c) : (a < c);
             key[e] = sw ? c : a;
             key[e ^ m] = sw ? a : c;
@@ -168,10 +169,10 @@ __device__ __forceinline__ void bitonic_warp(unsigned long long (&key)[E]) {
         for (int e = 0; e < E; e++) {
           const int i = e * 32 + lane;
           const bool asc = (i & k) == 0;
-          unsigned long long other = __shfl_xor_sync(SG_FULL, key[e], j);
+          K other = __shfl_xor_sync(SG_FULL, key[e], j);
           const bool lower = (lane & j) == 0;
-          unsigned long long mn = key[e] < other ? key[e] : other;
-          unsigned long long mx = key[e] < other ? other : key[e];
+          K mn = key[e] < other ? key[e] : other;
+          K mx = key[e] < other ? other : key[e];
           key[e] = (lower == asc) ? mn : mx;
         }
       }
@@ -181,38 +182,64 @@ __device__ __forceinline__ void bitonic_warp(unsigned long long (&key)[E]) {
 
 // Sort the samples of a ray in shared memory.  sz[0, done) hold the
 // samples, sz[done, S) the -1 padding (warp_sample_ray's layout).  On
-// return sz[i] / spos[i] hold the depth and original position of sorted
-// position i: the padding first (stable: positions done, done+1, ...), then
-// the samples ascending by (depth, position).  Only the samples are sorted,
-// with the smallest register bitonic network that holds them.
+// return sz[i] holds the depth of sorted position i: the padding first, then
+// the samples ascending by (depth, position); with POS, spos[i] holds the
+// original position (padding stable: done, done+1, ...).  Only the samples
+// are sorted, with the smallest register bitonic network that holds them;
+// done <= 32 * EMAX.  Without POS the keys are the depths alone: samples of
+// equal depth have equal bits, so the sorted depths are the same.
+template <int EMAX, bool POS>
 __device__ __forceinline__ void warp_sort_samples(float *sz, int *spos, int S, int done) {
   const int lane = lane_id();
   const int npad = S - done;
-  for (int q = lane; q < npad; q += 32) spos[q] = done + q;
+  if (POS)
+    for (int q = lane; q < npad; q += 32) spos[q] = done + q;
   if (done > 0) {
     auto run = [&](auto tag) {
       constexpr int E = decltype(tag)::value;
-      unsigned long long key[E];
+      if constexpr (POS) {
+        unsigned long long key[E];
 #pragma unroll
-      for (int e = 0; e < E; e++) {
-        const int i = e * 32 + lane;
-        key[e] = (i < done) ? (((unsigned long long)ordered_bits(sz[i]) << 32) | (unsigned)i) : ~0ull;
-      }
-      __syncwarp();
-      bitonic_warp<E>(key);
+        for (int e = 0; e < E; e++) {
+          const int i = e * 32 + lane;
+          key[e] = (i < done) ? (((unsigned long long)ordered_bits(sz[i]) << 32) | (unsigned)i) : ~0ull;
+        }
+        __syncwarp();
+        bitonic_warp<E>(key);
 #pragma unroll
-      for (int e = 0; e < E; e++) {
-        const int j = e * 32 + lane;
-        if (j < done) {
-          sz[npad + j] = from_ordered((uint32_t)(key[e] >> 32));
-          spos[npad + j] = (int)(key[e] & 0xffffffffu);
+        for (int e = 0; e < E; e++) {
+          const int j = e * 32 + lane;
+          if (j < done) {
+            sz[npad + j] = from_ordered((uint32_t)(key[e] >> 32));
+            spos[npad + j] = (int)(key[e] & 0xffffffffu);
+          }
+        }
+      } else {
+        uint32_t key[E];
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+          const int i = e * 32 + lane;
+          key[e] = (i < done) ? ordered_bits(sz[i]) : ~0u;
+        }
+        __syncwarp();
+        bitonic_warp<E>(key);
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+          const int j = e * 32 + lane;
+          if (j < done) sz[npad + j] = from_ordered(key[e]);
         }
       }
     };
-    if (done <= 32) run(std::integral_constant<int, 1>());
-    else if (done <= 64) run(std::integral_constant<int, 2>());
-    else if (done <= 128) run(std::integral_constant<int, 4>());
-    else run(std::integral_constant<int, 8>());
+    if (done <= 32) {
+      run(std::integral_constant<int, 1>());
+    } else if constexpr (EMAX >= 2) {
+      if (done <= 64) {
+        run(std::integral_constant<int, 2>());
+      } else if constexpr (EMAX >= 4) {
+        if (done <= 128) run(std::integral_constant<int, 4>());
+        else if constexpr (EMAX >= 8) run(std::integral_constant<int, 8>());
+      }
+    }
   }
   __syncwarp();
   for (int q = lane; q < npad; q += 32) sz[q] = -1.0f;

@@ -88,8 +88,9 @@ struct RenderSmem {
 };
 
 // Samples, sort, field taps, alpha and transmittance of ray r (frame b, S
-// samples) into ev; sorted depths stay in sm.z, sorted positions in sm.p.
-template <int E, int C>
+// samples) into ev; sorted depths stay in sm.z, with POS the sorted
+// positions in sm.p.
+template <int E, int C, bool POS>
 __device__ __forceinline__ void eval_ray(const RenderParams &p, long r, int b, int S, int sgm,
                                          const RenderSmem<E> &sm, RayEval<E> &ev) {
   const int lane = lane_id();
@@ -97,7 +98,7 @@ __device__ __forceinline__ void eval_ray(const RenderParams &p, long r, int b, i
   ev.done = warp_sample_ray(p.sp, r, b, S, nh, p.rand_const, sm.z, sm.i, *sm.sc);
   ev.valid = ev.proc = ev.post = 0;
   if (ev.done == 0) return;
-  warp_sort_samples(sm.z, sm.p, S, ev.done);
+  warp_sort_samples<E, POS>(sm.z, sm.p, S, ev.done);
   const float *bb = p.sp.t.vol_bbox + 6 * b;
   const float bmin[3] = {bb[0], bb[2], bb[4]};
   const float inv_vs = 1.0f / __ldg(p.sp.t.voxel_size + b);
@@ -165,7 +166,7 @@ __global__ void __launch_bounds__(256) render_fwd_kernel(RenderParams p) {
     int b, S, sgm;
     ray_frame(p, r, b, S, sgm);
     RayEval<E> ev;
-    eval_ray<E, C>(p, r, b, S, sgm, sm, ev);
+    eval_ray<E, C, true>(p, r, b, S, sgm, sm, ev);
     float acc_r = 0.0f, acc_g = 0.0f, acc_b = 0.0f, d = 0.0f, ws = 0.0f, aa = 0.0f;
     if (p.out_z) {
       for (int i = lane; i < Smax; i += 32) {
@@ -277,7 +278,7 @@ __global__ void __launch_bounds__(256) render_bwd_kernel(RenderParams p) {
     int b, S, sgm;
     ray_frame(p, r, b, S, sgm);
     RayEval<E> ev;
-    eval_ray<E, C>(p, r, b, S, sgm, sm, ev);
+    eval_ray<E, C, false>(p, r, b, S, sgm, sm, ev);
     if (ev.done == 0) {
       if (p.grad_sigma) {
         for (int i = lane; i < Smax; i += 32) {
@@ -314,9 +315,20 @@ __global__ void __launch_bounds__(256) render_bwd_kernel(RenderParams p) {
     // w*rgb, w*z, w, w*alpha; totals by carries (the forward's outputs)
     float w[E], pf[E][3], pd[E], pw[E], pa[E];
     float cf[3] = {0.0f, 0.0f, 0.0f}, cd = 0.0f, cw = 0.0f, ca = 0.0f;
+    const unsigned used = ev.proc & ev.valid;
 #pragma unroll
     for (int e = 0; e < E; e++) {
-      w[e] = (((ev.proc & ev.valid) >> e) & 1u) ? ev.al[e] * ev.tb[e] : 0.0f;
+      w[e] = ((used >> e) & 1u) ? ev.al[e] * ev.tb[e] : 0.0f;
+      if (!__any_sync(SG_FULL, (used >> e) & 1u)) {
+        // a block of positions no lane uses (past the ray's sample count or
+        // its termination): zero weights, the running totals stand
+#pragma unroll
+        for (int k = 0; k < 3; k++) pf[e][k] = cf[k];
+        pd[e] = cd;
+        pw[e] = cw;
+        pa[e] = ca;
+        continue;
+      }
 #pragma unroll
       for (int k = 0; k < 3; k++) {
         const float v = warp_incl_scan_f(w[e] * ev.rgb[e][k]);
@@ -411,7 +423,8 @@ __global__ void __launch_bounds__(256) render_bwd_kernel(RenderParams p) {
     const bool want_t = p.grad_tsdf != nullptr, want_f = p.grad_feat != nullptr;
 #pragma unroll
     for (int e = 0; e < E; e++) {
-      const bool use = (((ev.proc & ev.valid) >> e) & 1u) != 0;
+      const bool use = ((used >> e) & 1u) != 0;
+      if (!__any_sync(SG_FULL, use)) continue;  // no sample of this block contributes
       long long kf = -1, kt = -1;
       if (use) {
         const float pt[3] = {__fmaf_rn(dr[0], ev.z[e], o[0]), __fmaf_rn(dr[1], ev.z[e], o[1]),
@@ -446,10 +459,12 @@ __global__ void __launch_bounds__(256) render_bwd_kernel(RenderParams p) {
       s_kf[w8][lane] = kf;
       s_kt[w8][lane] = kt;
       __syncwarp();
+      // samples with a cell, in sorted order (the same mask in every lane)
+      const unsigned mf = __ballot_sync(SG_FULL, kf >= 0), mt = __ballot_sync(SG_FULL, kt >= 0);
       if (want_f) {
-        for (int j = 0; j < 32; j++) {
+        for (unsigned m = mf; m; m &= m - 1) {
+          const int j = __ffs(m) - 1;
           const long long k = s_kf[w8][j];
-          if (k < 0) continue;
           if (k != curf) {
             if (curf >= 0) flush_feat<C>(p, b, cell_of(curf), accf);
             curf = k;
@@ -467,9 +482,9 @@ __global__ void __launch_bounds__(256) render_bwd_kernel(RenderParams p) {
         }
       }
       if (want_t) {
-        for (int j = 0; j < 32; j++) {
+        for (unsigned m = mt; m; m &= m - 1) {
+          const int j = __ffs(m) - 1;
           const long long k = s_kt[w8][j];
-          if (k < 0) continue;
           if (k != curt) {
             if (curt >= 0) flush_tsdf<C>(p, b, cell_of(curt), acct);
             curt = k;

@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(256) sample_sorted_kernel(SampleParams p, cons
        r += ((long)gridDim.x * blockDim.x) >> 5) {
     const int nh = hit_count ? min(hit_count[r], p.W) : p.W;
     const int done = warp_sample_ray(p, r, (int)(r / p.N), S, nh, rand_const, s_z[w8], s_i[w8], s_sc[w8]);
-    warp_sort_samples(s_z[w8], s_p[w8], S, done);
+    warp_sort_samples<E, true>(s_z[w8], s_p[w8], S, done);
     for (int i = lane; i < S; i += 32) {
       out_z[(size_t)r * S + i] = s_z[w8][i];
       out_idx[(size_t)r * S + i] = s_i[w8][s_p[w8][i]];
