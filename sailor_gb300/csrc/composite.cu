@@ -87,7 +87,7 @@ __device__ __forceinline__ bool load_ray(const CompParams &p, long r, float *s_z
 template <int E, int CT>
 __global__ void __launch_bounds__(256) composite_fwd_kernel(CompParams p) {
   __shared__ float s_zall[8][32 * E];
-  __shared__ __align__(16) float s_fall[8][32 * E];
+  __shared__ __align__(16) float s_fall[8][kTransScratch<E>];
   const int lane = lane_id();
   float *s_z = s_zall[threadIdx.x >> 5];
   float *s_f = s_fall[threadIdx.x >> 5];
@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(256) composite_fwd_kernel(CompParams p) {
 template <int E, int CT>
 __global__ void __launch_bounds__(256) composite_bwd_kernel(CompParams p) {
   __shared__ float s_zall[8][32 * E];
-  __shared__ __align__(16) float s_fall[8][32 * E];
+  __shared__ __align__(16) float s_fall[8][kTransScratch<E>];
   const int lane = lane_id();
   float *s_z = s_zall[threadIdx.x >> 5];
   float *s_f = s_fall[threadIdx.x >> 5];

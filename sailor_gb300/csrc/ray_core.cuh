@@ -301,44 +301,79 @@ __device__ __forceinline__ void ray_alpha(const float (&z)[E], const float (&sg)
 // after each valid sample).  proc: position reached; post: transmittance
 // after the position still >= t_thres.
 //
-// Every lane runs the same chain (warp-uniform), four positions per step
-// from a shared-memory factor array; the factors are overwritten in place
-// by the transmittance before each position, which the owning lanes read
-// back.  Positions before the first valid one are padding (factor 1) and
-// are skipped.  s_f: 32*E floats of warp-private shared scratch.
+// Every lane runs the same chain (warp-uniform), eight positions per step
+// from a shared-memory factor array; lane 0 stores the transmittance before
+// each position into a second array, which the owning lanes read back.
+// When every factor is in [0, 1] the product never increases (rounding is
+// monotonic), so one test of the step's last value finds the step where it
+// first falls below t_thres; otherwise the step's lowest value is tested.
+// The product changes only at valid positions.
+// Positions before the first valid one are padding (factor 1) and are
+// skipped.  s_f: kTransScratch<E> floats of warp-private shared scratch,
+// 16-byte aligned.
+template <int E>
+constexpr int kTransScratch = 2 * (32 * E + 8);
+
 template <int E>
 __device__ __forceinline__ void ray_transmittance(const float (&al)[E], unsigned valid, int S, float t_thres,
                                                   float *s_f, float (&tb)[E], unsigned &proc, unsigned &post) {
   const int lane = lane_id();
+  float *s_t = s_f + kTransScratch<E> / 2;
   int m0 = 32 * E;
 #pragma unroll
   for (int e = E - 1; e >= 0; e--) {
     const unsigned vb = __ballot_sync(SG_FULL, (valid >> e) & 1u);
     if (vb) m0 = e * 32 + __ffs(vb) - 1;
   }
+  bool unit = true;  // every factor in [0, 1] (false for NaN)
 #pragma unroll
-  for (int e = 0; e < E; e++) s_f[e * 32 + lane] = ((valid >> e) & 1u) ? (1.0f - al[e]) : 1.0f;
+  for (int e = 0; e < E; e++) {
+    const float f = ((valid >> e) & 1u) ? (1.0f - al[e]) : 1.0f;
+    unit = unit && f >= 0.0f && f <= 1.0f;
+    s_f[e * 32 + lane] = f;
+  }
+  if (lane < 8) s_f[32 * E + lane] = 1.0f;  // the last step may read past position 32 E - 1
+  const bool mono = __all_sync(SG_FULL, unit);
   __syncwarp();
   int stop = 1 << 30;  // position whose update took T below t_thres
   int end = S;
   if (m0 < S) {
     float T = 1.0f;
-    for (int i = m0 & ~3; i < S; i += 4) {
-      const float4 f = *reinterpret_cast<const float4 *>(s_f + i);
-      const float T1 = T * f.x, T2 = T1 * f.y, T3 = T2 * f.z, T4 = T3 * f.w;
-      __syncwarp();
-      if (lane == 0) *reinterpret_cast<float4 *>(s_f + i) = make_float4(T, T1, T2, T3);
-      __syncwarp();
-      const bool c1 = i >= m0 && T1 < t_thres;
-      const bool c2 = i + 1 >= m0 && i + 1 < S && T2 < t_thres;
-      const bool c3 = i + 2 >= m0 && i + 2 < S && T3 < t_thres;
-      const bool c4 = i + 3 >= m0 && i + 3 < S && T4 < t_thres;
-      if (c1 || c2 || c3 || c4) {
-        stop = c1 ? i : (c2 ? i + 1 : (c3 ? i + 2 : i + 3));
-        end = stop + 1;
-        break;
+    for (int i = m0 & ~3; i < S; i += 8) {
+      const float4 f0 = *reinterpret_cast<const float4 *>(s_f + i);
+      const float4 f1 = *reinterpret_cast<const float4 *>(s_f + i + 4);
+      float Ta[9];
+      Ta[0] = T;
+      Ta[1] = Ta[0] * f0.x;
+      Ta[2] = Ta[1] * f0.y;
+      Ta[3] = Ta[2] * f0.z;
+      Ta[4] = Ta[3] * f0.w;
+      Ta[5] = Ta[4] * f1.x;
+      Ta[6] = Ta[5] * f1.y;
+      Ta[7] = Ta[6] * f1.z;
+      Ta[8] = Ta[7] * f1.w;
+      if (lane == 0) {
+        *reinterpret_cast<float4 *>(s_t + i) = make_float4(Ta[0], Ta[1], Ta[2], Ta[3]);
+        *reinterpret_cast<float4 *>(s_t + i + 4) = make_float4(Ta[4], Ta[5], Ta[6], Ta[7]);
       }
-      T = T4;
+      // lowest transmittance of the step: the last when the product cannot rise
+      float lo = Ta[8];
+      if (!mono)
+        lo = fminf(fminf(fminf(Ta[1], Ta[2]), fminf(Ta[3], Ta[4])), fminf(fminf(Ta[5], Ta[6]), fminf(Ta[7], Ta[8])));
+      if (lo < t_thres) {
+        // the first position q of [m0, S) in this step with T after it below
+        // t_thres (outside [m0, S) the factors are 1)
+        int k = 8;
+#pragma unroll
+        for (int q = 7; q >= 0; q--)
+          if (Ta[q + 1] < t_thres && i + q >= m0 && i + q < S) k = q;
+        if (k < 8) {
+          stop = i + k;
+          end = stop + 1;
+          break;
+        }
+      }
+      T = Ta[8];
     }
   } else {
     end = 0;
@@ -351,7 +386,7 @@ __device__ __forceinline__ void ray_transmittance(const float (&al)[E], unsigned
     const int i = e * 32 + lane;
     tb[e] = 0.0f;
     if (i >= m0 && i < end) {
-      tb[e] = s_f[i];
+      tb[e] = s_t[i];
       proc |= 1u << e;
       if (i != stop) post |= 1u << e;
     }

@@ -149,7 +149,7 @@ __device__ __forceinline__ void eval_ray(const RenderParams &p, long r, int b, i
 
 #define SG_RENDER_SMEM(E)                         \
   __shared__ __align__(16) float s_zall[8][32 * E]; \
-  __shared__ __align__(16) float s_fall[8][32 * E]; \
+  __shared__ __align__(16) float s_fall[8][kTransScratch<E>]; \
   __shared__ int s_iall[8][32 * E];                 \
   __shared__ int s_pall[8][32 * E];                 \
   __shared__ SampleScratch s_sc[8];                 \

@@ -234,6 +234,24 @@ def test_composite_presorted():
         assert np.abs(a.cpu().numpy() - b)[ok].max() <= ATOL
 
 
+@pytest.mark.parametrize("alpha_lo,alpha_hi,t_thres", [(-0.3, 1.4, 1e-4), (0.0, 1.0, 1.5)])
+def test_composite_alpha_outside_unit_interval(alpha_lo, alpha_hi, t_thres):
+    """Occupancy compositing (alpha given) with alphas outside [0, 1], where
+    the transmittance can rise or change sign, and a threshold above 1 (stop
+    at the first sample): outputs, and so the early-termination positions,
+    match the oracle."""
+    from sailor_gb300.dist import VoxelEncoding as VE
+    z, idx, _, _, feats, _ = _comp_inputs(5)
+    a = np.random.default_rng(6).uniform(alpha_lo, alpha_hi, z.shape + (1,)).astype(np.float32)
+    out = VE.volume_rendering_training_forward(_t(z), _t(idx, torch.int32), _t(a), _t(feats), 0, t_thres, True)
+    rf, rd, rw, ra, fl = orc.composite_fwd(z, idx, a, feats, t_thres, True)
+    ok = fl == 0
+    assert ok.mean() > 0.9
+    for x, y in zip(out, (rf, rd, rw, ra)):
+        # relative to the largest output: the transmittance can grow past 1
+        assert np.abs(x.cpu().numpy() - y)[ok].max() <= ATOL * max(1.0, np.abs(y).max())
+
+
 @pytest.mark.parametrize("occ_mode", [False, True])
 def test_composite_bwd_reference_formula(occ_mode):
     """The reference gradient formula (volume_rendering.cu:244-522).  The last
