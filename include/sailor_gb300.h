@@ -378,7 +378,8 @@ typedef struct SgRaySegments {
  * sdf_s) / sdf_s of the trilinear TSDF t (tsdf [B,D,D,D] over the tree's
  * vol_bbox / voxel_size); colour = head [3,C] x trilinear features of feat
  * [B,Df,Df,Df,C] over feat_bbox / feat_vs (head NULL: C == 3 and colour =
- * features).  C is 3 or 16. */
+ * features).  C is 3 or 16; with C == 16, feat and head are 16-byte
+ * aligned (SG_ERR_INVALID_ARG otherwise). */
 typedef struct SgRenderArgs {
   const float *ori, *dir;
   const int *hit_idx;

@@ -265,7 +265,7 @@ __device__ __forceinline__ void flush_tsdf(const RenderParams &p, int b, const C
 // d rgb = loss_scale * (rgb - target)); the outputs and per-ray loss are
 // written, and nothing is recomputed.
 template <int E, int C, bool TRAIN>
-__global__ void __launch_bounds__(256) render_bwd_kernel(RenderParams p) {
+__global__ void __launch_bounds__(256, 2) render_bwd_kernel(RenderParams p) {
   static_assert(C == 3 || C == 16, "feature grids of 3 or 16 channels");
   SG_RENDER_SMEM(E)
   __shared__ float s_wf[8][32][9], s_wt[8][32][9];
@@ -335,15 +335,33 @@ __global__ void __launch_bounds__(256) render_bwd_kernel(RenderParams p) {
         pf[e][k] = cf[k] + v;
         cf[k] += __shfl_sync(SG_FULL, v, 31);
       }
-      const float vd = warp_incl_scan_f(w[e] * ev.z[e]);
-      const float vw = warp_incl_scan_f(w[e]);
-      const float va = warp_incl_scan_f(w[e] * ev.al[e]);
-      pd[e] = cd + vd;
-      pw[e] = cw + vw;
-      pa[e] = ca + va;
-      cd += __shfl_sync(SG_FULL, vd, 31);
-      cw += __shfl_sync(SG_FULL, vw, 31);
-      ca += __shfl_sync(SG_FULL, va, 31);
+      if (!TRAIN) {
+        const float vd = warp_incl_scan_f(w[e] * ev.z[e]);
+        const float vw = warp_incl_scan_f(w[e]);
+        const float va = warp_incl_scan_f(w[e] * ev.al[e]);
+        pd[e] = cd + vd;
+        pw[e] = cw + vw;
+        pa[e] = ca + va;
+        cd += __shfl_sync(SG_FULL, vd, 31);
+        cw += __shfl_sync(SG_FULL, vw, 31);
+        ca += __shfl_sync(SG_FULL, va, 31);
+      }
+    }
+    if (TRAIN) {
+      // the loss reads only the colour: depth, weight sum and alpha sum are
+      // outputs alone, summed as the forward kernel sums them
+      float d = 0.0f, ws = 0.0f, aa = 0.0f;
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        if ((used >> e) & 1u) {
+          d += w[e] * ev.z[e];
+          ws += w[e];
+          aa += w[e] * ev.al[e];
+        }
+      }
+      cd = warp_sum(d);
+      cw = warp_sum(ws);
+      ca = warp_sum(aa);
     }
     if (TRAIN) {
       // forward outputs = the totals; upstream gradient of the per-ray loss
@@ -374,8 +392,10 @@ __global__ void __launch_bounds__(256) render_bwd_kernel(RenderParams p) {
       grgb[e][0] = grgb[e][1] = grgb[e][2] = 0.0f;
       if (((ev.proc & ev.valid) >> e) & 1u) {
         const float Ta = ev.tb[e] * (1.0f - ev.al[e]);
-        float acc = gws * (Ta - (cw - pw[e])) + gd * (Ta * ev.z[e] - (cd - pd[e])) +
-                    ga * (2.0f * ev.al[e] * Ta - (ca - pa[e]));
+        float acc = 0.0f;
+        if (!TRAIN)
+          acc = gws * (Ta - (cw - pw[e])) + gd * (Ta * ev.z[e] - (cd - pd[e])) +
+                ga * (2.0f * ev.al[e] * Ta - (ca - pa[e]));
 #pragma unroll
         for (int k = 0; k < 3; k++) acc += gc[k] * (Ta * ev.rgb[e][k] - (cf[k] - pf[e][k]));
         gsig[e] = ev.dl[e] * acc;
@@ -571,7 +591,8 @@ static int segment_params(const SgTree *tree, const SgRaySegments *seg, const Sg
   p.dk = a->sdf_scale / a->sdf_s;
   p.inv_s = 1.0f / a->sdf_s;
   p.shared = a->Df == a->D && a->feat_bbox == tree->vol_bbox && a->feat_vs == tree->voxel_size;
-  if (a->C == 16 && (((uintptr_t)a->feat) % 16 != 0)) return SG_ERR_INVALID_ARG;
+  // float4 loads of the feature rows and of the colour head's rows
+  if (a->C == 16 && (((uintptr_t)a->feat) % 16 != 0 || ((uintptr_t)a->head) % 16 != 0)) return SG_ERR_INVALID_ARG;
   return SG_OK;
 }
 
