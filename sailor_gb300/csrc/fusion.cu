@@ -292,10 +292,11 @@ __device__ __forceinline__ void load_views(const FuseParams &p, int b, ViewSmem 
 }
 
 // Fuse the VPT z-consecutive voxels (x, y, z0 .. z0+VPT-1) over all views and
-// store them; returns how many of them are occupied.
+// store them; returns how many of them are occupied.  Views whose bit is set
+// in skip are left out (none of these voxels passes their early returns).
 template <int VPT>
 __device__ __forceinline__ int fuse_group(const FuseParams &p, const FuseFrame &f, const ViewSmem &vw, int x,
-                                          int y, int z0) {
+                                          int y, int z0, unsigned skip) {
   const long v0 = ((long)x * p.Dy + y) * p.Dz + z0;
   float px = __fmaf_rn((float)x, f.vs, f.bx);
   float py = __fmaf_rn((float)y, f.vs, f.by);
@@ -308,6 +309,7 @@ __device__ __forceinline__ int fuse_group(const FuseParams &p, const FuseFrame &
     col[j] = 0.0f;
   }
   for (int k = 0; k < vw.n; k++) {
+    if ((skip >> k) & 1u) continue;
     const float *P = vw.P[k];
     const float *Kk = vw.K[k];
     float ax = __fmaf_rn(P[0], px, P[1] * py);
@@ -365,10 +367,142 @@ __global__ void __launch_bounds__(256) fuse_tsdf_kernel(FuseParams p) {
     long rem = v0 - (long)x * p.Dy * p.Dz;
     int y = (int)(rem / p.Dz);
     int z0 = (int)(rem - (long)y * p.Dz);
-    cnt += fuse_group<VPT>(p, f, vw, x, y, z0);
+    cnt += fuse_group<VPT>(p, f, vw, x, y, z0, 0u);
   }
   cnt = warp_sum(cnt);
   if (lane_id() == 0 && cnt) atomicAdd(p.count + b, cnt);
+}
+
+// Per-view culling of a voxel tile.  A view is left out of a whole tile
+// when every voxel of the tile would take one of integrate_view's early
+// returns for it, so the tile's results are unchanged:
+//   * every corner of the tile is behind the camera (cz < 0 for all voxels:
+//     cz is affine in the voxel position, extreme at the corners), or
+//   * the tile is in front of the camera (cz, uz > 0 at every corner) and
+//     the pixel rectangle that holds the projections of all its voxels
+//     (the projection of a box in front of the camera lies in the convex
+//     hull of its corners' projections; widened by 2 pixels for rounding)
+//     either misses the image, or holds no valid depth, or its deepest
+//     valid depth is more than trunc in front of the tile's nearest corner
+//     (diff < -trunc for every voxel).
+// Margins of 1e-4 m (and 1e-5 relative) cover the rounding of the float
+// camera coordinates; a NaN depth, which integrate_view takes as valid,
+// keeps the view.  Rectangles above kCullMaxPixels keep the view unscanned.
+constexpr float kCullEps = 1.0e-4f;
+constexpr int kCullMaxPixels = 1 << 15;
+
+struct CullSmem {
+  int rect[kMaxViews][4];  // x0, x1, y0, y1 (clamped to the image)
+  float czmin[kMaxViews];
+  int state[kMaxViews];    // 0: keep, 1: leave out, 2: scan the rectangle
+  float wmax[2][8];
+  int wnan[2][8];
+  unsigned skip;
+};
+
+// The CTA (256 threads; every thread calls) finds the views to leave out of
+// the tile of voxels lo .. hi (inclusive).  Result in cs.skip.
+__device__ __forceinline__ void tile_cull(const FuseParams &p, const FuseFrame &f, const ViewSmem &vw,
+                                          const int (&lo)[3], const int (&hi)[3], CullSmem &cs) {
+  const int tid = threadIdx.x, n = vw.n;
+  __syncthreads();  // the previous tile's readers of cs are done
+  // corners: thread = (view tid / 8, corner tid % 8), kMaxViews * 8 == 256
+  {
+    const int k = tid >> 3, c = tid & 7;
+    const int kv = k < n ? k : 0;
+    const float px = __fmaf_rn((float)((c & 4) ? hi[0] : lo[0]), f.vs, f.bx);
+    const float py = __fmaf_rn((float)((c & 2) ? hi[1] : lo[1]), f.vs, f.by);
+    const float pz = __fmaf_rn((float)((c & 1) ? hi[2] : lo[2]), f.vs, f.bz);
+    const float *P = vw.P[kv], *Kk = vw.K[kv];
+    const float cx = __fmaf_rn(P[2], pz, __fmaf_rn(P[0], px, P[1] * py)) + P[3];
+    const float cy = __fmaf_rn(P[6], pz, __fmaf_rn(P[4], px, P[5] * py)) + P[7];
+    const float cz = __fmaf_rn(P[10], pz, __fmaf_rn(P[8], px, P[9] * py)) + P[11];
+    const float ux = dot3c(Kk[0], Kk[1], Kk[2], cx, cy, cz);
+    const float uy = dot3c(Kk[3], Kk[4], Kk[5], cx, cy, cz);
+    const float uz = dot3c(Kk[6], Kk[7], Kk[8], cx, cy, cz);
+    float qx0 = ux / uz, qx1 = qx0, qy0 = uy / uz, qy1 = qy0;
+    float zmin = cz, zmax = cz, uzmin = uz;
+    bool fin = isfinite(qx0) && isfinite(qy0);
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+      qx0 = fminf(qx0, __shfl_xor_sync(SG_FULL, qx0, o));
+      qx1 = fmaxf(qx1, __shfl_xor_sync(SG_FULL, qx1, o));
+      qy0 = fminf(qy0, __shfl_xor_sync(SG_FULL, qy0, o));
+      qy1 = fmaxf(qy1, __shfl_xor_sync(SG_FULL, qy1, o));
+      zmin = fminf(zmin, __shfl_xor_sync(SG_FULL, zmin, o));
+      zmax = fmaxf(zmax, __shfl_xor_sync(SG_FULL, zmax, o));
+      uzmin = fminf(uzmin, __shfl_xor_sync(SG_FULL, uzmin, o));
+      fin = __shfl_xor_sync(SG_FULL, (int)fin, o) && fin;
+    }
+    if (c == 0 && k < n) {
+      int state = 0;
+      if (zmax < -kCullEps) {
+        state = 1;
+      } else if (zmin > kCullEps && uzmin > kCullEps && fin && fabsf(qx0) < 1.0e6f && fabsf(qx1) < 1.0e6f &&
+                 fabsf(qy0) < 1.0e6f && fabsf(qy1) < 1.0e6f) {
+        const int H = vw.hw[k][0], W = vw.hw[k][1];
+        const int x0 = max((int)floorf(qx0) - 2, 0), x1 = min((int)ceilf(qx1) + 2, W - 1);
+        const int y0 = max((int)floorf(qy0) - 2, 0), y1 = min((int)ceilf(qy1) + 2, H - 1);
+        if (x0 > x1 || y0 > y1) {
+          state = 1;
+        } else if ((long)(x1 - x0 + 1) * (y1 - y0 + 1) <= kCullMaxPixels) {
+          state = 2;
+          cs.rect[k][0] = x0;
+          cs.rect[k][1] = x1;
+          cs.rect[k][2] = y0;
+          cs.rect[k][3] = y1;
+          cs.czmin[k] = zmin;
+        }
+      }
+      cs.state[k] = state;
+    }
+  }
+  __syncthreads();
+  unsigned skip = 0u;
+  const int w8 = tid >> 5;
+  int buf = 0;
+  for (int k = 0; k < n; k++) {
+    const int state = cs.state[k];
+    if (state == 1) skip |= 1u << k;
+    if (state != 2) continue;
+    // deepest valid depth in the rectangle (16 x 16 threads over its pixels)
+    const int x0 = cs.rect[k][0], x1 = cs.rect[k][1], y0 = cs.rect[k][2], y1 = cs.rect[k][3];
+    const float *dimg = p.depth + vw.off[k];
+    const int W = vw.hw[k][1];
+    float m = -INFINITY;
+    int nan = 0;
+    for (int y = y0 + (tid >> 4); y <= y1; y += 16) {
+      const float *row = dimg + (size_t)y * W;
+      for (int x = x0 + (tid & 15); x <= x1; x += 16) {
+        const float dv = __ldg(row + x);
+        if (!(dv < 0.1f || dv > 4.0f)) {
+          m = fmaxf(m, dv);
+          nan |= dv != dv;
+        }
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      m = fmaxf(m, __shfl_xor_sync(SG_FULL, m, o));
+      nan |= __shfl_xor_sync(SG_FULL, nan, o);
+    }
+    if ((tid & 31) == 0) {
+      cs.wmax[buf][w8] = m;
+      cs.wnan[buf][w8] = nan;
+    }
+    __syncthreads();
+    float M = cs.wmax[buf][0];
+    int anynan = cs.wnan[buf][0];
+#pragma unroll
+    for (int j = 1; j < 8; j++) {
+      M = fmaxf(M, cs.wmax[buf][j]);
+      anynan |= cs.wnan[buf][j];
+    }
+    buf ^= 1;  // the next view writes the other half, so no second barrier
+    if (!anynan && (M == -INFINITY || M - cs.czmin[k] < -f.trunc - kCullEps - 1.0e-5f * fabsf(M))) skip |= 1u << k;
+  }
+  if (tid == 0) cs.skip = skip;
+  __syncthreads();
 }
 
 // Tiled order: a CTA of 256 threads fuses a 16 x 16 x 16 voxel tile, as four
@@ -376,12 +510,15 @@ __global__ void __launch_bounds__(256) fuse_tsdf_kernel(FuseParams p) {
 // voxels of one tile project to one compact patch of every view, so the
 // depth/colour gathers of the tile reuse L1 lines (a linear run of z voxels
 // projects to a line of distinct pixels instead).  Tiles are taken z-fastest
-// so CTAs resident at the same time work on neighbouring tiles.
+// so CTAs resident at the same time work on neighbouring tiles.  Views that
+// no voxel of the tile can pass are left out of the tile (tile_cull).
 constexpr int kTileEdge = 16;
 
 __global__ void __launch_bounds__(256) fuse_tsdf_tiled_kernel(FuseParams p, int tiles_y, int tiles_z,
                                                               long n_tiles) {
+  static_assert(kMaxViews * 8 == 256, "one corner thread per (view, corner)");
   __shared__ ViewSmem vw;
+  __shared__ CullSmem cs;
   const int b = blockIdx.y;
   load_views(p, b, vw);
   const FuseFrame f = fuse_frame(p, b);
@@ -391,12 +528,17 @@ __global__ void __launch_bounds__(256) fuse_tsdf_tiled_kernel(FuseParams p, int 
     const int Tz = (int)(t % tiles_z);
     const long r = t / tiles_z;
     const int Ty = (int)(r % tiles_y), Tx = (int)(r / tiles_y);
-    const int y = Ty * kTileEdge + ty, z0 = Tz * kTileEdge + tz * 4;
+    const int lo[3] = {Tx * kTileEdge, Ty * kTileEdge, Tz * kTileEdge};
+    const int hi[3] = {min(lo[0] + kTileEdge - 1, p.Dx - 1), min(lo[1] + kTileEdge - 1, p.Dy - 1),
+                       min(lo[2] + kTileEdge - 1, p.Dz - 1)};
+    tile_cull(p, f, vw, lo, hi, cs);
+    const unsigned skip = cs.skip;
+    const int y = lo[1] + ty, z0 = lo[2] + tz * 4;
     if (y >= p.Dy || z0 >= p.Dz) continue;
 #pragma unroll 1
     for (int pass = 0; pass < kTileEdge / 4; pass++) {
-      const int x = Tx * kTileEdge + pass * 4 + tx;
-      if (x < p.Dx) cnt += fuse_group<4>(p, f, vw, x, y, z0);
+      const int x = lo[0] + pass * 4 + tx;
+      if (x < p.Dx) cnt += fuse_group<4>(p, f, vw, x, y, z0, skip);
     }
   }
   cnt = warp_sum(cnt);
