@@ -297,7 +297,15 @@ def padded_views(fr):
     return np.stack(fr["K"])[None], np.stack(fr["RT"])[None], dep, col
 
 
-def batch_algorithmic_bytes(bcfg, w, n_hits, R, n_samples):
+def near_node_bricks(bp):
+    """Top bricks sg_zero_near_nodes clears for the pipeline's last gradient
+    pass: the nodes' bricks and their 26-neighbourhoods."""
+    B, Dt = bp.B, bp.Dt
+    m = (bp.grad_bricks >= 0).view(B, 1, Dt, Dt, Dt).float()
+    return int(torch.nn.functional.max_pool3d(m, 3, stride=1, padding=1).sum().item())
+
+
+def batch_algorithmic_bytes(bcfg, w, n_hits, R, n_samples, n_clear_bricks=None):
     """Per-launch algorithmic HBM bytes of each batched stage."""
     B, D, C = bcfg["frames"], bcfg["D"], bcfg["C"]
     V, Vt = B * D ** 3, B * (D // bcfg["rate"]) ** 3
@@ -313,8 +321,9 @@ def batch_algorithmic_bytes(bcfg, w, n_hits, R, n_samples):
         # per-ray loss out; the atomic adds into the feature-gradient grid
         # are not counted
         train=24 * R + 12 * n_hits + 8 * R + 12 * R + 24 * R + 4 * R,
-        # zeroing of the feature-gradient grid (side stream, overlapped)
-        zero_grad=4 * V * C,
+        # clear of the feature-gradient grid near the previous pass's nodes
+        # (side stream, beside fusion): 4 C bytes per voxel of those bricks
+        zero_grad=4 * C * bcfg["rate"] ** 3 * (n_clear_bricks if n_clear_bricks is not None else Vt),
     )
 
 
@@ -551,7 +560,7 @@ def run_batch(args):
     if rank == 0:
         pk, pk_kind = peaks()
         S_all = sum(n * s for _, n, s in targets)
-        ab = batch_algorithmic_bytes(bcfg, w, n_hits, R, S_all)
+        ab = batch_algorithmic_bytes(bcfg, w, n_hits, R, S_all, near_node_bricks(bp))
         rl = {k: ab[k] / (stages[k] / 1000.0) / 1e9 for k in ab if stages.get(k)}
         dom = max(rl, key=lambda k: stages[k])
         traffic = None

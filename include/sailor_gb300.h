@@ -274,6 +274,18 @@ int sg_grid_scatter(const float *ori, const float *dir, const float *z, int B,
                     const float *voxel_size, int mode, float scale, float s,
                     float *grad_grid, sg_stream_t stream);
 
+/* Zero of the part of a gradient grid a training pass can write.  grid
+ * [B, Db, Db, Db, C] lies on the tree's fine geometry (voxel centres at
+ * vol_bbox min + index * voxel_size); every top brick that is a node of the
+ * tree or borders one (26-neighbourhood) is set to 0 -- a trilinear tap at a
+ * sample inside a node (a brick, or a voxel of one) reaches at most one
+ * voxel beyond the brick.  After a pass over this tree accumulated into a
+ * grid that was 0 elsewhere, this restores an all-zero grid at a fraction
+ * of a full clear.  Bricks are cleared with 16-byte stores when rate * C is
+ * a multiple of 4 and grid is 16-byte aligned.  No counterpart in the
+ * reference (its training step clears dense gradients with torch). */
+int sg_zero_near_nodes(const SgTree *tree, float *grid, int C, sg_stream_t stream);
+
 /* Node-corner trilinear aggregation.  Replaces
  * MultiLayerOctree::trilinear_aggregate_features(_backward)
  * (sampling_kernel.cu:162-327, 1384-1462).  ori/dir [B,N,3],

@@ -23,7 +23,7 @@ EXPORTS = (
     "sg_render_fused", "sg_tune_set", "sg_tune_get", "sg_tree_build_static",
     "sg_grid_scatter", "sg_fuse_tsdf_views", "sg_intersect_segments", "sg_render_segments_fwd",
     "sg_render_segments_bwd", "sg_render_segments_train",
-    "sg_camera_params", "sg_rays_from_cameras", "sg_segment_rays",
+    "sg_camera_params", "sg_rays_from_cameras", "sg_segment_rays", "sg_zero_near_nodes",
 )
 
 
@@ -95,6 +95,7 @@ def _load():
     lib.sg_camera_params.argtypes = [p, p, p, i, p, p]
     lib.sg_rays_from_cameras.argtypes = [p, p, p, i, i, i, i, p, p]
     lib.sg_segment_rays.argtypes = [C.POINTER(SgRaySegments), p, p, p]
+    lib.sg_zero_near_nodes.argtypes = [C.POINTER(SgTree), p, i, p]
     lib.sg_tune_set.argtypes = [i, i]
     lib.sg_tune_get.argtypes = [i]
     lib.sg_trilerp_nodes_fwd.argtypes = [C.POINTER(SgTree), p, p, p, p, p, i, i, i, p, p]

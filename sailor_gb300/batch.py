@@ -139,6 +139,12 @@ class BatchPipeline:
         self.head = torch.zeros((3, C), **f32)
         self.grad_feat = torch.zeros((B, D, D, D, C), **f32)
         self.grad_tsdf = torch.zeros((B, D, D, D), **f32)
+        # brick map of the tree the gradients were last accumulated over (-1:
+        # none): outside its nodes' bricks and their neighbours the gradient
+        # grids are 0, so train_step clears only those (sg_zero_near_nodes)
+        self.grad_bricks = torch.full((Vt,), -1, **i32)
+        self.grad_tree = N.SgTree(B, self.Dt, D, rate, Vol, 0, Vt, Vol, N.ptr(self.grad_bricks), None, None, None,
+                                  None, None, None, N.ptr(self.voxel_size), N.ptr(self.vol_bbox))
         self.out_rgb = torch.empty((R, 3), **f32)
         self.out_depth = torch.empty(R, **f32)
         self.out_ws = torch.empty(R, **f32)
@@ -150,7 +156,7 @@ class BatchPipeline:
         self.trunc_weight = None
         self.events = None
         self.side_events = None
-        self.side = torch.cuda.Stream(device=dev)  # zeroing of the gradient grids beside the build
+        self.side = torch.cuda.Stream(device=dev)  # zeroing of the gradient grids beside fusion
 
     # ------------------------------------------------------------------ inputs
     def load_views(self, frames, vol_bbox, voxel_size, trunc_weight):
@@ -222,7 +228,7 @@ class BatchPipeline:
         return ev
 
     # ------------------------------------------------------------------ stages
-    def build(self, obs_weight=1.0, th_low=13.5, th_high=13.5):
+    def build(self, obs_weight=1.0, th_low=13.5, th_high=13.5, before_tree=None):
         st = N.stream()
         self.cnt.zero_()
         self.status.zero_()
@@ -233,6 +239,8 @@ class BatchPipeline:
                                          N.ptr(self.colorv), N.ptr(self.occ0), N.ptr(self.cnt[0]), st),
                 "fuse_tsdf_views")
         self._mark("fusion")
+        if before_tree is not None:
+            before_tree()
         N.check(N.lib.sg_brick_occupancy(N.ptr(self.occ0), self.B, self.D, self.rate, N.ptr(self.occ1),
                                          N.ptr(self.cnt[1]), st), "brick_occupancy")
         N.check(N.lib.sg_tree_build(C.byref(self.tree), N.ptr(self.occ1), N.ptr(self.occ0), N.ptr(self.scratch),
@@ -263,41 +271,55 @@ class BatchPipeline:
                  tsdf_grad=True, zero=True):
         if zero:
             self.grad_feat.zero_()
-            if tsdf_grad:
-                self.grad_tsdf.zero_()
+            self.grad_tsdf.zero_()  # both, so one brick map describes both grids
         self._mark("grad_prep")
         N.check(N.lib.sg_render_segments_bwd(C.byref(self.tree), C.byref(self.seg), C.byref(self.args),
                                              N.ptr(g_rgb), N.ptr(g_depth), N.ptr(g_ws), N.ptr(g_alpha),
                                              N.ptr(self.grad_feat), N.ptr(self.grad_tsdf) if tsdf_grad else None,
                                              N.ptr(grad_sigma), N.ptr(grad_rgb), N.stream()), "render_bwd")
         self._mark("backward")
+        if zero:
+            self.grad_bricks.copy_(self.brick_node)
+        else:
+            self.grad_bricks.fill_(0)  # unknown region: the next train_step clears everything
 
     def train_step(self):
         """Build, intersect, then one fused pass per ray: forward, the mean
         squared colour error against target_rgb (per-ray terms in out_loss)
         and its backward into grad_feat (and grad_tsdf when train_tsdf).
-        Allocates nothing.  The gradient grids are zeroed on a side stream
-        while fusion, tree build and intersection run (a memory-bound fill
-        beside compute-bound stages); the training pass waits for both."""
+        Allocates nothing.  The gradient grids are owned by the pipeline:
+        read them, do not write them (zero_grads() after writing).  Before
+        accumulating, train_step clears only the bricks the previous
+        gradient pass could reach (sg_zero_near_nodes over its brick map),
+        on a side stream beside fusion; the tree build waits for it, as it
+        rewrites the brick map the clear reads."""
         main = torch.cuda.current_stream()
         self.side.wait_stream(main)  # the previous step's users of the grids come first
         with torch.cuda.stream(self.side):
             z0 = self._side_event()
-            self.grad_feat.zero_()
+            N.check(N.lib.sg_zero_near_nodes(C.byref(self.grad_tree), N.ptr(self.grad_feat), self.C, N.stream()),
+                    "zero_near_nodes")
             if self.train_tsdf:
-                self.grad_tsdf.zero_()
+                N.check(N.lib.sg_zero_near_nodes(C.byref(self.grad_tree), N.ptr(self.grad_tsdf), 1, N.stream()),
+                        "zero_near_nodes")
             if z0 is not None:
                 self.side_events = (z0, self._side_event())
-        self.build()
+        self.build(before_tree=lambda: main.wait_stream(self.side))
         self.intersect()
-        main.wait_stream(self.side)
         self._mark("grad_prep")
         N.check(N.lib.sg_render_segments_train(
             C.byref(self.tree), C.byref(self.seg), C.byref(self.args), N.ptr(self.target_rgb),
             2.0 / (3.0 * self.R), N.ptr(self.out_rgb), N.ptr(self.out_depth), N.ptr(self.out_ws),
             N.ptr(self.out_alpha), N.ptr(self.out_loss), N.ptr(self.grad_feat),
             N.ptr(self.grad_tsdf) if self.train_tsdf else None, N.stream()), "render_train")
+        self.grad_bricks.copy_(self.brick_node)
         self._mark("train")
+
+    def zero_grads(self):
+        """Clear the gradient grids entirely (after writing into them)."""
+        self.grad_feat.zero_()
+        self.grad_tsdf.zero_()
+        self.grad_bricks.fill_(-1)
 
     def train_step_unfused(self):
         """The same step with separate forward and backward launches (the

@@ -174,6 +174,34 @@ __global__ void __launch_bounds__(256) grid_scatter_kernel(ScatterParams p) {
   }
 }
 
+// Zero of the part of a gradient grid [B, Db, Db, Db, C] (the tree's fine
+// geometry) that a training pass over the tree's nodes can write: a CTA per
+// top brick tests the brick's 26-neighbourhood for a node and, if it finds
+// one, clears the brick's rate^3 voxels (rate z-runs of rate * C floats).
+__global__ void __launch_bounds__(256) zero_near_nodes_kernel(SgTree t, float *grid, int C, int vec4) {
+  const int b = blockIdx.y, Dt = t.Dt;
+  const long vt = (long)Dt * Dt * Dt;
+  const long brick = blockIdx.x;
+  const int X = (int)(brick / ((long)Dt * Dt)), Y = (int)((brick / Dt) % Dt), Z = (int)(brick % Dt);
+  int near = 0;
+  if (threadIdx.x < 27) {
+    const int x = X + (int)threadIdx.x / 9 - 1, y = Y + ((int)threadIdx.x / 3) % 3 - 1, z = Z + (int)threadIdx.x % 3 - 1;
+    if (x >= 0 && y >= 0 && z >= 0 && x < Dt && y < Dt && z < Dt)
+      near = __ldg(t.brick_node + b * vt + ((long)x * Dt + y) * Dt + z) >= 0;
+  }
+  if (!__syncthreads_or(near)) return;
+  const int r = t.rate, Db = t.Db;
+  const int per_run = vec4 ? r * C / 4 : r * C;  // stores per z-run
+  float *g = grid + (size_t)b * Db * Db * Db * C;
+  for (int i = threadIdx.x; i < r * r * per_run; i += blockDim.x) {
+    const int xy = i / per_run, k = i - xy * per_run;
+    const int x = X * r + xy / r, y = Y * r + xy % r;
+    const size_t off = (((size_t)x * Db + y) * Db + (size_t)Z * r) * C;
+    if (vec4) reinterpret_cast<float4 *>(g + off)[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    else g[off + k] = 0.0f;
+  }
+}
+
 }  // namespace sg
 
 using namespace sg;
@@ -221,6 +249,18 @@ extern "C" int sg_grid_scatter(const float *ori, const float *dir, const float *
     case 16: grid_scatter_kernel<16><<<g, 256, 0, stream>>>(p); break;
     default: return SG_ERR_UNSUPPORTED;
   }
+  SG_LAUNCH_CHECK();
+  return SG_OK;
+}
+
+extern "C" int sg_zero_near_nodes(const SgTree *tree, float *grid, int C, sg_stream_t stream) {
+  if (!tree || !tree->brick_node || !grid) return SG_ERR_INVALID_ARG;
+  if (tree->B <= 0 || tree->Dt <= 0 || tree->rate <= 0 || tree->Db != tree->Dt * tree->rate || C <= 0)
+    return SG_ERR_INVALID_ARG;
+  const long vt = (long)tree->Dt * tree->Dt * tree->Dt;
+  if (vt > INT_MAX || tree->B > 65535) return SG_ERR_UNSUPPORTED;
+  const int vec4 = ((tree->rate * C) % 4 == 0 && ((uintptr_t)grid) % 16 == 0) ? 1 : 0;
+  zero_near_nodes_kernel<<<dim3((unsigned)vt, tree->B), 256, 0, stream>>>(*tree, grid, C, vec4);
   SG_LAUNCH_CHECK();
   return SG_OK;
 }

@@ -217,9 +217,11 @@ def test_train_step_graph_replay(work):
     torch.cuda.synchronize()
     ref = [t.clone() for t in (bp.out_rgb, bp.out_depth, bp.tsdf, bp.grad_feat, bp.grad_tsdf)]
     g = bp.capture()
+    # stale values where the step clears (the grids are 0 elsewhere by contract)
+    near = torch.as_tensor(_near_node_voxels(bp.grad_bricks.cpu().numpy(), bp.B, bp.Dt, RATE), device="cuda")
     for _ in range(2):
         bp.out_rgb.zero_()
-        bp.grad_feat.fill_(7.0)
+        bp.grad_feat.masked_fill_(near[..., None], 7.0)
         g.replay()
         torch.cuda.synchronize()
         assert torch.equal(bp.out_rgb, ref[0]) and torch.equal(bp.out_depth, ref[1])
@@ -246,3 +248,62 @@ def test_fused_train_step_matches_unfused(work):
     assert abs(bp.out_loss.sum().item() - mse) <= 1e-5 * max(mse, 1e-12) + 1e-9
     m = ref[4].abs().max().item()
     assert m > 0 and (bp.grad_feat - ref[4]).abs().max().item() <= 1e-5 * m
+
+
+def _near_node_voxels(brick_node, B, Dt, rate):
+    """Voxel mask [B, Db, Db, Db] of the bricks that are nodes or border one."""
+    node = (brick_node.reshape(B, Dt, Dt, Dt) >= 0)
+    pad = np.pad(node, ((0, 0), (1, 1), (1, 1), (1, 1)))
+    near = np.zeros_like(node)
+    for dx in range(3):
+        for dy in range(3):
+            for dz in range(3):
+                near |= pad[:, dx:dx + Dt, dy:dy + Dt, dz:dz + Dt]
+    return near.repeat(rate, 1).repeat(rate, 2).repeat(rate, 3)
+
+
+@pytest.mark.parametrize("C,aligned", [(16, True), (1, True), (3, False)])
+def test_zero_near_nodes_exact(work, C, aligned):
+    """sg_zero_near_nodes clears exactly the bricks that are nodes or border
+    one (16-byte stores, and the scalar path for an unaligned grid)."""
+    from sailor_gb300 import _native as N
+    bp = _pipeline(work)
+    B, Dt = bp.B, bp.Dt
+    n = B * D ** 3 * C
+    buf = torch.ones(n + 1, device="cuda")
+    grid = buf[:n] if aligned else buf[1:]
+    N.check(N.lib.sg_zero_near_nodes(_byref(bp.tree), N.ptr(grid), C, N.stream()), "zero_near_nodes")
+    torch.cuda.synchronize()
+    near = _near_node_voxels(bp.brick_node.cpu().numpy(), B, Dt, RATE)
+    assert 0 < near.mean() < 1
+    expect = np.repeat(np.where(near, 0.0, 1.0).astype(np.float32)[..., None], C, -1).reshape(-1)
+    assert np.array_equal(grid.cpu().numpy(), expect)
+
+
+def _byref(x):
+    return C.byref(x)
+
+
+def test_train_step_clears_previous_gradients(work):
+    """Two training steps on different scenes (the second's depths scaled, so
+    its tree differs): the second step's gradients equal a fresh pipeline's,
+    although the first left gradients outside the second's node bricks."""
+    frames2 = [dict(fr, depth=[(d * 0.9).astype(np.float32) for d in fr["depth"]]) for fr in work["frames"]]
+    bp = _pipeline(work)
+    bp.train_step()
+    torch.cuda.synchronize()
+    g1 = bp.grad_feat.clone()
+    nodes1 = bp.brick_node.clone()
+    bp.load_views(frames2, work["vol_bbox"], work["voxel_size"], work["trunc_weight"])
+    bp.train_step()
+    torch.cuda.synchronize()
+    assert not torch.equal(nodes1, bp.brick_node)
+    near2 = torch.as_tensor(_near_node_voxels(bp.brick_node.cpu().numpy(), bp.B, bp.Dt, RATE), device="cuda")
+    assert (g1.abs().sum(-1) * (~near2)).max().item() > 0  # stale values a dense-only scheme would keep
+    fresh = _pipeline(work)
+    fresh.load_views(frames2, work["vol_bbox"], work["voxel_size"], work["trunc_weight"])
+    fresh.train_step()
+    torch.cuda.synchronize()
+    m = fresh.grad_feat.abs().max().item()
+    assert m > 0 and (bp.grad_feat - fresh.grad_feat).abs().max().item() <= 1e-5 * m
+    assert torch.equal(bp.out_rgb, fresh.out_rgb)
