@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="small configuration (256^3, 512^2) for profiling")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
-    ap.add_argument("--workload", default="batch", choices=["batch", "plain"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "plain", "project"])
     ap.add_argument("--unfused", action="store_true",
                     help="render with four kernels (sample+sort, two field gathers, composite) instead of one")
     return ap.parse_args()
@@ -608,7 +608,169 @@ def main():
         return run_reference(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "project":
+        return run_project(args)
     return run_plain(args)
+
+
+# --------------------------------------------------------------------------
+# projection into the source views + 2D feature gather (SRONet's step after
+# sampling): the fused sg_project_gather against the reference's torch
+# sequence on the same GPU
+# --------------------------------------------------------------------------
+PROJ = dict(views=4, res=512, C_geo=32, C_rgb=32, target=512, S=64, seed=13)
+
+
+def torch_proj_persp(points, K, R, T, p_depths, n_views, depth_thres=0.01, min_d=0.1, max_d=4.0, res=512):
+    """The reference's proj_persp (utils_render/utils_render.py:380-414) as the
+    torch calls it makes, for timing."""
+    if p_depths is not None:
+        invalid_d = (p_depths < min_d) | (p_depths > max_d)
+        points = points[:, None].repeat(1, n_views, 1, 1).view(-1, *points.shape[-2:])
+    pts = R @ points + T
+    ori_pts = pts.clone()
+    depth = pts[:, -1:, :].clone()
+    invalid = depth < depth_thres
+    depth_ = depth.clone()
+    depth_[invalid] = 1
+    if p_depths is not None:
+        invalid_d = invalid_d[:, None].repeat(1, n_views, 1, 1).view(-1, 1, invalid_d.shape[-1])
+        depth[invalid_d] = -2
+    pts /= depth_
+    pts_screen = (K @ pts)[:, :2, :]
+    grids = (pts_screen - res // 2) / (res // 2)
+    grids[invalid.repeat(1, 2, 1)] = -2
+    if p_depths is not None:
+        grids[invalid_d.repeat(1, 2, 1)] = -2
+    return ori_pts, grids, depth
+
+
+def torch_forward_sample_feature(feats_geo, depths, feats_rgb, rgbs_n, xy, z):
+    """BasicRenNet.forward_sample_feature (SRONet/BasicRenNet.py:245-259)."""
+    import torch
+    import torch.nn.functional as F
+    geo = F.grid_sample(feats_geo, xy, align_corners=True, mode="bilinear")[..., 0].permute(0, 2, 1).contiguous()
+    sd = F.grid_sample(depths, xy, align_corners=True, mode="bilinear")[..., 0]
+    psdf = (torch.clamp(z - sd, -0.01, 0.01) * (1.0 / 0.01)).permute(0, 2, 1).contiguous()
+    rgbf = F.grid_sample(feats_rgb, xy, align_corners=True, mode="bilinear")[..., 0].permute(0, 2, 1).contiguous()
+    rgbs = F.grid_sample(rgbs_n, xy, align_corners=True, mode="bilinear")[..., 0].permute(0, 2, 1).contiguous()
+    return geo, rgbf, psdf, rgbs
+
+
+def run_project(args):
+    import torch
+
+    from oracle import oracle as orc
+    from sailor_gb300 import synthetic as syn
+    from sailor_gb300 import views
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    cfg = dict(PROJ)
+    if args.small:
+        cfg.update(target=128)
+    V, H, S = cfg["views"], cfg["res"], cfg["S"]
+    rng = np.random.default_rng(cfg["seed"])
+    cams = syn.ring_cameras(V)
+    K = np.repeat(syn.intrinsics(H)[None], V, 0).astype(np.float32)
+    R = np.stack([c[0] for c in cams]).astype(np.float32)
+    T = np.stack([c[1] for c in cams]).astype(np.float32).reshape(V, 3, 1)
+    ori, dirs = syn.target_rays(seed=cfg["seed"], res=cfg["target"])
+    Nr = ori.shape[1]
+    z = np.sort(rng.uniform(1.5, 3.5, (Nr, S)), -1).astype(np.float32)
+    pts_rs = (ori[0, :, None, :] + dirs[0, :, None, :] * z[..., None]).astype(np.float32)  # [Nr, S, 3]
+    Np = Nr * S
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+    points = t(pts_rs.reshape(1, Np, 3)).permute(0, 2, 1)  # [1, 3, N], a view as SRONet makes it
+    p_depths = t(z.reshape(1, 1, Np))
+    Kt, Rt, Tt = t(K), t(R), t(T)
+    maps = [torch.randn((V, cfg["C_geo"], H, H), device=dev), 1.0 + 2.0 * torch.rand((V, 1, H, H), device=dev),
+            torch.randn((V, cfg["C_rgb"], H, H), device=dev), torch.rand((V, 3, H, H), device=dev)]
+    maps_cl = [m.contiguous(memory_format=torch.channels_last) for m in maps]
+    ch = sum(m.shape[1] for m in maps)
+
+    def ours(mp):
+        return views.project_sample_features(points, Kt, Rt, Tt, p_depths, V, *mp, res=H)
+
+    # the torch sequence in chunks of points, as SRONet renders in ray chunks
+    # (cuDNN's grid_sample takes at most 2^31 output elements); chunk
+    # outputs are consumed as they come, not concatenated
+    chunk = 1 << 21
+
+    def plain():
+        outs = []
+        for c0 in range(0, Np, chunk):
+            sl = slice(c0, min(c0 + chunk, Np))
+            _, grids, depth = torch_proj_persp(points[:, :, sl], Kt, Rt, Tt, p_depths[:, :, sl], V, res=H)
+            xy = grids.permute(0, 2, 1).reshape(V, -1, 1, 2)
+            outs.append(torch_forward_sample_feature(*maps, xy, depth))
+        return outs
+
+    def timed(fn, steps, warm):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    # parity of the timed paths on the first chunk (features within 1e-5 of
+    # torch's fp32 grid_sample)
+    a, b_ = ours(maps_cl), plain()[0]
+    c1 = min(chunk, Np)
+    err = max((a[1][:, :c1] - b_[0]).abs().max().item(), (a[2][:, :c1] - b_[1]).abs().max().item(),
+              (a[4][:, :c1] - b_[3]).abs().max().item())
+    del a, b_
+    warm = max(args.warmup, 3)
+    import tempfile
+    clk = ClockSampler(os.path.join(tempfile.gettempdir(), "sg_clocks_project.csv"))
+    with clk:
+        ms = timed(lambda: ours(maps_cl), args.steps, warm)
+    ms_nchw = timed(lambda: ours(maps), args.steps, warm)
+    ms_plain = timed(plain, args.steps, warm)
+    vp = V * Np
+    value = vp / (ms / 1000.0)
+    map_bytes = sum(m.numel() for m in maps) * 4
+    ab = vp * (4 * ch + 4) + Np * 16 + map_bytes  # outputs + point/p_depth reads + maps once
+    pk, pk_kind = peaks()
+    achieved = ab / (ms / 1000.0) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath) and not args.small:
+        traffic = json.load(open(tpath)).get("project_gather")
+    out = dict(metric="view-points/s projected and gathered (proj_persp + 4x grid_sample + t_psdf)", value=value,
+               unit="view-points/s", n_gpus=1, steps=args.steps, warmup=warm, ms_per_step=ms, higher_is_better=True,
+               scaling="weak", vs_baseline=None, dtype="f32", data="synthetic (ring cameras, N(0,1) feature maps)",
+               config=dict(workload=f"{V} views of {H}^2 maps ({cfg['C_geo']}+1+{cfg['C_rgb']}+3 ch), "
+                                    f"{cfg['target']}^2 rays x {S} samples ({Np} points)",
+                           maps="channels-last", l2=f"maps {map_bytes / 1e6:.0f} MB, outputs "
+                                                    f"{vp * (4 * ch + 4) / 1e9:.1f} GB per step >> L2"),
+               ms_nchw_maps=ms_nchw, plain_torch=dict(ms_per_step=ms_plain, value=vp / (ms_plain / 1000.0),
+                                                      ratio=ms_plain / ms),
+               max_abs_err_vs_torch=err,
+               roofline=dict(bound="hbm", kernel="project_gather", achieved=achieved, peak=pk["hbm_gbs"],
+                             unit="GB/s", frac=achieved / pk["hbm_gbs"], traffic=traffic, peak_kind=pk_kind,
+                             algorithmic_bytes=ab),
+               gpu_launches=args.steps, clocks=clk.summary())
+    if not args.no_cpu_baseline:
+        n_s = 8192
+        sel = rng.choice(Np, n_s, replace=False)
+        p_s = pts_rs.reshape(Np, 3)[sel].T[None]
+        pd_s = z.reshape(Np)[sel][None, None]
+        mcpu = [m.cpu().numpy() for m in maps]
+        t0 = time.perf_counter()
+        _, g_s, _ = orc.proj_persp(p_s, K, R, T, pd_s, V, res=H)
+        gg = np.transpose(g_s, (0, 2, 1))
+        for m in mcpu:
+            orc.grid_sample(m, gg)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = dict(value=V * n_s / dt, unit="view-points/s", cores=1, kind="port",
+                                   sample=f"oracle float64 numpy proj_persp + 4 grid_sample on {n_s} of {Np} points")
+    print(json.dumps(out), flush=True)
 
 
 def run_plain(args):

@@ -286,6 +286,82 @@ int sg_grid_scatter(const float *ori, const float *dir, const float *z, int B,
  * reference (its training step clears dense gradients with torch). */
 int sg_zero_near_nodes(const SgTree *tree, float *grid, int C, sg_stream_t stream);
 
+/* ------------------------------------------------------------------------ */
+/* Projection into the source views and 2D feature gather                   */
+/* ------------------------------------------------------------------------ */
+
+/* Projection of sampled points into every view.  Replaces
+ * MultiLayerOctree::project_sampled_xyz (sampling_kernel.cu:1333-1381) and
+ * its kernel project_xyz (:55-159).  ray_ori/ray_dir [B,N,3], sampled_z /
+ * sampled_idx [B,N,S] (node ids of `tree`, -1: none), K [B,V,3,3], RT
+ * [B,V,3,4] -> proj_xy [B,V,N,S,P,2] normalised to [-1,1] as
+ * (pixel - size/2) / (size/2), proj_z [B,V,N,S,P] camera z, with P = 9
+ * (the point, then its node's eight corners, x outermost) when
+ * record_corners, else P = 1.  Items whose sample has node id -1 are -1
+ * (the reference's fill); with record_corners, corners of an id that is not
+ * a node of `tree` are -1 (the reference would read an arbitrary node).
+ * Point and projection use the reference's float operations; the
+ * normalisation, which the reference evaluates in double precision, equals
+ * it exactly when size/2 is a power of two and otherwise except in rare
+ * near-tie cases (then by 1 ulp).  tree may be NULL without record_corners. */
+int sg_project_sampled_xyz(const SgTree *tree, const float *ray_ori, const float *ray_dir,
+                           const float *sampled_z, const int *sampled_idx, const float *K,
+                           const float *RT, int B, int num_views, int N, int S, int ori_w,
+                           int ori_h, int record_corners, float *proj_xy, float *proj_z,
+                           sg_stream_t stream);
+
+/* A [n_images, C, H, W] feature map read through element strides
+ * {image, channel, y, x} (NCHW or channels-last), and its gathered output
+ * out [n_images, num_points, C] (channel-last, the layout F.grid_sample's
+ * result has after .permute(0,2,1).contiguous()). */
+typedef struct SgFeatureMap {
+  const float *data;
+  long long stride[4];
+  int C, H, W;
+  float *out;
+} SgFeatureMap;
+
+/* proj_persp + F.grid_sample of up to four maps + clamped depth difference.
+ * Replaces utils_render.proj_persp (utils_render/utils_render.py:380-414)
+ * and SRONet's forward_sample_feature (SRONet/BasicRenNet.py:245-259).
+ * points [batch, 3, num_points] through element strides {batch, axis,
+ * point}; view image i uses point batch i / points_div (points_div = V when
+ * the points are shared by a frame's V views, as proj_persp repeats them).
+ * K, R [n_images,3,3], T [n_images,3].  Per (image, point):
+ *   pts = R p + T (ori_pts [n_images,3,N]), depth = pts.z; invalid = depth <
+ *   depth_thres (divided by 1 instead); with p_depths ([batch, 1, N] through
+ *   strides {batch, point}) a point whose p_depth is outside [min_d, max_d]
+ *   gets depth -2; grids [n_images,2,N] = ((K pts/depth).xy - half_res) /
+ *   half_res, -2 for invalid points (either test).
+ * Each map is then sampled bilinearly at grids (align_corners=True, zero
+ * padding), and with psdf_map >= 0, psdf [n_images, N] = clamp(depth -
+ * sample of that map's channel 0, -psdf_clip, psdf_clip) * psdf_scale.
+ * ori_pts, grids, depth may be NULL.  With grids_in [n_images, N, 2] (the
+ * grid F.grid_sample takes) the projection is skipped: the maps are sampled
+ * at grids_in and psdf uses depth_in [n_images, N] (points, K, R, T unused).
+ * Float arithmetic of one thread per (image, point); torch's matrix
+ * products may sum in another order, so results agree with the reference's
+ * to float rounding. */
+typedef struct SgProjGather {
+  const float *grids_in, *depth_in;
+  const float *points;
+  long long points_stride[3];
+  int points_div;
+  const float *p_depths;
+  long long p_depths_stride[2];
+  const float *K, *R, *T;
+  int n_images, num_points;
+  float depth_thres, min_d, max_d, half_res;
+  float *ori_pts, *grids, *depth;
+  int n_maps;
+  SgFeatureMap maps[4];
+  int psdf_map;
+  float psdf_clip, psdf_scale;
+  float *psdf;
+} SgProjGather;
+
+int sg_project_gather(const SgProjGather *args, sg_stream_t stream);
+
 /* Node-corner trilinear aggregation.  Replaces
  * MultiLayerOctree::trilinear_aggregate_features(_backward)
  * (sampling_kernel.cu:162-327, 1384-1462).  ori/dir [B,N,3],

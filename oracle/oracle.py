@@ -56,6 +56,8 @@ def lib():
         L.orc_grid_gather.argtypes = [l, i, i, _f32p, _vp, _f32p, _f32p, _f32p, _f64p]
         L.orc_grid_scatter.argtypes = [l, i, i, i, _f32p, _vp, _f32p, _f32p, _f32p, _f64p]
         L.orc_node_geometry.argtypes = [f, i, _f32p, _i32p, _f32p, _f32p]
+        L.orc_project_xyz.argtypes = [i, i, i, i, _f32p, _f32p, _f32p, _i32p, _f32p, _f32p, i, i, _vp, i,
+                                      _f32p, _f32p]
         L.orc_num_threads.restype = i
         L.orc_set_threads.argtypes = [i]
         _lib = L
@@ -345,6 +347,100 @@ def grid_scatter(pts, gout, B, D, bbox_min, voxel_size, batch=None):
                            _f(bbox_min).reshape(-1), _f(voxel_size).reshape(-1), gout.reshape(-1),
                            gg.reshape(-1))
     return gg
+
+
+# --------------------------------------------------------------------------
+# projection into the views (sampling_kernel.cu:55-159, utils_render.py:380)
+# and the bilinear 2D feature gather (F.grid_sample, BasicRenNet.py:245-259)
+# --------------------------------------------------------------------------
+def node_corner_table(tree, voxel_size, vol_bbox):
+    """[n_nodes, 8, 3] corners of every node id of an oracle tree, in the
+    order of OcTree::calculate_xyz_corners (octree.h:109-129, x outermost):
+    the node centre plus or minus half its edge, in float32."""
+    n = tree["base_top"] + tree["ntop"]
+    ids = np.concatenate([np.arange(tree["base_bot"], tree["base_bot"] + tree["nbot"]),
+                          np.arange(tree["base_top"], tree["base_top"] + tree["ntop"])])
+    keys = node_keys(tree, ids)
+    out = np.full((n, 8, 3), -1.0, np.float32)  # ids that are no node stay -1
+    vs = np.asarray(voxel_size, np.float32).reshape(-1)
+    bb = np.asarray(vol_bbox, np.float32).reshape(-1, 3, 2)
+    rate = tree["Db"] // tree["Dt"]
+    for g, key in zip(ids, keys):
+        lvl, b, x, y, z = (int(v) for v in key)
+        c, nvs = node_geometry(vs[b], rate if lvl == 1 else 1, bb[b, :, 0].copy(), np.array([x, y, z], np.int32))
+        h = np.float32(nvs) / np.float32(2.0)
+        for i in range(8):
+            sgn = np.array([1 if i & 4 else -1, 1 if i & 2 else -1, 1 if i & 1 else -1], np.float32)
+            out[g, i] = c + sgn * h
+    return out
+
+
+def project_xyz(ori, dirs, z, idx, K, RT, ori_w, ori_h, corners=None):
+    """ori/dirs [B,N,3], z/idx [B,N,S], K [B,V,3,3], RT [B,V,3,4] ->
+    (proj_xy [B,V,N,S,P,2], proj_z [B,V,N,S,P]) with P = 9 when a node
+    corner table is given (node_corner_table), else 1."""
+    z = _f(z)
+    B, N, S = z.shape
+    V = np.asarray(K).shape[1]
+    per = 9 if corners is not None else 1
+    xy = np.empty((B, V, N, S, per, 2), np.float32)
+    pz = np.empty((B, V, N, S, per), np.float32)
+    ct = None if corners is None else np.ascontiguousarray(corners, np.float32)
+    lib().orc_project_xyz(B, V, N, S, _f(ori).reshape(-1), _f(dirs).reshape(-1), z.reshape(-1),
+                          _i(idx).reshape(-1), _f(K).reshape(-1), _f(RT).reshape(-1), int(ori_w), int(ori_h),
+                          None if ct is None else ct.ctypes.data, 0 if ct is None else ct.shape[0],
+                          xy.reshape(-1), pz.reshape(-1))
+    return xy, pz
+
+
+def proj_persp(points, K, R, T, p_depths, n_views, depth_thres=0.01, min_d=0.1, max_d=4.0, res=512):
+    """float64 restatement of utils_render.proj_persp (utils_render.py:380-414):
+    points [B', 3, N]; K, R [n, 3, 3]; T [n, 3, 1] -> (ori_pts, grids, depth)."""
+    pts = np.asarray(points, np.float64)
+    K, R, T = (np.asarray(a, np.float64) for a in (K, R, T))
+    n = K.shape[0]
+    if p_depths is not None:
+        pd = np.asarray(p_depths, np.float64)
+        invalid_d = (pd < min_d) | (pd > max_d)                      # [B', 1, N]
+        pts = np.repeat(pts[:, None], n_views, 1).reshape(-1, *pts.shape[-2:])
+        invalid_d = np.repeat(invalid_d[:, None], n_views, 1).reshape(-1, 1, invalid_d.shape[-1])
+    elif pts.shape[0] != n:
+        pts = np.broadcast_to(pts, (n,) + pts.shape[1:])
+    p = R @ pts + T
+    ori = p.copy()
+    depth = p[:, 2:3].copy()
+    invalid = depth < depth_thres
+    d_ = np.where(invalid, 1.0, depth)
+    if p_depths is not None:
+        depth[invalid_d] = -2
+    scr = (K @ (p / d_))[:, :2]
+    half = int(res) // 2
+    grids = (scr - half) / half
+    grids[np.repeat(invalid, 2, 1)] = -2
+    if p_depths is not None:
+        grids[np.repeat(invalid_d, 2, 1)] = -2
+    return ori, grids, depth
+
+
+def grid_sample(img, grid):
+    """float64 F.grid_sample(img [n, C, H, W], grid [n, N, 2], bilinear,
+    align_corners=True, zero padding) -> [n, N, C]."""
+    img = np.asarray(img, np.float64)
+    g = np.asarray(grid, np.float64)
+    n, C_, H, W = img.shape
+    ix = (g[..., 0] + 1) / 2 * (W - 1)
+    iy = (g[..., 1] + 1) / 2 * (H - 1)
+    x0, y0 = np.floor(ix), np.floor(iy)
+    out = np.zeros(g.shape[:2] + (C_,))
+    bidx = np.arange(n)[:, None]
+    for cx, cy, w in ((x0, y0, (x0 + 1 - ix) * (y0 + 1 - iy)), (x0 + 1, y0, (ix - x0) * (y0 + 1 - iy)),
+                      (x0, y0 + 1, (x0 + 1 - ix) * (iy - y0)), (x0 + 1, y0 + 1, (ix - x0) * (iy - y0))):
+        ok = (cx >= 0) & (cx <= W - 1) & (cy >= 0) & (cy <= H - 1)
+        xi = np.where(ok, cx, 0).astype(np.int64)
+        yi = np.where(ok, cy, 0).astype(np.int64)
+        v = img[bidx, :, yi, xi]                                     # [n, N, C]
+        out += np.where(ok, w, 0.0)[..., None] * v
+    return out
 
 
 # --------------------------------------------------------------------------

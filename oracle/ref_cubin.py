@@ -14,6 +14,7 @@ as device memory:
   sort_samplings          sampling_kernel.cu:1308-1329 (torch.sort)
   volume_rendering_*      volume_rendering.cu:525-787
   rays_calculating        sampling_kernel.cu:674-731
+  project_sampled_xyz     sampling_kernel.cu:1333-1381
 
 It is used only to generate golden vectors (tests/golden/make_golden.py) and
 by optional GPU tests that skip when the cubins are absent.
@@ -51,6 +52,7 @@ _NAMES = {
     "vr_occ": ("volume_rendering", "volume_rendering_occ_kernelIfE"),
     "rays_inverse": ("sampling_kernel", "14inverse_mat3x3IfE"),
     "rays": ("sampling_kernel", "23rays_calculating_kernelIfE"),
+    "project": ("sampling_kernel", "11project_xyz"),
 }
 
 
@@ -232,7 +234,8 @@ class Octree:
                     depth=col(4, np.int32)[:, 0], gindex=col(8, np.int32)[:, 0],
                     nleaves=col(16, np.int32)[:, 0], batch=col(28, np.int32)[:, 0],
                     voxel_size=col(32, np.float32)[:, 0], xyz=col(36, np.int32, 3),
-                    centre=col(48, np.float32, 3), father=col(840, np.int32)[:, 0],
+                    centre=col(48, np.float32, 3), corners=col(72, np.float32, 24).reshape(-1, 8, 3),
+                    father=col(840, np.int32)[:, 0],
                     children=col(844, np.int32, 64))
 
     def voxel_traversal(self, ori, dirs, W, th_early_stop=-1, is_training=False, opt_num=-1):
@@ -273,6 +276,24 @@ class Octree:
                                      i32(self.max_hits), i32(start_level), i32(2), self.voxel_size])
         torch.cuda.synchronize()
         return si, sd
+
+
+def project_sampled_xyz(tree, ori, dirs, z, idx, K, RT, ori_w, ori_h, record_corners):
+    """MultiLayerOctree::project_sampled_xyz (sampling_kernel.cu:1333-1381):
+    -1-filled outputs, then project_xyz (:55-159) over B*V*N*S items."""
+    d = driver()
+    zt, it = _dev(z, torch.float32), _dev(idx, torch.int32)
+    B, N, S = zt.shape
+    V = np.asarray(K).shape[1]
+    shape = (B, V, N, S, 9) if record_corners else (B, V, N, S)
+    xy = torch.full(shape + (2,), -1.0, device="cuda")
+    pz = torch.full(shape + (1,), -1.0, device="cuda")
+    d.launch("project", B * V * N * S, [tree.nodes, _dev(ori, torch.float32), _dev(dirs, torch.float32),
+                                        _dev(K, torch.float32), _dev(RT, torch.float32), it, zt, xy, pz,
+                                        i32(ori_w), i32(ori_h), i32(B), i32(N), i32(S), i32(V),
+                                        cb(bool(record_corners))])
+    torch.cuda.synchronize()
+    return xy, pz
 
 
 def sort_samplings(z):

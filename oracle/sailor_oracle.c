@@ -958,3 +958,62 @@ void orc_grid_scatter(long P, int C, int D, int B, const float *pts,
     }
   }
 }
+
+/* ------------------------------------------------------------------------ */
+/* Projection of sampled points into the views: project_xyz,                 */
+/* sampling_kernel.cu:55-159 (host MultiLayerOctree::project_sampled_xyz     */
+/* :1333-1381).  Items (b, v, r, s), s fastest.  The sample point is         */
+/* ori + dir * z (:89-91, one fma as nvcc contracts it); camera point and    */
+/* pixel use the operand order of integrate_cuda's projection (the same      */
+/* expressions); pixel / pixel_z in float; the [-1, 1] normalisation in      */
+/* double, as the reference's ori_w / 2.0 makes it (:113-114).  corners:     */
+/* [n_nodes][8][3] corner table indexed by node id (NULL: record_corners     */
+/* off); items with node id -1 keep the -1 fill, as do the corners of an     */
+/* id outside the table.                                                     */
+/* ------------------------------------------------------------------------ */
+static void orc_proj_one(const float *K, const float *P, float x, float y, float z, int w, int h,
+                         float *gx, float *gy, float *cz) {
+  float cx = fmaf(P[2], z, fmaf(P[0], x, P[1] * y)) + P[3];
+  float cy = fmaf(P[6], z, fmaf(P[4], x, P[5] * y)) + P[7];
+  float c3 = fmaf(P[10], z, fmaf(P[8], x, P[9] * y)) + P[11];
+  float ux = fmaf(K[2], c3, fmaf(K[0], cx, K[1] * cy));
+  float uy = fmaf(K[5], c3, fmaf(K[3], cx, K[4] * cy));
+  float uz = fmaf(K[8], c3, fmaf(K[6], cx, K[7] * cy));
+  ux = ux / uz;
+  uy = uy / uz;
+  *gx = (float)(((double)ux - w / 2.0) / (w / 2.0));
+  *gy = (float)(((double)uy - h / 2.0) / (h / 2.0));
+  *cz = c3;
+}
+
+void orc_project_xyz(int B, int V, int N, int S, const float *ori, const float *dir, const float *z,
+                     const int *idx, const float *K, const float *RT, int w, int h, const float *corners,
+                     int n_nodes, float *xy, float *pz) {
+  const int per = corners ? 9 : 1;
+  long total = (long)B * V * N * S;
+#pragma omp parallel for schedule(static)
+  for (long k = 0; k < total; k++) {
+    long rs = k % ((long)N * S), bv = k / ((long)N * S);
+    int b = (int)(bv / V);
+    long si = (long)b * N * S + rs;
+    long r = rs / S;
+    float *oxy = xy + k * 2 * per, *oz = pz + k * per;
+    for (int i = 0; i < per; i++) {
+      oxy[2 * i] = -1.0f;
+      oxy[2 * i + 1] = -1.0f;
+      oz[i] = -1.0f;
+    }
+    int id = idx[si];
+    if (id == -1) continue;
+    const float *o = ori + ((long)b * N + r) * 3, *d = dir + ((long)b * N + r) * 3;
+    float zs = z[si];
+    float px = fmaf(d[0], zs, o[0]), py = fmaf(d[1], zs, o[1]), p3 = fmaf(d[2], zs, o[2]);
+    const float *Kk = K + bv * 9, *P = RT + bv * 12;
+    orc_proj_one(Kk, P, px, py, p3, w, h, &oxy[0], &oxy[1], &oz[0]);
+    if (!corners || id < 0 || id >= n_nodes) continue;
+    for (int i = 0; i < 8; i++) {
+      const float *c = corners + ((size_t)id * 8 + i) * 3;
+      orc_proj_one(Kk, P, c[0], c[1], c[2], w, h, &oxy[2 * (i + 1)], &oxy[2 * (i + 1) + 1], &oz[i + 1]);
+    }
+  }
+}

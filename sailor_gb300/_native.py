@@ -24,6 +24,7 @@ EXPORTS = (
     "sg_grid_scatter", "sg_fuse_tsdf_views", "sg_intersect_segments", "sg_render_segments_fwd",
     "sg_render_segments_bwd", "sg_render_segments_train",
     "sg_camera_params", "sg_rays_from_cameras", "sg_segment_rays", "sg_zero_near_nodes",
+    "sg_project_sampled_xyz", "sg_project_gather",
 )
 
 
@@ -54,6 +55,22 @@ class SgRenderArgs(C.Structure):
                 ("feat", C.c_void_p), ("Df", C.c_int), ("C", C.c_int), ("feat_bbox", C.c_void_p),
                 ("feat_vs", C.c_void_p), ("head", C.c_void_p), ("t_thres", C.c_float)]
 
+
+
+class SgFeatureMap(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("stride", C.c_longlong * 4), ("C", C.c_int), ("H", C.c_int),
+                ("W", C.c_int), ("out", C.c_void_p)]
+
+
+class SgProjGather(C.Structure):
+    _fields_ = [("grids_in", C.c_void_p), ("depth_in", C.c_void_p),
+                ("points", C.c_void_p), ("points_stride", C.c_longlong * 3), ("points_div", C.c_int),
+                ("p_depths", C.c_void_p), ("p_depths_stride", C.c_longlong * 2), ("K", C.c_void_p),
+                ("R", C.c_void_p), ("T", C.c_void_p), ("n_images", C.c_int), ("num_points", C.c_int),
+                ("depth_thres", C.c_float), ("min_d", C.c_float), ("max_d", C.c_float), ("half_res", C.c_float),
+                ("ori_pts", C.c_void_p), ("grids", C.c_void_p), ("depth", C.c_void_p), ("n_maps", C.c_int),
+                ("maps", SgFeatureMap * 4), ("psdf_map", C.c_int), ("psdf_clip", C.c_float),
+                ("psdf_scale", C.c_float), ("psdf", C.c_void_p)]
 
 def _load():
     if not os.path.exists(LIB_PATH):
@@ -96,6 +113,8 @@ def _load():
     lib.sg_rays_from_cameras.argtypes = [p, p, p, i, i, i, i, p, p]
     lib.sg_segment_rays.argtypes = [C.POINTER(SgRaySegments), p, p, p]
     lib.sg_zero_near_nodes.argtypes = [C.POINTER(SgTree), p, i, p]
+    lib.sg_project_sampled_xyz.argtypes = [C.POINTER(SgTree), p, p, p, p, p, p, i, i, i, i, i, i, i, p, p, p]
+    lib.sg_project_gather.argtypes = [C.POINTER(SgProjGather), p]
     lib.sg_tune_set.argtypes = [i, i]
     lib.sg_tune_get.argtypes = [i]
     lib.sg_trilerp_nodes_fwd.argtypes = [C.POINTER(SgTree), p, p, p, p, p, i, i, i, p, p]

@@ -354,6 +354,33 @@ class MultiLayerOctree:
                                                Cf, N.ptr(gin), N.stream()), "trilerp_bwd")
             return gin
 
+    def project_sampled_xyz(self, ray_ori, ray_dir, sampled_z, sampled_idx, Ks, RTs, ori_w, ori_h, num_views,
+                            record_corners=True):
+        """Samples (and, with record_corners, their nodes' eight corners)
+        projected into every view: (proj_xy [B,V,N,S,9,2] or [B,V,N,S,2]
+        normalised to [-1, 1], proj_z [B,V,N,S,9,1] or [B,V,N,S,1] camera z);
+        -1 where the sample has no node (sampling_kernel.cu:1333-1381)."""
+        if record_corners and self._tree is None:
+            raise RuntimeError("project_sampled_xyz with record_corners before init_octree")
+        with torch.cuda.device(self.device):
+            z = _in(sampled_z, "sampled_z")
+            idx = _in(sampled_idx, "sampled_idx", torch.int32)
+            B, Nr, S = z.shape
+            V = int(num_views)
+            K = _in(Ks, "Ks")
+            RT = _in(RTs, "RTs")
+            if K.numel() != B * V * 9 or RT.numel() != B * V * 12:
+                raise RuntimeError(f"Ks / RTs must hold [{B}, {V}] cameras")
+            shape = (B, V, Nr, S, 9) if record_corners else (B, V, Nr, S)
+            xy = torch.empty(shape + (2,), device=self.device)
+            pz = torch.empty(shape + (1,), device=self.device)
+            N.check(N.lib.sg_project_sampled_xyz(C.byref(self._tree) if self._tree is not None else None,
+                                                 N.ptr(_in(ray_ori, "ray_ori")), N.ptr(_in(ray_dir, "ray_dir")),
+                                                 N.ptr(z), N.ptr(idx), N.ptr(K), N.ptr(RT), B, V, Nr, S,
+                                                 int(ori_w), int(ori_h), 1 if record_corners else 0, N.ptr(xy),
+                                                 N.ptr(pz), N.stream()), "project_sampled_xyz")
+            return xy, pz
+
     # -- node queries -----------------------------------------------------
     def get_nodes_tensor(self):
         with torch.cuda.device(self.device):

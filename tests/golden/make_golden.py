@@ -7,7 +7,8 @@ they lie; this script only loads the cubins):
     python tests/golden/make_golden.py --out <dir>
 
 It writes ``ref_chain_explicit.npz``, ``ref_chain_auto.npz``,
-``ref_composite.npz`` and ``ref_rays.npz`` (``--only rays``: that one alone).  Each holds the seeded inputs
+``ref_composite.npz``, ``ref_rays.npz`` and ``ref_project.npz`` (``--only rays`` or
+``--only project``: that one alone).  Each holds the seeded inputs
 and the reference outputs of fusion, coarse occupancy, the two-level tree
 (as canonical node keys, since the reference's node ids depend on atomic
 ordering), the voxel traversal, the coarse sampling, the sort, compositing
@@ -133,16 +134,64 @@ def rays(out_dir):
     print("rays done", flush=True)
 
 
+def project(out_dir):
+    """project_sampled_xyz on the reference's own tree and samples: 128 rays
+    of 16 samples (rays without samples included), four views; with node
+    corners at 640 x 480 (half sizes not powers of two) and without at
+    512 x 512.  Node ids are remapped to the referenced nodes, whose corner
+    table (read from the reference's node array) and canonical keys are
+    stored."""
+    Sp = 16
+    scene = syn.make_scene(seed=13, n_views=VIEWS, res=RES, n_prims=PRIMS, D=D, trunc=0.03)
+    ori, dirs = syn.target_rays(seed=13, res=TRES)
+    f = rc.integrate(scene["K"], scene["RT"], scene["colors"], scene["depths"], D, 1.0, 0.025,
+                     scene["trunc_weight"], 13.5, 13.5, vol_bbox=scene["vol_bbox"], voxel_size=scene["voxel_size"])
+    occ1, cnt1 = rc.build_multi_res_volumes(f["occ"], f["count"], RATE)
+    tree = rc.Octree(f["occ"], occ1, f["count"], cnt1, f["voxel_size"], f["vol_bbox"], RATE)
+    table = tree.node_table()
+    W = 4 * tree.Dt * (RATE ** 3 + 1)
+    idx, t0, t1, vl, _ = tree.voxel_traversal(ori, dirs, W)
+    si, sd = tree.sample_coarse(idx, t0, t1, np.full((1, ori.shape[1], Sp), 0.5, np.float32), vl, Sp)
+    si, sd = si.cpu().numpy(), sd.cpu().numpy()
+    rng = np.random.default_rng(17)
+    hit = np.where((si[0] >= 0).any(-1))[0]
+    miss = np.where(~(si[0] >= 0).any(-1))[0]
+    rays = np.sort(np.concatenate([rng.choice(hit, 120, replace=False), rng.choice(miss, 8, replace=False)]))
+    o, d = ori[:, rays], dirs[:, rays]
+    sub_i, sub_z = si[:, rays], sd[:, rays]
+    K = scene["K"].reshape(1, VIEWS, 3, 3)
+    RT = scene["RT"].reshape(1, VIEWS, 3, 4)
+    out = dict(ori=o, dirs=d, sampled_z=sub_z, K=K, RT=RT, vol_bbox=scene["vol_bbox"],
+               voxel_size=scene["voxel_size"], rate=np.array(RATE), Dt=np.array(tree.Dt))
+    used = np.unique(sub_i[sub_i >= 0])
+    remap = np.full(int(sub_i.max()) + 1 if used.size else 1, -1, np.int32)
+    remap[used] = np.arange(used.size, dtype=np.int32)
+    out["sampled_idx"] = np.where(sub_i >= 0, remap[np.maximum(sub_i, 0)], -1).astype(np.int32)
+    out["node_corners"] = table["corners"][used]
+    out["node_keys"] = canonical(table, tree.Dt, used)
+    for name, (w, h, rec) in (("corners", (640, 480, True)), ("point", (512, 512, False))):
+        xy, pz = rc.project_sampled_xyz(tree, o, d, sub_z, sub_i, K, RT, w, h, rec)
+        out[f"{name}_size"] = np.array([w, h], np.int32)
+        out[f"{name}_xy"] = xy.cpu().numpy()
+        out[f"{name}_z"] = pz.cpu().numpy()
+    np.savez_compressed(os.path.join(out_dir, "ref_project.npz"), **out)
+    print("project done: nodes", used.size, flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
-    ap.add_argument("--only", choices=["rays"])
+    ap.add_argument("--only", choices=["rays", "project"])
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
     assert rc.available(), "reference cubins or GPU missing"
+    if args.only == "project":
+        project(args.out)
+        return
     rays(args.out)
     if args.only == "rays":
         return
+    project(args.out)
     scene = syn.make_scene(seed=11, n_views=VIEWS, res=RES, n_prims=PRIMS, D=D, trunc=0.03)
     ori, dirs = syn.target_rays(seed=11, res=TRES)
     rng = np.random.default_rng(5)

@@ -73,3 +73,34 @@ def test_unsupported_tree_levels():
         o.init_octree([None] * 3, [0, 0, 0], [None] * 3, [0, 0, 0], None, None)
     with pytest.raises(NotImplementedError):
         o.octree_traversal()
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """Every ctypes mirror of a header struct has the C compiler's size and
+    field offsets (a probe compiled with gcc against the header)."""
+    import shutil
+    import subprocess
+    from sailor_gb300 import _native as N
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    structs = {name: getattr(N, name) for name in ("SgTree", "SgViews", "SgRaySegments", "SgRenderArgs",
+                                                   "SgFeatureMap", "SgProjGather")}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "sailor_gb300.h"', "int main(void) {"]
+    for name, cls in structs.items():
+        lines.append(f'  printf("{name} size %zu\\n", sizeof({name}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'  printf("{name} {fname} %zu\\n", offsetof({name}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "probe.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "probe"
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    subprocess.check_call(["gcc", "-I", os.path.join(root, "include"), str(src), "-o", str(exe)])
+    got = {}
+    for line in subprocess.check_output([str(exe)]).decode().splitlines():
+        name, field, val = line.split()
+        got[(name, field)] = int(val)
+    for name, cls in structs.items():
+        assert got[(name, "size")] == C.sizeof(cls), name
+        for fname, _ in cls._fields_:
+            assert got[(name, fname)] == getattr(cls, fname).offset, (name, fname)

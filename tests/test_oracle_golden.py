@@ -189,3 +189,56 @@ def test_rays_bit_exact_vs_reference():
     assert np.array_equal(out.view(np.uint32), g["rays"].view(np.uint32))
     assert np.array_equal(orc.inverse3x3(g["K"]).view(np.uint32), g["Kinv"].view(np.uint32))
     assert np.array_equal(orc.inverse3x3(g["R"]).view(np.uint32), g["Rinv"].view(np.uint32))
+
+
+def test_project_xyz_bit_exact_vs_reference(golden):
+    """Projection of sampled points (project_xyz, sampling_kernel.cu:55-159)
+    against the reference kernel's own output, with node corners at 640 x 480
+    (the double-precision normalisation with half sizes that are not powers
+    of two) and without at 512 x 512: bit for bit, -1 fills included.  The
+    corner table is the reference's node array (ids remapped)."""
+    g = golden("ref_project.npz")
+    for name, table in (("corners", g["node_corners"]), ("point", None)):
+        w, h = (int(v) for v in g[f"{name}_size"])
+        xy, pz = orc.project_xyz(g["ori"], g["dirs"], g["sampled_z"], g["sampled_idx"], g["K"], g["RT"], w, h,
+                                 corners=table)
+        assert np.array_equal(xy.reshape(-1).view(np.uint32), g[f"{name}_xy"].reshape(-1).view(np.uint32)), name
+        assert np.array_equal(pz.reshape(-1).view(np.uint32), g[f"{name}_z"].reshape(-1).view(np.uint32)), name
+    assert (g["sampled_idx"] == -1).any() and (g["corners_xy"] != -1).any()
+
+
+def test_node_corners_bit_exact_vs_reference(golden):
+    """The oracle's node geometry (centre plus or minus half the edge, the
+    corner order of octree.h:120-129) gives the reference's corner table bit
+    for bit, for top bricks and fine voxels."""
+    g = golden("ref_project.npz")
+    vs = float(np.asarray(g["voxel_size"]).reshape(-1)[0])
+    bmin = np.ascontiguousarray(g["vol_bbox"][0, :, 0])
+    rate = int(g["rate"])
+    levels = set()
+    for key, ref in zip(g["node_keys"], g["node_corners"]):
+        lvl, b, x, y, z = (int(v) for v in key)
+        levels.add(lvl)
+        c, nvs = orc.node_geometry(vs, rate if lvl == 1 else 1, bmin, np.array([x, y, z], np.int32))
+        hh = np.float32(nvs) / np.float32(2.0)
+        for i in range(8):
+            sgn = np.array([1 if i & 4 else -1, 1 if i & 2 else -1, 1 if i & 1 else -1], np.float32)
+            assert np.array_equal((c + sgn * hh).view(np.uint32), ref[i].view(np.uint32))
+    assert levels == {0, 1}
+
+
+def test_grid_sample_restatement_vs_torch():
+    """The oracle's float64 bilinear gather against torch's F.grid_sample
+    (CPU, float64, align_corners=True, zero padding), edges and the -2
+    invalid marker included."""
+    import torch
+    import torch.nn.functional as F
+    rng = np.random.default_rng(1)
+    img = rng.normal(size=(3, 5, 17, 23))
+    grid = rng.uniform(-1.2, 1.2, (3, 400, 2))
+    grid[:, :10] = -2.0
+    grid[:, 10:20, 0] = 1.0
+    grid[:, 20:30, 1] = -1.0
+    ref = F.grid_sample(torch.tensor(img), torch.tensor(grid)[:, :, None, :], align_corners=True,
+                        mode="bilinear")[..., 0].permute(0, 2, 1).numpy()
+    assert np.abs(orc.grid_sample(img, grid) - ref).max() <= 1e-12
