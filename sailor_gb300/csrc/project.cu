@@ -232,7 +232,7 @@ __device__ __forceinline__ float gather_map(const GatherMap &m, int img, long k,
 #pragma unroll
     for (int i = 0; i < 4; i++)
       if ((f.mask >> i) & 1) a = __fmaf_rn(__ldg(m.data + off[i] + (long)c * m.sc), f.w[i], a);
-    out[c] = a;
+    __stcs(out + c, a);
     if (c == 0) first = a;
   }
   return first;
@@ -311,7 +311,7 @@ __device__ __forceinline__ void gather_rows(const GatherMap &m, long k0, long to
         acc.z = __fmaf_rn(v.z, wt[i], acc.z);
         acc.w = __fmaf_rn(v.w, wt[i], acc.w);
       }
-      out[q] = acc;
+      __stcs(out + q, acc);  // streaming: the maps, not the output, should stay in L2
     }
   }
 }
