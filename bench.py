@@ -740,8 +740,8 @@ def run_project(args):
     achieved = ab / (ms / 1000.0) / 1e9
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath) and not args.small:
-        traffic = json.load(open(tpath)).get("project_gather")
+    if os.path.exists(tpath) and args.small:  # captured on the small case (reads do not scale with points)
+        traffic = json.load(open(tpath)).get("project_gather_small")
     out = dict(metric="view-points/s projected and gathered (proj_persp + 4x grid_sample + t_psdf)", value=value,
                unit="view-points/s", n_gpus=1, steps=args.steps, warmup=warm, ms_per_step=ms, higher_is_better=True,
                scaling="weak", vs_baseline=None, dtype="f32", data="synthetic (ring cameras, N(0,1) feature maps)",
