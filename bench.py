@@ -300,6 +300,7 @@ def padded_views(fr):
 def near_node_bricks(bp):
     """Top bricks sg_zero_near_nodes clears for the pipeline's last gradient
     pass: the nodes' bricks and their 26-neighbourhoods."""
+    import torch
     B, Dt = bp.B, bp.Dt
     m = (bp.grad_bricks >= 0).view(B, 1, Dt, Dt, Dt).float()
     return int(torch.nn.functional.max_pool3d(m, 3, stride=1, padding=1).sum().item())
