@@ -907,6 +907,9 @@ def run_plain(args):
             roofline=dict(bound="hbm", kernel=dom, achieved=achieved, peak=pk["hbm_gbs"], unit="GB/s",
                           frac=achieved / pk["hbm_gbs"], traffic=traffic, peak_kind=pk_kind,
                           algorithmic_bytes=ab[dom]),
+            rooflines={k: dict(achieved=ab[k] / (stages[k] / 1000.0) / 1e9,
+                               frac=ab[k] / (stages[k] / 1000.0) / 1e9 / pk["hbm_gbs"], algorithmic_bytes=ab[k])
+                       for k in ab if stages.get(k)},
             e2e=dict(value=e2e_value, unit=UNIT, h2d_bytes_per_step=h2d, d2h_bytes_per_step=d2h),
             gpu_launches=(9 if fused else 12) * args.steps,
             clocks=clk.summary(),
