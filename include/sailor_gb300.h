@@ -427,7 +427,12 @@ int sg_rays_from_cameras(const float *K, const float *R, const float *T, int B,
  * Frame b owns views [view_begin[b], view_begin[b+1]) (at most 32); view v
  * has K [3,3] and RT [3,4] at K + 9v / RT + 12v and an H x W image
  * (view_hw[2v], view_hw[2v+1]) starting at element view_offset[v] of the
- * packed depth / colour buffers. */
+ * packed depth / colour buffers.  Optional (both NULL or both set):
+ * depth_blocks, a float buffer of sum_v ceil(H/8) ceil(W/8) entries, and
+ * block_offset [n_views], where view v's 8 x 8 pixel blocks start; fusion
+ * then fills it with each block's deepest valid depth and answers its
+ * per-tile view culling from it instead of reading every pixel of the
+ * tile's footprint (the same results, faster). */
 typedef struct SgViews {
   int max_views;                /* most views of one frame (host value, <= 32) */
   const int *view_begin;        /* [B+1]           */
@@ -437,6 +442,8 @@ typedef struct SgViews {
   const float *RT;              /* [n_views, 3, 4] */
   const float *depth;           /* packed images   */
   const float *color;           /* packed images   */
+  const long long *block_offset;/* [n_views] or NULL */
+  float *depth_blocks;          /* scratch or NULL */
 } SgViews;
 
 /* Ray segments (device arrays): segment s (one target camera) owns rays

@@ -39,7 +39,7 @@ class SgTree(C.Structure):
 class SgViews(C.Structure):
     _fields_ = [("max_views", C.c_int), ("view_begin", C.c_void_p), ("view_hw", C.c_void_p),
                 ("view_offset", C.c_void_p), ("K", C.c_void_p), ("RT", C.c_void_p), ("depth", C.c_void_p),
-                ("color", C.c_void_p)]
+                ("color", C.c_void_p), ("block_offset", C.c_void_p), ("depth_blocks", C.c_void_p)]
 
 
 class SgRaySegments(C.Structure):

@@ -71,8 +71,14 @@ class BatchPipeline:
         self.RT = torch.zeros((V, 3, 4), **f32)
         self.depth = torch.zeros(self.view_pix, **f32)
         self.color = torch.zeros(self.view_pix, **f32)
+        # per-view maps of 8 x 8 depth blocks: fusion culls tiles from them
+        nblk = [((h + 7) // 8) * ((w + 7) // 8) for h, w in self.views_hw]
+        boffs = np.concatenate([[0], np.cumsum(nblk)]).astype(np.int64)
+        self.block_off = torch.tensor(boffs[:-1], dtype=torch.int64, device=dev)
+        self.depth_blocks = torch.empty(max(int(boffs[-1]), 1), **f32)
         self.views = N.SgViews(max(nv), N.ptr(self.view_begin), N.ptr(self.view_hw_t), N.ptr(self.view_off),
-                               N.ptr(self.K), N.ptr(self.RT), N.ptr(self.depth), N.ptr(self.color))
+                               N.ptr(self.K), N.ptr(self.RT), N.ptr(self.depth), N.ptr(self.color),
+                               N.ptr(self.block_off), N.ptr(self.depth_blocks))
         # volumes and tree
         Vol, Vt = B * D ** 3, B * self.Dt ** 3
         self.vol_bbox = torch.zeros((B, 3, 2), **f32)

@@ -145,13 +145,19 @@ struct FuseParams {
   // view table (NULL: every frame has N views of H x W at [b, k] of K / RT / images)
   const int *view_begin, *view_hw;
   const long long *view_off;
+  // per-view maps of 8 x 8 pixel blocks (deepest valid depth), or null
+  const long long *block_off;
+  float *blocks;
 };
+
+constexpr int kDepthBlock = 8;
 
 // Cameras and images of one frame's views, staged in shared memory.
 struct ViewSmem {
   float K[kMaxViews][9];
   float P[kMaxViews][12];
   long long off[kMaxViews];
+  long long boff[kMaxViews];  // block map offsets (with FuseParams::blocks)
   int hw[kMaxViews][2];
   int n;
 };
@@ -277,6 +283,7 @@ __device__ __forceinline__ void load_views(const FuseParams &p, int b, ViewSmem 
     else vw.P[v][k - 9] = p.RT[(size_t)(v0 + v) * 12 + (k - 9)];
   }
   for (int v = threadIdx.x; v < n; v += blockDim.x) {
+    if (p.blocks) vw.boff[v] = p.block_off[v0 + v];
     if (p.view_begin) {
       vw.off[v] = p.view_off[v0 + v];
       vw.hw[v][0] = p.view_hw[2 * (v0 + v)];
@@ -373,6 +380,31 @@ __global__ void __launch_bounds__(256) fuse_tsdf_kernel(FuseParams p) {
   if (lane_id() == 0 && cnt) atomicAdd(p.count + b, cnt);
 }
 
+// Deepest valid depth of every 8 x 8 pixel block of every view (block
+// (by, bx) of view v at blocks[block_off[v] + by * ceil(W / 8) + bx]):
+// -infinity when no pixel of the block is valid, +infinity when one is NaN
+// (integrate_view takes NaN as valid).  Grid (CTAs per view, frame, view
+// slot of the frame); thread per block.
+__global__ void __launch_bounds__(256) depth_blocks_kernel(FuseParams p) {
+  const int b = blockIdx.y;
+  const int v = __ldg(p.view_begin + b) + (int)blockIdx.z;
+  if (v >= __ldg(p.view_begin + b + 1)) return;
+  const int H = __ldg(p.view_hw + 2 * v), W = __ldg(p.view_hw + 2 * v + 1);
+  const int Wb = (W + kDepthBlock - 1) / kDepthBlock, Hb = (H + kDepthBlock - 1) / kDepthBlock;
+  const float *img = p.depth + __ldg(p.view_off + v);
+  float *out = p.blocks + __ldg(p.block_off + v);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < Hb * Wb; k += gridDim.x * blockDim.x) {
+    const int by = k / Wb, bx = k - by * Wb;
+    float m = -INFINITY;
+    for (int y = by * kDepthBlock; y < min(H, by * kDepthBlock + kDepthBlock); y++)
+      for (int x = bx * kDepthBlock; x < min(W, bx * kDepthBlock + kDepthBlock); x++) {
+        const float dv = __ldg(img + (size_t)y * W + x);
+        if (!(dv < 0.1f || dv > 4.0f)) m = dv != dv ? INFINITY : fmaxf(m, dv);
+      }
+    out[k] = m;
+  }
+}
+
 // Per-view culling of a voxel tile.  A view is left out of a whole tile
 // when every voxel of the tile would take one of integrate_view's early
 // returns for it, so the tile's results are unchanged:
@@ -395,6 +427,7 @@ struct CullSmem {
   int rect[kMaxViews][4];  // x0, x1, y0, y1 (clamped to the image)
   float czmin[kMaxViews];
   int state[kMaxViews];    // 0: keep, 1: leave out, 2: scan the rectangle
+  int bskip[kMaxViews];    // block-map verdict of a scanned view
   float wmax[2][8];
   int wnan[2][8];
   unsigned skip;
@@ -460,6 +493,37 @@ __device__ __forceinline__ void tile_cull(const FuseParams &p, const FuseFrame &
   __syncthreads();
   unsigned skip = 0u;
   const int w8 = tid >> 5;
+  if (p.blocks) {
+    // the block map: warp w8 takes views w8, w8 + 8, ..., its lanes the 8 x 8
+    // blocks covering the rectangle (a superset of its pixels, so the test
+    // stays conservative)
+    const int lane = tid & 31;
+    for (int k = w8; k < n; k += 8) {
+      if (cs.state[k] != 2) continue;
+      const int bx0 = cs.rect[k][0] / kDepthBlock, bx1 = cs.rect[k][1] / kDepthBlock;
+      const int by0 = cs.rect[k][2] / kDepthBlock, by1 = cs.rect[k][3] / kDepthBlock;
+      const int Wb = (vw.hw[k][1] + kDepthBlock - 1) / kDepthBlock;
+      const int nbx = bx1 - bx0 + 1, nb = nbx * (by1 - by0 + 1);
+      const float *bm = p.blocks + vw.boff[k];
+      float m = -INFINITY;
+      for (int i = lane; i < nb; i += 32) {
+        const int yy = i / nbx;
+        m = fmaxf(m, __ldg(bm + (size_t)(by0 + yy) * Wb + bx0 + (i - yy * nbx)));
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(SG_FULL, m, o));
+      if (lane == 0)
+        cs.bskip[k] = (m == -INFINITY || m - cs.czmin[k] < -f.trunc - kCullEps - 1.0e-5f * fabsf(m)) ? 1 : 0;
+    }
+    __syncthreads();
+    for (int k = 0; k < n; k++) {
+      const int state = cs.state[k];
+      if (state == 1 || (state == 2 && cs.bskip[k])) skip |= 1u << k;
+    }
+    if (tid == 0) cs.skip = skip;
+    __syncthreads();
+    return;
+  }
   int buf = 0;
   for (int k = 0; k < n; k++) {
     const int state = cs.state[k];
@@ -572,6 +636,7 @@ static int launch_fuse(const FuseParams &p, int B, sg_stream_t stream) {
     const int ty = ceil_div(Dy, kTileEdge), tz = ceil_div(Dz, kTileEdge);
     const long n_tiles = (long)ceil_div(Dx, kTileEdge) * ty * tz;
     const int gx = n_tiles < 65535L * 16 ? (int)n_tiles : 65535 * 16;
+    if (p.blocks) depth_blocks_kernel<<<dim3(16, B, kMaxViews), 256, 0, stream>>>(p);
     fuse_tsdf_tiled_kernel<<<dim3(gx, B), 256, 0, stream>>>(p, ty, tz, n_tiles);
     SG_LAUNCH_CHECK();
     return SG_OK;
@@ -613,8 +678,9 @@ extern "C" int sg_fuse_tsdf_views(const SgViews *views, int B, int D, const floa
   if (views->max_views > kMaxViews) return SG_ERR_UNSUPPORTED;
   if ((((uintptr_t)tsdf) | ((uintptr_t)weight) | ((uintptr_t)colorv) | ((uintptr_t)occ)) % 16 != 0)
     return SG_ERR_INVALID_ARG;
+  if ((views->block_offset == nullptr) != (views->depth_blocks == nullptr)) return SG_ERR_INVALID_ARG;
   FuseParams p{views->K, views->RT, views->color, views->depth, vol_bbox, voxel_size, tsdf, weight, colorv, occ,
                count, 0, 0, 0, D, D, D, obs_weight, trunc_weight, th_low, th_high, views->view_begin,
-               views->view_hw, views->view_offset};
+               views->view_hw, views->view_offset, views->block_offset, views->depth_blocks};
   return launch_fuse(p, B, stream);
 }
