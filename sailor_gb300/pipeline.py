@@ -82,21 +82,46 @@ class FramePipeline:
             ev.record()
             self.events.append((name, ev))
 
+    def _views(self, K, RT, colors, depths):
+        """SgViews of B frames of N views of H x W, packed as the [B, N, ...]
+        tensors already are, with 8 x 8 depth-block maps for the fusion's tile
+        culling (built once per shape and set of buffers)."""
+        B, Nv, H, W = depths.shape
+        for t_ in (K, RT, colors, depths):
+            if not (t_.is_contiguous() and t_.dtype == torch.float32):
+                raise RuntimeError("K, RT, colors and depths must be contiguous float32")
+        key = (B, Nv, H, W, K.data_ptr(), RT.data_ptr(), colors.data_ptr(), depths.data_ptr())
+        if getattr(self, "_vkey", None) != key:
+            if Nv > 32:
+                raise RuntimeError("at most 32 views per frame")
+            n = B * Nv
+            i32 = dict(dtype=torch.int32, device=self.dev)
+            nb = ((H + 7) // 8) * ((W + 7) // 8)
+            self._vbufs = dict(begin=torch.arange(0, n + 1, Nv, **i32), hw=torch.tensor([H, W] * n, **i32),
+                               off=torch.arange(n, dtype=torch.int64, device=self.dev) * (H * W),
+                               boff=torch.arange(n, dtype=torch.int64, device=self.dev) * nb,
+                               blocks=torch.empty(n * nb, dtype=torch.float32, device=self.dev))
+            v = self._vbufs
+            self._vstruct = N.SgViews(Nv, N.ptr(v["begin"]), N.ptr(v["hw"]), N.ptr(v["off"]), N.ptr(K), N.ptr(RT),
+                                      N.ptr(depths), N.ptr(colors), N.ptr(v["boff"]), N.ptr(v["blocks"]))
+            self._vkey = key
+        return self._vstruct
+
     def build(self, K, RT, colors, depths, vol_bbox, voxel_size, trunc_weight, th_low=13.5, th_high=13.5,
               obs_weight=1.0):
         """Fuse B frames of N views into the TSDF grid and build the tree."""
         B, D = self.B, self.D
-        Nv, H, W = depths.shape[1:]
         self.vol_bbox, self.voxel_size = vol_bbox, voxel_size
         self.trunc_weight = float(trunc_weight)
+        views = self._views(K, RT, colors, depths)
         st = N.stream()
         self.cnt.zero_()
         self.status.zero_()
         self._mark("start")
-        N.check(N.lib.sg_fuse_tsdf(N.ptr(K), N.ptr(RT), N.ptr(colors), N.ptr(depths), B, Nv, H, W, D, D, D,
-                                   N.ptr(vol_bbox), N.ptr(voxel_size), float(obs_weight), float(trunc_weight),
-                                   float(th_low), float(th_high), N.ptr(self.tsdf), N.ptr(self.weight),
-                                   N.ptr(self.color), N.ptr(self.occ0), N.ptr(self.cnt[0]), st), "fuse_tsdf")
+        N.check(N.lib.sg_fuse_tsdf_views(C.byref(views), B, D, N.ptr(vol_bbox), N.ptr(voxel_size),
+                                         float(obs_weight), float(trunc_weight), float(th_low), float(th_high),
+                                         N.ptr(self.tsdf), N.ptr(self.weight), N.ptr(self.color), N.ptr(self.occ0),
+                                         N.ptr(self.cnt[0]), st), "fuse_tsdf_views")
         self._mark("fusion")
         N.check(N.lib.sg_brick_occupancy(N.ptr(self.occ0), B, D, self.rate, N.ptr(self.occ1), N.ptr(self.cnt[1]),
                                          st), "brick_occupancy")
