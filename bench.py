@@ -97,7 +97,7 @@ def workload(cfg, rank=0):
 
 
 def algorithmic_bytes(cfg, n_hits, n_rays, S, n_pix):
-    """Per-launch algorithmic HBM bytes of each stage (see DESIGN.md)."""
+    """Per-launch algorithmic HBM bytes of each stage."""
     D = cfg["D"]
     V = D ** 3
     Vt = (D // cfg["rate"]) ** 3
@@ -572,7 +572,7 @@ def run_batch(args):
         out = dict(
             metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=args.steps, warmup=args.warmup,
             ms_per_step=ms_max, higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32",
-            data="synthetic (seeded capsule/ellipsoid scenes per frame, see DESIGN.md)",
+            data="synthetic (seeded capsule/ellipsoid scenes per frame)",
             config=dict(workload=("batched training step: %d frames x 4-8 views at {512,768,1024}^2, 256^3 TSDF "
                                   "+ 256^3x16 feature grid per frame, 8^3 bricks, %d targets 256^2-1024^2 "
                                   "(%d rays), S 32-128, forward + adjoint, CUDA graph" %
@@ -894,7 +894,7 @@ def run_plain(args):
         out = dict(
             metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=args.steps, warmup=args.warmup,
             ms_per_step=ms_max, higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32",
-            data="synthetic (seeded capsule/ellipsoid scenes, see DESIGN.md)",
+            data="synthetic (seeded capsule/ellipsoid scenes)",
             config=dict(workload="full-resolution plain forward: 4x1024^2 views, 512^3 TSDF, 8^3 bricks, "
                                  "1024^2 target, S=96" if not args.small else
                         "small: 4x512^2 views, 256^3 TSDF, 8^3 bricks, 512^2 target, S=64",

@@ -1,7 +1,7 @@
 /*
  * sailor_oracle.c -- CPU restatement of SAILOR's VoxelEncoding hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker: tests, the smoke check
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle: tests, the smoke check
  * and the CPU-baseline leg of the benchmark call it; the product (the CUDA
  * library under sailor_gb300/) never links or calls it.
  *

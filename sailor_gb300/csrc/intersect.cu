@@ -16,7 +16,7 @@
 //
 // Isolated occupied bricks (no occupied neighbour, hence not nodes) are
 // treated as empty.  The reference instead looks up node index == the
-// brick's local id there, i.e. an unrelated node (see DESIGN.md).
+// brick's local id there, i.e. an unrelated node.
 #include "common.cuh"
 
 namespace sg {
