@@ -89,6 +89,47 @@ def test_fuse_views_matches_per_frame(work):
     assert int(bp.status[0]) == 0
 
 
+def test_fusion_block_culling_with_nan_and_far_views(work):
+    """Fusion through the depth-block maps against the oracle, bit for bit,
+    with NaN depths (valid to the integrator, so they must stop a view from
+    being culled), depths beyond the valid range and a view whose camera is
+    moved far behind the volume."""
+    from sailor_gb300.batch import BatchPipeline
+    rng = np.random.default_rng(9)
+    frames = []
+    for fr in work["frames"]:
+        dep = [d.copy() for d in fr["depth"]]
+        for d in dep:
+            m = rng.random(d.shape) < 0.01
+            d[m] = np.nan
+            d[rng.random(d.shape) < 0.01] = 4.5
+        RT = [r.copy() for r in fr["RT"]]
+        RT[0][:, 3] = RT[0][:, 3] + np.float32(40.0)  # the volume is behind or outside this view
+        frames.append(dict(fr, depth=dep, RT=RT))
+    view_hw = [[d.shape for d in fr["depth"]] for fr in frames]
+    targets = [(t["frame"], t["ori"].shape[0], t["S"]) for t in work["targets"]]
+    bp = BatchPipeline(view_hw, targets, D=D, rate=RATE, C=CF, W_hits=96)
+    bp.load_views(frames, work["vol_bbox"], work["voxel_size"], work["trunc_weight"])
+    bp.build()
+    torch.cuda.synchronize()
+    for b, fr in enumerate(frames):
+        K = np.stack(fr["K"])[None]
+        RT = np.stack(fr["RT"])[None]
+        hmax = max(d.shape[0] for d in fr["depth"])
+        nv = len(fr["depth"])
+        dep = np.zeros((1, nv, hmax, hmax), np.float32)
+        col = np.zeros((1, nv, hmax, hmax), np.float32)
+        for v in range(nv):
+            h, w_ = fr["depth"][v].shape
+            dep[0, v, :h, :w_] = fr["depth"][v]
+            col[0, v, :h, :w_] = fr["color"][v]
+        ref = orc.integrate(K, RT, col, dep, D, work["vol_bbox"][b:b + 1], work["voxel_size"][b:b + 1], 1.0,
+                            work["trunc_weight"], 13.5, 13.5)
+        for got, key in ((bp.tsdf[b], "tsdf"), (bp.weight[b], "weight"), (bp.colorv[b], "color")):
+            assert np.array_equal(got.cpu().numpy().view(np.uint32), ref[key][0].view(np.uint32)), key
+        assert np.isnan(dep).any()
+
+
 def _hash_uniform(seed, r, q):
     x = (np.uint64(seed) + r.astype(np.uint64) * np.uint64(0x9E3779B97F4A7C15) + q.astype(np.uint64))
     x ^= x >> np.uint64(30)
