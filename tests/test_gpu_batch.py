@@ -325,12 +325,15 @@ def _byref(x):
     return C.byref(x)
 
 
-def test_train_step_clears_previous_gradients(work):
+@pytest.mark.parametrize("train_tsdf", [False, True])
+def test_train_step_clears_previous_gradients(work, train_tsdf):
     """Two training steps on different scenes (the second's depths scaled, so
-    its tree differs): the second step's gradients equal a fresh pipeline's,
-    although the first left gradients outside the second's node bricks."""
+    its tree differs): the second step's gradients (feature grid, and TSDF
+    grid when trained) equal a fresh pipeline's, although the first left
+    gradients outside the second's node bricks."""
     frames2 = [dict(fr, depth=[(d * 0.9).astype(np.float32) for d in fr["depth"]]) for fr in work["frames"]]
     bp = _pipeline(work)
+    bp.train_tsdf = train_tsdf
     bp.train_step()
     torch.cuda.synchronize()
     g1 = bp.grad_feat.clone()
@@ -342,9 +345,13 @@ def test_train_step_clears_previous_gradients(work):
     near2 = torch.as_tensor(_near_node_voxels(bp.brick_node.cpu().numpy(), bp.B, bp.Dt, RATE), device="cuda")
     assert (g1.abs().sum(-1) * (~near2)).max().item() > 0  # stale values a dense-only scheme would keep
     fresh = _pipeline(work)
+    fresh.train_tsdf = train_tsdf
     fresh.load_views(frames2, work["vol_bbox"], work["voxel_size"], work["trunc_weight"])
     fresh.train_step()
     torch.cuda.synchronize()
     m = fresh.grad_feat.abs().max().item()
     assert m > 0 and (bp.grad_feat - fresh.grad_feat).abs().max().item() <= 1e-5 * m
     assert torch.equal(bp.out_rgb, fresh.out_rgb)
+    if train_tsdf:
+        mt = fresh.grad_tsdf.abs().max().item()
+        assert mt > 0 and (bp.grad_tsdf - fresh.grad_tsdf).abs().max().item() <= 1e-5 * mt
