@@ -449,10 +449,14 @@ typedef struct SgViews {
 /* Ray segments (device arrays): segment s (one target camera) owns rays
  * [ray_begin[s], ray_begin[s+1]) of the packed ray buffers; they look into
  * frame frame[s] of the tree and grids and take samples[s] samples per ray
- * (at most the S of the launch). */
+ * (at most the S of the launch).  The render entry points process rays
+ * [ray_begin[0], total): a table whose arrays start at segment s0 of a
+ * larger one (count and total set to match) renders just those segments,
+ * so targets grouped by sample count can each go through the kernel sized
+ * for them (SgRenderArgs.S = the group's largest samples). */
 typedef struct SgRaySegments {
   int count;
-  int total;            /* rays of all segments (= ray_begin[count]) */
+  int total;            /* end of the last segment (= ray_begin[count]) */
   const int *ray_begin; /* [count+1] */
   const int *frame;     /* [count]   */
   const int *samples;   /* [count]   */

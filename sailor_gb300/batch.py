@@ -103,19 +103,36 @@ class BatchPipeline:
                              N.ptr(self.top_key), N.ptr(self.top_child_base), N.ptr(self.bot_key),
                              N.ptr(self.bot_parent), N.ptr(self.counts), N.ptr(self.voxel_size),
                              N.ptr(self.vol_bbox))
-        # rays and segments
+        # rays and segments.  Targets are laid out grouped by the sample
+        # capacity their S needs (32, 64 or 128 samples per ray), so each
+        # group is one launch of the training kernel sized for it;
+        # ray_slices[t] are the rays of target t in that layout, and the
+        # segment tables list targets in the order self.order.
         self.targets = [(int(f), int(n), int(s)) for f, n, s in targets]
         T = len(self.targets)
-        counts = [n for _, n, _ in self.targets]
+        cap = lambda s_: 32 if s_ <= 32 else (64 if s_ <= 64 else 128)  # noqa: E731
+        self.order = sorted(range(T), key=lambda t: (cap(self.targets[t][2]), t))
+        seg_t = [self.targets[t] for t in self.order]
+        counts = [n for _, n, _ in seg_t]
         rb = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
         if rb[-1] >= 2 ** 31:
             raise ValueError("at most 2^31 - 1 rays per launch")
         self.R = R = int(rb[-1])
         self.S = S = max(s for _, _, s in self.targets)
-        self.ray_slices = [(int(rb[t]), int(rb[t + 1])) for t in range(T)]
+        self.ray_slices = [None] * T
+        for i, t in enumerate(self.order):
+            self.ray_slices[t] = (int(rb[i]), int(rb[i + 1]))
         self.seg_begin = torch.tensor(rb.astype(np.int32), **i32)
-        self.seg_frame = torch.tensor([f for f, _, _ in self.targets], **i32)
-        self.seg_samples = torch.tensor([s for _, _, s in self.targets], **i32)
+        self.seg_frame = torch.tensor([f for f, _, _ in seg_t], **i32)
+        self.seg_samples = torch.tensor([s_ for _, _, s_ in seg_t], **i32)
+        # (first segment, end segment, largest S) of each capacity group
+        self._groups = []
+        for i, (_, _, s_) in enumerate(seg_t):
+            if self._groups and cap(seg_t[self._groups[-1][0]][2]) == cap(s_):
+                g0, _, sm = self._groups[-1]
+                self._groups[-1] = (g0, i + 1, max(sm, s_))
+            else:
+                self._groups.append((i, i + 1, s_))
         self.cameras = target_widths is not None
         if self.cameras:
             if len(target_widths) != T or any(n % int(w) for (_, n, _), w in zip(self.targets, target_widths)):
@@ -124,7 +141,7 @@ class BatchPipeline:
             self.tR = torch.zeros((T, 3, 3), **f32)
             self.tT = torch.zeros((T, 3), **f32)
             self.cams = torch.zeros((T, 21), **f32)
-            self.cam_w = torch.tensor([int(w) for w in target_widths], **i32)
+            self.cam_w = torch.tensor([int(target_widths[t]) for t in self.order], **i32)
             self.cam_seg = N.SgRaySegments(T, R, N.ptr(self.seg_begin), N.ptr(self.seg_frame),
                                            N.ptr(self.seg_samples), N.ptr(self.cams), N.ptr(self.cam_w))
         else:
@@ -197,9 +214,10 @@ class BatchPipeline:
         rays_calculating (origin -R^-1 T, direction R^-1 K^-1 [w, h, 1])."""
         if not self.cameras:
             raise RuntimeError("this pipeline takes ray buffers (load_rays)")
-        self.tK.copy_(torch.as_tensor(np.asarray(K, np.float32)).reshape(self.tK.shape))
-        self.tR.copy_(torch.as_tensor(np.asarray(R, np.float32)).reshape(self.tR.shape))
-        self.tT.copy_(torch.as_tensor(np.asarray(T, np.float32)).reshape(self.tT.shape))
+        perm = self.order  # the segment tables' target order
+        self.tK.copy_(torch.as_tensor(np.asarray(K, np.float32).reshape(self.tK.shape)[perm]))
+        self.tR.copy_(torch.as_tensor(np.asarray(R, np.float32).reshape(self.tR.shape)[perm]))
+        self.tT.copy_(torch.as_tensor(np.asarray(T, np.float32).reshape(self.tT.shape)[perm]))
 
     def set_fields(self, feat=None, head=None, target_rgb=None):
         if feat is not None:
@@ -212,12 +230,23 @@ class BatchPipeline:
     def render_args(self, trunc_metres, sdf_s=0.005, t_thres=1e-4, rand_seed=0, rand_const=0.5):
         """Fix the render's scalar parameters (trunc_metres: the truncation
         margin in metres; sdf_s: the density's length scale)."""
-        self.args = N.SgRenderArgs(
-            N.ptr(self.ori), N.ptr(self.dirs), N.ptr(self.hit_idx), N.ptr(self.hit_t0), N.ptr(self.hit_t1),
-            N.ptr(self.hit_count), N.ptr(self.valid_len), self.W, self.S, None, float(rand_const),
-            int(rand_seed), N.ptr(self.tsdf), self.D, float(trunc_metres), float(sdf_s), N.ptr(self.feat), self.D,
-            self.C, N.ptr(self.vol_bbox), N.ptr(self.voxel_size), N.ptr(self.head) if self.C != 3 else None,
-            float(t_thres))
+        def args(S):
+            return N.SgRenderArgs(
+                N.ptr(self.ori), N.ptr(self.dirs), N.ptr(self.hit_idx), N.ptr(self.hit_t0), N.ptr(self.hit_t1),
+                N.ptr(self.hit_count), N.ptr(self.valid_len), self.W, S, None, float(rand_const),
+                int(rand_seed), N.ptr(self.tsdf), self.D, float(trunc_metres), float(sdf_s), N.ptr(self.feat),
+                self.D, self.C, N.ptr(self.vol_bbox), N.ptr(self.voxel_size),
+                N.ptr(self.head) if self.C != 3 else None, float(t_thres))
+
+        self.args = args(self.S)
+        # one (segment sub-table, arguments) per capacity group: the training
+        # pass runs each group through the kernel sized for its largest S
+        rb = self.seg_begin.cpu().numpy()
+        self._group_launch = []
+        for g0, g1, sm in self._groups:
+            seg = N.SgRaySegments(g1 - g0, int(rb[g1]), self.seg_begin.data_ptr() + 4 * g0,
+                                  self.seg_frame.data_ptr() + 4 * g0, self.seg_samples.data_ptr() + 4 * g0)
+            self._group_launch.append((seg, args(sm)))
         return self.args
 
     def _mark(self, name):
@@ -313,11 +342,12 @@ class BatchPipeline:
         self.build(before_tree=lambda: main.wait_stream(self.side))
         self.intersect()
         self._mark("grad_prep")
-        N.check(N.lib.sg_render_segments_train(
-            C.byref(self.tree), C.byref(self.seg), C.byref(self.args), N.ptr(self.target_rgb),
-            2.0 / (3.0 * self.R), N.ptr(self.out_rgb), N.ptr(self.out_depth), N.ptr(self.out_ws),
-            N.ptr(self.out_alpha), N.ptr(self.out_loss), N.ptr(self.grad_feat),
-            N.ptr(self.grad_tsdf) if self.train_tsdf else None, N.stream()), "render_train")
+        for seg, args in self._group_launch:
+            N.check(N.lib.sg_render_segments_train(
+                C.byref(self.tree), C.byref(seg), C.byref(args), N.ptr(self.target_rgb),
+                2.0 / (3.0 * self.R), N.ptr(self.out_rgb), N.ptr(self.out_depth), N.ptr(self.out_ws),
+                N.ptr(self.out_alpha), N.ptr(self.out_loss), N.ptr(self.grad_feat),
+                N.ptr(self.grad_tsdf) if self.train_tsdf else None, N.stream()), "render_train")
         self.grad_bricks.copy_(self.brick_node)
         self._mark("train")
 

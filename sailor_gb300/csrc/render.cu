@@ -161,7 +161,10 @@ __global__ void __launch_bounds__(256) render_fwd_kernel(RenderParams p) {
   SG_RENDER_SMEM(E)
   const int lane = lane_id();
   const int Smax = p.sp.S;
-  for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < p.R;
+  // a segment table covers rays [ray_begin[0], total): a sub-table of
+  // consecutive segments is a group of targets
+  const long r0 = p.nseg > 0 ? (long)__ldg(p.seg_begin) : 0;
+  for (long r = r0 + (((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5); r < p.R;
        r += ((long)gridDim.x * blockDim.x) >> 5) {
     int b, S, sgm;
     ray_frame(p, r, b, S, sgm);
@@ -273,7 +276,10 @@ __global__ void __launch_bounds__(256, 2) render_bwd_kernel(RenderParams p) {
   __shared__ long long s_kf[8][32], s_kt[8][32];  // packed cell keys, -1: no contribution
   const int lane = lane_id();
   const int Smax = p.sp.S;
-  for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < p.R;
+  // a segment table covers rays [ray_begin[0], total): a sub-table of
+  // consecutive segments is a group of targets
+  const long r0 = p.nseg > 0 ? (long)__ldg(p.seg_begin) : 0;
+  for (long r = r0 + (((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5); r < p.R;
        r += ((long)gridDim.x * blockDim.x) >> 5) {
     int b, S, sgm;
     ray_frame(p, r, b, S, sgm);
