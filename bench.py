@@ -488,6 +488,7 @@ def run_batch(args):
         e1.record()
         barrier()
     ms_max, value = whole_job(e0.elapsed_time(e1) / args.steps, R, world, dev)
+    ref_rgb = bp.out_rgb.cpu()  # the timed steps' image, for the e2e check below
 
     # per-stage times (eager pass with events on the launching stream)
     stage_sum = {}
@@ -529,9 +530,11 @@ def run_batch(args):
                 color=torch.as_tensor(np.concatenate([c.reshape(-1) for fr in w["frames"] for c in fr["color"]])),
                 K=torch.as_tensor(np.stack([k for fr in w["frames"] for k in fr["K"]])),
                 RT=torch.as_tensor(np.stack([k for fr in w["frames"] for k in fr["RT"]])),
-                tK=torch.as_tensor(np.stack([t["K"] for t in w["targets"]])),
-                tR=torch.as_tensor(np.stack([t["R"] for t in w["targets"]])),
-                tT=torch.as_tensor(np.stack([t["T"] for t in w["targets"]])),
+                # target cameras in the pipeline's segment order (what
+                # load_cameras arranges; here once, outside the timed region)
+                tK=torch.as_tensor(np.stack([w["targets"][t]["K"] for t in bp.order])),
+                tR=torch.as_tensor(np.stack([w["targets"][t]["R"] for t in bp.order])),
+                tT=torch.as_tensor(np.stack([w["targets"][t]["T"] for t in bp.order])),
                 target_rgb=torch.as_tensor(target))
     host = {k: v.contiguous().pin_memory() for k, v in host.items()}
     dst = dict(depth=bp.depth, color=bp.color, K=bp.K, RT=bp.RT, tK=bp.tK, tR=bp.tR, tT=bp.tT,
@@ -557,6 +560,8 @@ def run_batch(args):
     f1.record()
     barrier()
     _, e2e_value = whole_job(f0.elapsed_time(f1) / args.steps, R, world, dev)
+    if not torch.equal(out_host, ref_rgb):
+        raise RuntimeError("the e2e steps rendered a different image than the timed steps")
 
     if rank == 0:
         pk, pk_kind = peaks()
@@ -590,9 +595,10 @@ def run_batch(args):
                           algorithmic_bytes=ab[dom]),
             rooflines={k: dict(achieved=v, frac=v / pk["hbm_gbs"], algorithmic_bytes=ab[k]) for k, v in rl.items()},
             e2e=dict(value=e2e_value, unit=UNIT, h2d_bytes_per_step=h2d, d2h_bytes_per_step=d2h),
-            # per step: fusion 1, coarse occupancy 1, tree 5, camera table 1,
-            # ray generation 1, intersection 1, training pass 1
-            gpu_launches=11 * args.steps,
+            # per step: gradient clear 1, depth blocks 1, fusion 1, coarse
+            # occupancy 1, tree 5, camera table 1, ray generation 1,
+            # intersection 1, and one training pass per sample-capacity group
+            gpu_launches=(12 + len(bp._group_launch)) * args.steps,
             clocks=clk.summary(),
         )
         if not args.no_cpu_baseline:
