@@ -141,8 +141,11 @@ __device__ __forceinline__ float from_ordered(uint32_t k) {
   return __uint_as_float((k >> 31) ? (k ^ 0x80000000u) : ~k);
 }
 
-// E keys per lane, element i = e*32 + lane, P = 32*E (power of two); K is
-// a 64-bit (depth, position) key or a 32-bit depth key
+// E keys per lane in blocked order, element i = lane*E + e, P = 32*E (a
+// power of two); K is a 64-bit (depth, position) key or a 32-bit depth key.
+// Partner distances below E stay in the lane, so of the network's
+// log2(P)(log2(P)+1)/2 steps only those with distance >= E exchange across
+// lanes (15 of 28 at E = 4).
 template <int E, typename K>
 __device__ __forceinline__ void bitonic_warp(K (&key)[E]) {
   const int lane = lane_id();
@@ -151,33 +154,131 @@ __device__ __forceinline__ void bitonic_warp(K (&key)[E]) {
   for (int k = 2; k <= P; k <<= 1) {
 #pragma unroll
     for (int j = k >> 1; j > 0; j >>= 1) {
-      if (j >= 32) {
-        const int m = j >> 5;
+      if (j < E) {
 #pragma unroll
         for (int e = 0; e < E; e++) {
-          if ((e & m) == 0) {
-            const int i = e * 32 + lane;
-            const bool asc = (i & k) == 0;
-            K a = key[e], c = key[e ^ m];
-            bool sw = asc ? (a > c) : (a < c);
+          if ((e & j) == 0) {
+            const bool asc = ((lane * E + e) & k) == 0;
+            const K a = key[e], c = key[e + j];
+            const bool sw = asc ? (a > c) : (a < c);
             key[e] = sw ? c : a;
-            key[e ^ m] = sw ? a : c;
+            key[e + j] = sw ? a : c;
           }
         }
       } else {
+        const int m = j / E;  // partner lane distance
+        const bool lower = (lane & m) == 0;
 #pragma unroll
         for (int e = 0; e < E; e++) {
-          const int i = e * 32 + lane;
-          const bool asc = (i & k) == 0;
-          K other = __shfl_xor_sync(SG_FULL, key[e], j);
-          const bool lower = (lane & j) == 0;
-          K mn = key[e] < other ? key[e] : other;
-          K mx = key[e] < other ? other : key[e];
+          const bool asc = ((lane * E + e) & k) == 0;
+          const K other = __shfl_xor_sync(SG_FULL, key[e], m);
+          const K mn = key[e] < other ? key[e] : other;
+          const K mx = key[e] < other ? other : key[e];
           key[e] = (lower == asc) ? mn : mx;
         }
       }
     }
   }
+}
+
+// E consecutive floats from a 4E-byte aligned address (E = 1, 2, 4, 8)
+template <int E>
+__device__ __forceinline__ void load_run(const float *src, float (&v)[E]) {
+  if constexpr (E == 1) {
+    v[0] = src[0];
+  } else if constexpr (E == 2) {
+    const float2 a = *reinterpret_cast<const float2 *>(src);
+    v[0] = a.x;
+    v[1] = a.y;
+  } else {
+#pragma unroll
+    for (int q = 0; q < E; q += 4) {
+      const float4 a = *reinterpret_cast<const float4 *>(src + q);
+      v[q] = a.x;
+      v[q + 1] = a.y;
+      v[q + 2] = a.z;
+      v[q + 3] = a.w;
+    }
+  }
+}
+
+// E consecutive 32-bit words to a 4E-byte aligned address (E = 1, 2, 4, 8)
+template <int E>
+__device__ __forceinline__ void store_run(uint32_t *dst, const uint32_t (&v)[E]) {
+  if constexpr (E == 1) {
+    dst[0] = v[0];
+  } else if constexpr (E == 2) {
+    *reinterpret_cast<uint2 *>(dst) = make_uint2(v[0], v[1]);
+  } else {
+#pragma unroll
+    for (int q = 0; q < E; q += 4) *reinterpret_cast<uint4 *>(dst + q) = make_uint4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+  }
+}
+
+// Stable warp sort of n <= 32E values with their input positions, on 32-bit
+// keys.  The (depth, position) order needs 64-bit compare-exchanges, and the
+// network is bound by the integer pipe; here the network sorts the depth
+// keys alone, and each input element finds its place afterwards: a binary
+// search gives the number of smaller keys, and elements of equal keys (rare
+// but for padding) count the equal ones before them in input order, slot
+// by slot with __match_any_sync.
+//   buf: shared, 16-byte aligned, 32E words; on entry buf[0, n) the values
+//        in input order (overwritten: the sorted keys).
+//   cnt: shared scratch of n ints.
+//   key: on return the sorted keys, blocked (element j = lane*E + e; ~0u
+//        past n).  pos: the sorted position of input element e*32 + lane.
+template <int E>
+__device__ __forceinline__ void warp_sort_ranked(float *buf, int *cnt, int n, uint32_t (&key)[E], int (&pos)[E]) {
+  const int lane = lane_id();
+  uint32_t *u = reinterpret_cast<uint32_t *>(buf);
+  uint32_t x[E];
+#pragma unroll
+  for (int e = 0; e < E; e++) x[e] = (e * 32 + lane < n) ? ordered_bits(buf[e * 32 + lane]) : 0u;
+  {
+    float v[E];
+    load_run<E>(buf + lane * E, v);
+#pragma unroll
+    for (int e = 0; e < E; e++) key[e] = (lane * E + e < n) ? ordered_bits(v[e]) : ~0u;
+  }
+  __syncwarp();
+  bitonic_warp<E>(key);
+  store_run<E>(u + lane * E, key);
+  __syncwarp();
+  int lb[E];
+  bool tie[E];
+  bool any = false;
+#pragma unroll
+  for (int e = 0; e < E; e++) {
+    // lower bound of x among the 32E sorted keys (entries past n are ~0u,
+    // never below an input key)
+    int l = 0;
+#pragma unroll
+    for (int step = 16 * E; step >= 1; step >>= 1) l += (u[l + step - 1] < x[e]) ? step : 0;
+    lb[e] = l;
+    pos[e] = l;
+    tie[e] = (e * 32 + lane < n) && l + 1 < n && u[l + 1] == x[e];
+    any |= tie[e];
+  }
+  if (__any_sync(SG_FULL, any)) {
+#pragma unroll
+    for (int e = 0; e < E; e++)
+      if (tie[e]) cnt[lb[e]] = 0;
+    __syncwarp();
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      // slot e holds inputs 32e .. 32e+31: earlier slots are counted in
+      // cnt, earlier lanes of this slot by the match mask
+      const unsigned m = __match_any_sync(SG_FULL, tie[e] ? lb[e] : -1 - lane);
+      int before = 0;
+      if (tie[e]) before = cnt[lb[e]] + __popc(m & lt);
+      __syncwarp();
+      if (tie[e] && (m >> lane) == 1u) cnt[lb[e]] += __popc(m);
+      __syncwarp();
+      pos[e] += before;
+    }
+  }
+  __syncwarp();
 }
 
 // Sort the samples of a ray in shared memory.  sz[0, done) hold the
@@ -192,40 +293,31 @@ template <int EMAX, bool POS>
 __device__ __forceinline__ void warp_sort_samples(float *sz, int *spos, int S, int done) {
   const int lane = lane_id();
   const int npad = S - done;
-  if (POS)
-    for (int q = lane; q < npad; q += 32) spos[q] = done + q;
   if (done > 0) {
     auto run = [&](auto tag) {
       constexpr int E = decltype(tag)::value;
       if constexpr (POS) {
-        unsigned long long key[E];
+        uint32_t key[E];
+        int pos[E];
+        warp_sort_ranked<E>(sz, spos, done, key, pos);  // spos[0, done): scratch
 #pragma unroll
         for (int e = 0; e < E; e++) {
+          const int j = lane * E + e;
+          if (j < done) sz[npad + j] = from_ordered(key[e]);
           const int i = e * 32 + lane;
-          key[e] = (i < done) ? (((unsigned long long)ordered_bits(sz[i]) << 32) | (unsigned)i) : ~0ull;
-        }
-        __syncwarp();
-        bitonic_warp<E>(key);
-#pragma unroll
-        for (int e = 0; e < E; e++) {
-          const int j = e * 32 + lane;
-          if (j < done) {
-            sz[npad + j] = from_ordered((uint32_t)(key[e] >> 32));
-            spos[npad + j] = (int)(key[e] & 0xffffffffu);
-          }
+          if (i < done) spos[npad + pos[e]] = i;
         }
       } else {
         uint32_t key[E];
+        float v[E];
+        load_run<E>(sz + lane * E, v);
 #pragma unroll
-        for (int e = 0; e < E; e++) {
-          const int i = e * 32 + lane;
-          key[e] = (i < done) ? ordered_bits(sz[i]) : ~0u;
-        }
+        for (int e = 0; e < E; e++) key[e] = (lane * E + e < done) ? ordered_bits(v[e]) : ~0u;
         __syncwarp();
         bitonic_warp<E>(key);
 #pragma unroll
         for (int e = 0; e < E; e++) {
-          const int j = e * 32 + lane;
+          const int j = lane * E + e;
           if (j < done) sz[npad + j] = from_ordered(key[e]);
         }
       }
@@ -242,7 +334,10 @@ __device__ __forceinline__ void warp_sort_samples(float *sz, int *spos, int S, i
     }
   }
   __syncwarp();
-  for (int q = lane; q < npad; q += 32) sz[q] = -1.0f;
+  for (int q = lane; q < npad; q += 32) {
+    sz[q] = -1.0f;
+    if (POS) spos[q] = done + q;
+  }
   __syncwarp();
 }
 

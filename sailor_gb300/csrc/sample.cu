@@ -10,9 +10,10 @@
 // then one coalesced row write.  Sample depths reproduce the reference's
 // double-precision expression with float-only error-free arithmetic.
 //
-// sort_rows_kernel / sample_sorted_kernel: a register bitonic network per
-// row on (depth, position) keys -- a total order, so equal depths keep their
-// input order.
+// sort_rows_kernel / sample_sorted_kernel: the stable (depth, position)
+// order of each row -- equal depths keep their input order -- from a
+// register bitonic network on 32-bit depth keys and a ranking pass
+// (warp_sort_ranked in ray_core.cuh).
 #include "ray_core.cuh"
 
 namespace sg {
@@ -35,28 +36,77 @@ __global__ void __launch_bounds__(256) sample_coarse_kernel(SampleParams p) {
   }
 }
 
-template <int E>
+// A warp per row: the row goes through shared memory into the ranked sort
+// (warp_sort_ranked).  VEC: rows start 16-byte aligned and S is a multiple
+// of 4, so each lane's run of E consecutive elements moves as float2 /
+// float4 / int4 (a run of 8 as two quads, each within the row or wholly
+// past its end).
+template <int E, bool VEC>
 __global__ void __launch_bounds__(256) sort_rows_kernel(const float *__restrict__ z, long R, int S,
                                                         float *sorted, int *idx) {
-  const int lane = lane_id();
+  constexpr int Q = E < 4 ? E : 4;  // elements per vector access
+  __shared__ __align__(16) float s_v[8][32 * E];
+  __shared__ __align__(16) int s_p[8][32 * E];
+  const int lane = lane_id(), w8 = threadIdx.x >> 5;
+  const int i0 = lane * E;
+  float *sv = s_v[w8];
+  int *sp = s_p[w8];
   for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < R;
        r += ((long)gridDim.x * blockDim.x) >> 5) {
-    unsigned long long key[E];
+    const float *zr = z + (size_t)r * S;
 #pragma unroll
-    for (int e = 0; e < E; e++) {
-      int i = e * 32 + lane;
-      key[e] = (i < S) ? (((unsigned long long)ordered_bits(__ldg(z + (size_t)r * S + i)) << 32) | (unsigned)i)
-                       : ~0ull;
+    for (int q = 0; q < E; q += Q) {
+      float t[Q];
+      if (VEC && Q > 1) {
+        if (i0 + q < S) {
+          load_run<Q>(zr + i0 + q, t);
+        } else {
+#pragma unroll
+          for (int u = 0; u < Q; u++) t[u] = 0.0f;
+        }
+      } else {
+#pragma unroll
+        for (int u = 0; u < Q; u++) t[u] = (i0 + q + u < S) ? __ldg(zr + i0 + q + u) : 0.0f;
+      }
+      uint32_t w[Q];
+#pragma unroll
+      for (int u = 0; u < Q; u++) w[u] = __float_as_uint(t[u]);
+      store_run<Q>(reinterpret_cast<uint32_t *>(sv + i0 + q), w);
     }
-    bitonic_warp<E>(key);
+    __syncwarp();
+    uint32_t key[E];
+    int pos[E];
+    warp_sort_ranked<E>(sv, sp, S, key, pos);
 #pragma unroll
-    for (int e = 0; e < E; e++) {
-      int i = e * 32 + lane;
-      if (i < S) {
-        sorted[(size_t)r * S + i] = from_ordered((uint32_t)(key[e] >> 32));
-        idx[(size_t)r * S + i] = (int)(key[e] & 0xffffffffu);
+    for (int e = 0; e < E; e++)
+      if (e * 32 + lane < S) sp[pos[e]] = e * 32 + lane;
+    __syncwarp();
+    float *sr = sorted + (size_t)r * S;
+    int *ir = idx + (size_t)r * S;
+#pragma unroll
+    for (int q = 0; q < E; q += Q) {
+      if (VEC && Q > 1) {
+        if (i0 + q < S) {
+          if constexpr (Q == 2) {
+            *reinterpret_cast<float2 *>(sr + i0 + q) = make_float2(from_ordered(key[q]), from_ordered(key[q + 1]));
+            *reinterpret_cast<int2 *>(ir + i0 + q) = *reinterpret_cast<const int2 *>(sp + i0 + q);
+          } else if constexpr (Q == 4) {
+            *reinterpret_cast<float4 *>(sr + i0 + q) = make_float4(from_ordered(key[q]), from_ordered(key[q + 1]),
+                                                                   from_ordered(key[q + 2]), from_ordered(key[q + 3]));
+            *reinterpret_cast<int4 *>(ir + i0 + q) = *reinterpret_cast<const int4 *>(sp + i0 + q);
+          }
+        }
+      } else {
+#pragma unroll
+        for (int u = 0; u < Q; u++) {
+          if (i0 + q + u < S) {
+            sr[i0 + q + u] = from_ordered(key[q + u]);
+            ir[i0 + q + u] = sp[i0 + q + u];
+          }
+        }
       }
     }
+    __syncwarp();
   }
 }
 
@@ -66,7 +116,7 @@ __global__ void __launch_bounds__(256) sort_rows_kernel(const float *__restrict_
 template <int E>
 __global__ void __launch_bounds__(256) sample_sorted_kernel(SampleParams p, const int *__restrict__ hit_count,
                                                             float rand_const, float *out_z, int *out_idx) {
-  __shared__ float s_z[8][32 * E];
+  __shared__ __align__(16) float s_z[8][32 * E];
   __shared__ int s_i[8][32 * E];
   __shared__ int s_p[8][32 * E];
   __shared__ SampleScratch s_sc[8];
@@ -141,10 +191,16 @@ extern "C" int sg_sort_samples(const float *z, int R, int S, float *sorted, int 
   if (!z || !sorted || !idx || R < 0 || S <= 0) return SG_ERR_INVALID_ARG;
   if (R == 0) return SG_OK;
   int g = grid_for(R);
-  if (S <= 32) sort_rows_kernel<1><<<g, 256, 0, stream>>>(z, R, S, sorted, idx);
-  else if (S <= 64) sort_rows_kernel<2><<<g, 256, 0, stream>>>(z, R, S, sorted, idx);
-  else if (S <= 128) sort_rows_kernel<4><<<g, 256, 0, stream>>>(z, R, S, sorted, idx);
-  else if (S <= 256) sort_rows_kernel<8><<<g, 256, 0, stream>>>(z, R, S, sorted, idx);
+  const bool vec = (S % 4 == 0) && ((((uintptr_t)z) | ((uintptr_t)sorted) | ((uintptr_t)idx)) & 15) == 0;
+  auto go = [&](auto tag) {
+    constexpr int E = decltype(tag)::value;
+    if (vec) sort_rows_kernel<E, true><<<g, 256, 0, stream>>>(z, R, S, sorted, idx);
+    else sort_rows_kernel<E, false><<<g, 256, 0, stream>>>(z, R, S, sorted, idx);
+  };
+  if (S <= 32) go(std::integral_constant<int, 1>());
+  else if (S <= 64) go(std::integral_constant<int, 2>());
+  else if (S <= 128) go(std::integral_constant<int, 4>());
+  else if (S <= 256) go(std::integral_constant<int, 8>());
   else return SG_ERR_UNSUPPORTED;
   SG_LAUNCH_CHECK();
   return SG_OK;

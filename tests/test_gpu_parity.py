@@ -154,6 +154,33 @@ def test_sort_exact(case):
     assert np.array_equal(idx.cpu().numpy(), i2)
 
 
+@pytest.mark.parametrize("S", [1, 7, 31, 32, 33, 50, 64, 96, 100, 128, 132, 200, 256])
+def test_sort_row_lengths(S):
+    """sort_samplings over every network size (rows of up to 32, 64, 128,
+    256), row lengths off the vector width, -1 padding and repeated depths:
+    exactly the oracle's stable order; a view that starts 4 bytes
+    past an allocation takes the scalar path with the same result."""
+    rng = np.random.default_rng(S)
+    R = 300
+    z = rng.uniform(0.0, 4.0, (1, R, S)).astype(np.float32)
+    z[0, ::3, S // 2:] = -1.0  # the sampler's padding
+    z[0, 1::5, :] = -1.0  # rays with no sample
+    z[0, 2::7, : max(1, S // 3)] = np.float32(1.25)  # repeated depths
+    z[0, 4::11, ::2] = 0.0
+    from sailor_gb300.dist import VoxelEncoding as VE
+    octree = VE.MultiLayerOctree(2, 1, 4, 0)
+    s2, i2 = orc.sort(z)
+    srt, idx = octree.sort_samplings(_t(z))
+    assert np.array_equal(srt.cpu().numpy().view(np.uint32), s2.view(np.uint32))
+    assert np.array_equal(idx.cpu().numpy(), i2)
+    buf = torch.empty(z.size + 1, device="cuda")
+    view = buf[1:].view(z.shape)
+    view.copy_(_t(z))
+    srt, idx = octree.sort_samplings(view)
+    assert np.array_equal(srt.cpu().numpy().view(np.uint32), s2.view(np.uint32))
+    assert np.array_equal(idx.cpu().numpy(), i2)
+
+
 def test_trilerp_nodes(case):
     g, r = case["g"], case["ref"]
     octree = g["octree"]
