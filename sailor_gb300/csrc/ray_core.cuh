@@ -94,8 +94,12 @@ __device__ __forceinline__ int warp_sample_ray(const SampleParams &p, long r, in
       sc.id[lane] = id;
       __syncwarp();
       const int end = min(has + __shfl_sync(SG_FULL, incl, 31), S);
+      // owners are among the lanes with samples; lanes past the last of
+      // them start at or after end, so the search stops there
+      const unsigned with_n = __ballot_sync(SG_FULL, n > 0);
+      const int last = with_n ? 31 - __clz(with_n) : 0;
       for (int q = has + lane; q < end; q += 32) {
-        int lo = 0, up = 31;
+        int lo = 0, up = last;
         while (lo < up) {
           const int mid = (lo + up + 1) >> 1;
           if (sc.start[mid] <= q) lo = mid;
