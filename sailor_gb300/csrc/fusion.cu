@@ -427,7 +427,7 @@ struct CullSmem {
   int rect[kMaxViews][4];  // x0, x1, y0, y1 (clamped to the image)
   float czmin[kMaxViews];
   int state[kMaxViews];    // 0: keep, 1: leave out, 2: scan the rectangle
-  int bskip[kMaxViews];    // block-map verdict of a scanned view
+  int bskip[kMaxViews];    // block-map decision of a scanned view
   float wmax[2][8];
   int wnan[2][8];
   unsigned skip;
