@@ -324,10 +324,12 @@ class MultiLayerOctree:
     def sort_samplings(self, sampled_depths):
         with torch.cuda.device(self.device):
             z = _in(sampled_depths, "sampled_depths")
-            S = z.shape[-1]
-            R = z.numel() // S
             srt = torch.empty_like(z)
             idx = torch.empty(z.shape, dtype=torch.int32, device=z.device)
+            if z.numel() == 0:  # as torch.sort: empty in, empty out
+                return srt, idx
+            S = z.shape[-1]
+            R = z.numel() // S
             N.check(N.lib.sg_sort_samples(N.ptr(z), R, S, N.ptr(srt), N.ptr(idx), N.stream()), "sort")
             return srt, idx
 

@@ -181,6 +181,31 @@ def test_sort_row_lengths(S):
     assert np.array_equal(idx.cpu().numpy(), i2)
 
 
+def test_sort_empty_rows():
+    """As torch.sort along the last axis: empty in, empty out."""
+    from sailor_gb300.dist import VoxelEncoding as VE
+    octree = VE.MultiLayerOctree(2, 1, 4, 0)
+    for shape in ((1, 0, 16), (2, 5, 0)):
+        srt, idx = octree.sort_samplings(torch.empty(shape, device="cuda"))
+        assert srt.shape == shape and idx.shape == shape and idx.dtype == torch.int32
+
+
+@pytest.mark.parametrize("S", [1, 200, 256])
+def test_sampling_sizes_given_oracle_hits(case, S):
+    """The smallest and the largest sample rows (one sample; 200 and 256:
+    the 8-per-lane layout) give the oracle's samples bit for bit."""
+    h, r = case["ref"]["hits"], case["ref"]
+    octree = case["g"]["octree"]
+    B, R = h["idx"].shape[:2]
+    rands = np.random.default_rng(S).random((B, R, S), dtype=np.float32)
+    si, sz = octree.ray_voxels_points_sampling_coarse(_t(h["idx"], torch.int32), _t(h["t0"]), _t(h["t1"]),
+                                                      _t(rands), _t(h["valid_len"]), 0, S)
+    si2, sz2, _ = orc.sample_coarse(r["tree"], h, rands, r["voxel_size"], S)
+    assert np.array_equal(si.cpu().numpy(), si2)
+    assert np.array_equal(sz.cpu().numpy(), sz2)
+    assert (si2 >= 0).any()
+
+
 def test_trilerp_nodes(case):
     g, r = case["g"], case["ref"]
     octree = g["octree"]
