@@ -45,7 +45,10 @@
 #define FLAG_ALIAS 2    /* ray visits an occupied top brick that is not a node */
 #define FLAG_OVERFLOW 4 /* more hits than the output row holds                 */
 
+/* Near ties of finite values only: an infinite slab distance (a direction */
+/* component of 0) is infinite on the GPU as well, so it decides the same.  */
 static inline int near_eq(double a, double b) {
+  if (!isfinite(a) || !isfinite(b)) return 0;
   double m = fabs(a) > fabs(b) ? fabs(a) : fabs(b);
   return fabs(a - b) <= TIE_REL * m + 1e-30;
 }

@@ -126,6 +126,41 @@ def test_traversal(case):
     assert (g["idx"][pad] == -1).all() and (g["t0"][pad] == -1).all() and (g["t1"][pad] == -1).all()
 
 
+def test_axis_aligned_rays(case):
+    """Rays along the axes and in the axis planes (direction components
+    exactly 0, so the slab test's reciprocals are infinite), started outside
+    the volume on the far side of a random inside point: traversal rows equal
+    the oracle's on unflagged rays, and the samples given those rows too."""
+    g, r = case["g"], case["ref"]
+    bb = r["vol_bbox"]
+    B = bb.shape[0]
+    n = 3000
+    rng = np.random.default_rng(11)
+    axes = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1],
+                     [0.6, 0.8, 0], [0, -0.8, 0.6], [0.8, 0, -0.6]], np.float32)
+    dirs = axes[rng.integers(0, len(axes), (B, n))]
+    lo, hi = bb[:, None, :, 0], bb[:, None, :, 1]
+    inside = lo + (hi - lo) * rng.random((B, n, 3))
+    ori = (inside - dirs * (hi - lo).max() * 1.5).astype(np.float32)
+    W = case["W"]
+    octree = g["octree"]
+    idx, t0, t1, vl = octree.voxel_traversal(_t(ori), _t(dirs), W, 0, -1, False, -1)
+    h = orc.voxel_traversal(r["tree"], ori, dirs, r["voxel_size"], bb, W=W)
+    idx, t0, t1 = idx.cpu().numpy(), t0.cpu().numpy(), t1.cpu().numpy()
+    ok = h["flags"] == 0
+    rows_eq = np.all(idx == h["idx"], axis=-1)
+    assert rows_eq[ok].all(), f"{(~rows_eq[ok]).sum()} unflagged rays differ"
+    assert ok.mean() > 0.9 and (h["idx"] >= 0).sum() > 100
+    m = (h["idx"] >= 0) & rows_eq[..., None]
+    assert np.abs(t0[m] - h["t0"][m]).max() <= ATOL and np.abs(t1[m] - h["t1"][m]).max() <= ATOL
+    S = case["c"]["S"]
+    rands = rng.random((B, n, S), dtype=np.float32)
+    si, sz = octree.ray_voxels_points_sampling_coarse(_t(h["idx"], torch.int32), _t(h["t0"]), _t(h["t1"]),
+                                                      _t(rands), _t(h["valid_len"]), 0, S)
+    si2, sz2, _ = orc.sample_coarse(r["tree"], h, rands, r["voxel_size"], S)
+    assert np.array_equal(si.cpu().numpy(), si2) and np.array_equal(sz.cpu().numpy(), sz2)
+
+
 def test_sampling_given_oracle_hits(case):
     """Same hit lists in -> bit-identical samples out (counts, ids, depths)."""
     from sailor_gb300.dist import VoxelEncoding as VE  # noqa: F401
