@@ -188,8 +188,9 @@ extern "C" int sg_sample_coarse(const SgTree *tree, const int *hit_idx, const fl
 }
 
 extern "C" int sg_sort_samples(const float *z, int R, int S, float *sorted, int *idx, sg_stream_t stream) {
-  if (!z || !sorted || !idx || R < 0 || S <= 0) return SG_ERR_INVALID_ARG;
-  if (R == 0) return SG_OK;
+  if (R < 0 || S <= 0) return SG_ERR_INVALID_ARG;
+  if (R == 0) return SG_OK;  // no rows (the buffers may be NULL)
+  if (!z || !sorted || !idx) return SG_ERR_INVALID_ARG;
   int g = grid_for(R);
   const bool vec = (S % 4 == 0) && ((((uintptr_t)z) | ((uintptr_t)sorted) | ((uintptr_t)idx)) & 15) == 0;
   auto go = [&](auto tag) {

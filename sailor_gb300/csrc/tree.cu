@@ -335,8 +335,9 @@ __global__ void tree_nodes_kernel(SgTree t, int n_nodes, float *out) {
 using namespace sg;
 
 extern "C" int sg_tree_nodes(const SgTree *tree, int n_nodes, float *out, sg_stream_t stream) {
-  if (!tree || !out || n_nodes < 0) return SG_ERR_INVALID_ARG;
-  if (n_nodes == 0) return SG_OK;
+  if (!tree || n_nodes < 0) return SG_ERR_INVALID_ARG;
+  if (n_nodes == 0) return SG_OK;  // an empty tree: nothing to write (out may be NULL)
+  if (!out) return SG_ERR_INVALID_ARG;
   int g = ceil_div(n_nodes, 256);
   if (g > 152 * 32) g = 152 * 32;
   tree_nodes_kernel<<<g, 256, 0, stream>>>(*tree, n_nodes, out);

@@ -161,6 +161,65 @@ def test_axis_aligned_rays(case):
     assert np.array_equal(si.cpu().numpy(), si2) and np.array_equal(sz.cpu().numpy(), sz2)
 
 
+def test_rays_starting_inside(case):
+    """Rays whose origin lies inside the volume (the whole-grid slab test
+    clamps the entry to t = 0, so the walk starts in the origin's brick):
+    rows as the oracle's on unflagged rays (t-values and valid lengths within
+    the traversal tolerances), and the samples given the oracle's rows bit
+    for bit."""
+    g, r = case["g"], case["ref"]
+    bb = r["vol_bbox"]
+    B = bb.shape[0]
+    n = 2000
+    rng = np.random.default_rng(12)
+    lo, hi = bb[:, None, :, 0], bb[:, None, :, 1]
+    ori = (lo + (hi - lo) * rng.uniform(0.05, 0.95, (B, n, 3))).astype(np.float32)
+    d = rng.normal(size=(B, n, 3))
+    dirs = (d / np.linalg.norm(d, axis=-1, keepdims=True)).astype(np.float32)
+    octree = g["octree"]
+    idx, t0, t1, vl = octree.voxel_traversal(_t(ori), _t(dirs), case["W"], 0, -1, False, -1)
+    h = orc.voxel_traversal(r["tree"], ori, dirs, r["voxel_size"], bb, W=case["W"])
+    ok = h["flags"] == 0
+    idx = idx.cpu().numpy()
+    assert np.array_equal(idx[ok], h["idx"][ok]) and ok.mean() > 0.9 and (h["idx"] >= 0).sum() > 100
+    # t-values from the reference's approximate reciprocal: within ATOL
+    m = (h["idx"] >= 0) & ok[..., None]
+    assert np.abs(t0.cpu().numpy()[m] - h["t0"][m]).max() <= ATOL
+    assert np.abs(vl.cpu().numpy()[..., 0][ok] - h["valid_len"][..., 0][ok]).max() <= 1e-4
+    S = case["c"]["S"]
+    rands = rng.random((B, n, S), dtype=np.float32)
+    si, sz = octree.ray_voxels_points_sampling_coarse(_t(h["idx"], torch.int32), _t(h["t0"]), _t(h["t1"]),
+                                                      _t(rands), _t(h["valid_len"]), 0, S)
+    si2, sz2, _ = orc.sample_coarse(r["tree"], h, rands, r["voxel_size"], S)
+    assert np.array_equal(si.cpu().numpy(), si2) and np.array_equal(sz.cpu().numpy(), sz2)
+
+
+def test_empty_scene_chain():
+    """Views with no valid depth: nothing is fused (TSDF 1, weight 0, no
+    occupied voxel), the tree is empty, every ray misses, every sample slot
+    is -1 and compositing gives zeros -- as the oracle."""
+    sc = syn.make_scene(seed=41, n_views=4, res=96, n_prims=6, D=64, trunc=0.03)
+    sc["depths"] = np.zeros_like(sc["depths"])
+    ori, dirs = syn.target_rays(seed=41, res=32)
+    S = 32
+    rands = np.full((1, ori.shape[1], S), 0.5, np.float32)
+    g = gpu_chain(sc, 64, 4, S, ori, dirs, rands, 256)
+    ref = orc.chain(sc, 64, 4, S, ori, dirs, rands, W=256, trunc_weight=sc["trunc_weight"])
+    assert (g["tsdf"] == 1).all() and (g["weight"] == 0).all() and (g["occ0"] == -1).all()
+    assert int(g["cnt0"].sum()) == 0 and g["counts"] == [0, 0]
+    for k in ("tsdf", "weight", "color"):
+        assert np.array_equal(g[k], ref["fusion"][k])
+    assert (g["idx"] == -1).all() and (g["si"] == -1).all() and (g["sz"] == -1).all()
+    assert np.array_equal(g["srt"], ref["sorted_z"]) and np.array_equal(g["sidx"], ref["sort_idx"])
+    R = ori.shape[1]
+    from sailor_gb300.dist import VoxelEncoding as VE
+    feats, d, ws, al = VE.volume_rendering_training_forward(_t(g["srt"]), _t(g["sidx"], torch.int32),
+                                                            torch.ones((1, R, S, 1), device="cuda"),
+                                                            torch.ones((1, R, S, 3), device="cuda"), 0, 1e-4, False)
+    for t in (feats, d, ws, al):
+        assert (t == 0).all()
+
+
 def test_sampling_given_oracle_hits(case):
     """Same hit lists in -> bit-identical samples out (counts, ids, depths)."""
     from sailor_gb300.dist import VoxelEncoding as VE  # noqa: F401
