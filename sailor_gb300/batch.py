@@ -36,6 +36,39 @@ import torch
 from . import _native as N
 
 
+def sample_capacity(S):
+    """Samples per ray of the training kernel that holds S samples (32 per
+    lane block: 32, 64 or 128)."""
+    return 32 if S <= 32 else (64 if S <= 64 else 128)
+
+
+def capacity_layout(targets):
+    """Ray layout of the targets (frame, n_rays, S), grouped by sample
+    capacity so that each group is one launch of the training kernel sized
+    for it.  Returns (order, ray_begin, ray_slices, groups): order lists the
+    targets in layout order (by capacity, then as given); ray_begin [T + 1]
+    the first ray of each target in that order (int64) and the total;
+    ray_slices[t] the (begin, end) rays of target t; groups the (first
+    segment, end segment, largest S) of each capacity group."""
+    T = len(targets)
+    order = sorted(range(T), key=lambda t: (sample_capacity(targets[t][2]), t))
+    seg_t = [targets[t] for t in order]
+    rb = np.concatenate([[0], np.cumsum([n for _, n, _ in seg_t])]).astype(np.int64)
+    if rb[-1] >= 2 ** 31:
+        raise ValueError("at most 2^31 - 1 rays per launch")
+    ray_slices = [None] * T
+    for i, t in enumerate(order):
+        ray_slices[t] = (int(rb[i]), int(rb[i + 1]))
+    groups = []
+    for i, (_, _, s_) in enumerate(seg_t):
+        if groups and sample_capacity(seg_t[groups[-1][0]][2]) == sample_capacity(s_):
+            g0, _, sm = groups[-1]
+            groups[-1] = (g0, i + 1, max(sm, s_))
+        else:
+            groups.append((i, i + 1, s_))
+    return order, rb, ray_slices, groups
+
+
 class BatchPipeline:
     def __init__(self, view_hw, targets, D=256, rate=8, C=16, W_hits=64, train_tsdf=False, target_widths=None,
                  device="cuda"):
@@ -110,29 +143,13 @@ class BatchPipeline:
         # segment tables list targets in the order self.order.
         self.targets = [(int(f), int(n), int(s)) for f, n, s in targets]
         T = len(self.targets)
-        cap = lambda s_: 32 if s_ <= 32 else (64 if s_ <= 64 else 128)  # noqa: E731
-        self.order = sorted(range(T), key=lambda t: (cap(self.targets[t][2]), t))
+        self.order, rb, self.ray_slices, self._groups = capacity_layout(self.targets)
         seg_t = [self.targets[t] for t in self.order]
-        counts = [n for _, n, _ in seg_t]
-        rb = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
-        if rb[-1] >= 2 ** 31:
-            raise ValueError("at most 2^31 - 1 rays per launch")
         self.R = R = int(rb[-1])
         self.S = S = max(s for _, _, s in self.targets)
-        self.ray_slices = [None] * T
-        for i, t in enumerate(self.order):
-            self.ray_slices[t] = (int(rb[i]), int(rb[i + 1]))
         self.seg_begin = torch.tensor(rb.astype(np.int32), **i32)
         self.seg_frame = torch.tensor([f for f, _, _ in seg_t], **i32)
         self.seg_samples = torch.tensor([s_ for _, _, s_ in seg_t], **i32)
-        # (first segment, end segment, largest S) of each capacity group
-        self._groups = []
-        for i, (_, _, s_) in enumerate(seg_t):
-            if self._groups and cap(seg_t[self._groups[-1][0]][2]) == cap(s_):
-                g0, _, sm = self._groups[-1]
-                self._groups[-1] = (g0, i + 1, max(sm, s_))
-            else:
-                self._groups.append((i, i + 1, s_))
         self.cameras = target_widths is not None
         if self.cameras:
             if len(target_widths) != T or any(n % int(w) for (_, n, _), w in zip(self.targets, target_widths)):
