@@ -164,7 +164,8 @@ int sg_tree_build_static(SgTree *tree, int *occ_top, int *occ_bot,
 
 /* Node table [n_nodes, 6] = (centre x, y, z, edge, valid, frame) per node
  * id.  Replaces MultiLayerOctree::output_all_nodes_tensor
- * (octree_kernel.cu:309-328, 699-717). */
+ * (octree_kernel.cu:309-328, 699-717).  n_nodes == 0 (an empty tree) is a
+ * no-op and out may then be NULL. */
 int sg_tree_nodes(const SgTree *tree, int n_nodes, float *out,
                   sg_stream_t stream);
 
@@ -213,7 +214,8 @@ int sg_sample_sorted(const SgTree *tree, const int *hit_idx,
 
 /* Per-row ascending sort of R rows of S floats (S <= 256); equal keys keep
  * their input order.  Replaces sort_samplings (sampling_kernel.cu:
- * 1308-1329, torch::sort along dim 2 + int cast). */
+ * 1308-1329, torch::sort along dim 2 + int cast).  R == 0 is a no-op and the
+ * buffers may then be NULL. */
 int sg_sort_samples(const float *z, int R, int S, float *sorted, int *idx,
                     sg_stream_t stream);
 
