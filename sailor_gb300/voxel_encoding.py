@@ -20,7 +20,8 @@ import torch
 
 from . import _native as N
 
-__all__ = ["rays_calculating", "integrate", "integrate_in_box", "build_multi_res_volumes", "volume_rendering_training_forward",
+__all__ = ["rays_calculating", "integrate", "get_origin_bbox", "integrate_in_box", "build_multi_res_volumes",
+           "volume_rendering_training_forward",
            "volume_rendering_training_backward", "volume_rendering_occ_forward", "MultiLayerOctree"]
 
 
@@ -107,6 +108,25 @@ def integrate(occupied_vol, num_occ_voxel, cam_intr, cam_pose, cam_R, cam_T, col
         out = integrate_in_box(occupied_vol, num_occ_voxel, cam_intr, cam_pose, color_ims, depth_ims, vol_bbox,
                                voxel_size, obs_weight, trunc_weight, tsdf_th_low, tsdf_th_high, device)
         return out[0], out[1], out[2], vol_origin, vol_bbox, voxel_size
+
+
+def get_origin_bbox(depth_ims, cam_intr, cam_R, cam_T, th_bbox, device):
+    """Bounding box [B, 3, 2] (min, max per axis) of the back-projected valid
+    depth pixels, widened by th_bbox: the reference's get_origin_bbox
+    (fusion_kernel.cu:473-534), the first steps of integrate."""
+    with _Dev(device, depth_ims, cam_intr, cam_R, cam_T):
+        depth = _in(depth_ims, "depth_ims")
+        B, Nv, H, W = depth.shape
+        K = _in(cam_intr, "cam_intr").view(B, Nv, 3, 3)
+        R = _in(cam_R, "cam_R").view(B, Nv, 3, 3)
+        T = _in(cam_T, "cam_T").view(B, Nv, 3)
+        vol_origin = torch.empty((B, 3, 2), device=depth.device)
+        vol_bbox = torch.empty((B, 3, 2), device=depth.device)  # the cubic box integrate goes on to take
+        voxel_size = torch.empty((B, 1), device=depth.device)
+        N.check(N.lib.sg_auto_bbox(N.ptr(depth), N.ptr(K), N.ptr(R), N.ptr(T), B, Nv, H, W, 2, float(th_bbox),
+                                   N.ptr(vol_origin), N.ptr(vol_bbox), N.ptr(voxel_size), N.stream()),
+                "origin bbox")
+        return vol_origin
 
 
 def integrate_in_box(occupied_vol, num_occ_voxel, cam_intr, cam_pose, color_ims, depth_ims, vol_bbox, voxel_size,

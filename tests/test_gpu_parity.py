@@ -573,6 +573,34 @@ def test_fusion_paths_bit_exact(obs, views, frac_colour):
     assert np.array_equal(occ.cpu().numpy(), ref["occ"])
 
 
+@pytest.mark.parametrize("seed,views,res", [(61, 4, 128), (62, 6, 96)])
+def test_integrate_auto_bbox_bit_exact(seed, views, res):
+    """integrate in the reference's own mode (the cubic box fitted to the
+    back-projected depth points, fusion_kernel.cu:51-184): camera inverses,
+    origin box, resized box, voxel size and the fused volumes, bit for bit
+    against the oracle; get_origin_bbox gives the same origin box."""
+    from sailor_gb300.dist import VoxelEncoding as VE
+    D = 64
+    sc = syn.make_scene(seed=seed, n_views=views, res=res, n_prims=8, D=D, trunc=0.03)
+    K, RT = sc["K"], sc["RT"]
+    R, T = RT[..., :3], RT[..., 3]
+    B = K.shape[0]
+    occ = torch.full((B, D, D, D), -1, dtype=torch.int32, device="cuda")
+    cnt = torch.zeros((B, 1), dtype=torch.int32, device="cuda")
+    masks = torch.ones(sc["depths"].shape, dtype=torch.int32, device="cuda")
+    ts, w, c, vo, vb, vs = VE.integrate(occ, cnt, _t(K), _t(RT), _t(R), _t(T), _t(sc["colors"]), _t(sc["depths"]),
+                                        masks, 1.0, 0.025, sc["trunc_weight"], 13.5, 13.5, 0)
+    rvo, rvb, rvs = orc.auto_bbox(sc["depths"], K, R, T, D, 0.025)
+    assert np.array_equal(vo.cpu().numpy(), rvo)
+    assert np.array_equal(vb.cpu().numpy(), rvb)
+    assert np.array_equal(vs.cpu().numpy().reshape(-1), rvs.reshape(-1))
+    ref = orc.integrate(K, RT, sc["colors"], sc["depths"], D, rvb, rvs, 1.0, sc["trunc_weight"], 13.5, 13.5)
+    assert np.array_equal(ts.cpu().numpy(), ref["tsdf"]) and np.array_equal(w.cpu().numpy(), ref["weight"])
+    assert np.array_equal(c.cpu().numpy(), ref["color"]) and np.array_equal(occ.cpu().numpy(), ref["occ"])
+    org = VE.get_origin_bbox(_t(sc["depths"]), _t(K), _t(R), _t(T), 0.025, 0)
+    assert torch.equal(org, vo)
+
+
 @pytest.mark.parametrize("D", [64, 72])
 def test_launch_shapes_do_not_change_results(D):
     """Every autotuner knob value gives bit-identical outputs (D = 72: the
