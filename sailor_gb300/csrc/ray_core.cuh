@@ -135,7 +135,8 @@ __device__ __forceinline__ int warp_sample_ray(const SampleParams &p, long r, in
 }
 
 // ---------------------------------------------------------------------------
-// per-ray sort: register bitonic network on (depth, position) keys
+// per-ray sort: register bitonic network on 32-bit depth keys; input
+// positions, where read, by ranking (warp_sort_ranked)
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t ordered_bits(float f) {
   uint32_t u = __float_as_uint(f);
@@ -146,7 +147,7 @@ __device__ __forceinline__ float from_ordered(uint32_t k) {
 }
 
 // E keys per lane in blocked order, element i = lane*E + e, P = 32*E (a
-// power of two); K is a 64-bit (depth, position) key or a 32-bit depth key.
+// power of two); K is an unsigned key type (here the 32-bit ordered depth).
 // Partner distances below E stay in the lane, so of the network's
 // log2(P)(log2(P)+1)/2 steps only those with distance >= E exchange across
 // lanes (15 of 28 at E = 4).
