@@ -28,7 +28,6 @@ back).  The per-step working set (> 10 GB) is far larger than L2.
 """
 import argparse
 import json
-import math
 import os
 import subprocess
 import sys

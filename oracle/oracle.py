@@ -5,7 +5,6 @@ Each method restates one reference operation of SAILOR's VoxelEncoding path
 Inputs are converted to contiguous float32/int32; outputs are new arrays.
 """
 import ctypes as C
-import os
 
 import numpy as np
 
