@@ -1,0 +1,124 @@
+"""Oracle (test infrastructure) for the occupancy MLP of SAILOR's FastNerf
+inference path: a numpy restatement of
+
+  density_feat_kernel   c_lib/FastNerf/src/infer_mlp.cu:120-199
+  density_sigma_kernel  infer_mlp.cu:202-240
+  infer_density_mlp     infer_mlp.cu:583-636 (the two kernels around a
+                        float32 mean over the views)
+
+with the reference's float16 arithmetic reproduced step for step: every
+layer starts from its bias and adds one weight x input product at a time
+with __hfma (a fused multiply-add rounded once to float16, round to nearest
+even), in the reference's loop order; ReLU is max(x, 0) on float16 values.
+The occupancy compositing that consumes the densities
+(volume_rendering_occ_kernel, infer_mlp.cu:508-580) is the pre-sorted
+occupancy mode of ``oracle.composite_fwd`` with C channels.
+
+Parity unpinned: the reference kernels have not yet been run to produce
+golden vectors for this restatement (``oracle/build.py --fastnerf`` compiles
+them to a cubin); the CPU tests pin the float16 arithmetic (``hfma`` against
+exact rational arithmetic) and the parameter layout.
+
+Parameter layout of the density network (one float16 vector, per layer the
+weights [out][in] row-major, then the bias [out]):
+  [0, 13696)       feature MLP 18 -> 64 -> 64 -> 64 -> 64 (ReLU after each)
+  [13696, 22081)   sigma MLP 64 -> 64 -> 64 -> 1 (ReLU, ReLU, sigmoid)
+  [22081, 22521)   geometry MLP 18 -> 16 -> 8 (ReLU after each)
+"""
+import numpy as np
+
+F16, F32, F64 = np.float16, np.float32, np.float64
+
+FEAT_LAYERS = ((18, 64), (64, 64), (64, 64), (64, 64))
+SIGMA_LAYERS = ((64, 64), (64, 64), (64, 1))
+GEO_LAYERS = ((18, 16), (16, 8))
+SIGMA_OFFSET = 13696  # infer_mlp.cu:125, 208
+GEO_OFFSET = 22081    # infer_mlp.cu:127
+PARAM_COUNT = GEO_OFFSET + 440
+
+
+def layer_sizes(layers):
+    return sum(i * o + o for i, o in layers)
+
+
+def hfma(a, b, c):
+    """a * b + c rounded once to float16 (__hfma), elementwise.
+
+    The float64 sum of the float16 product and addend is exact whenever the
+    result is finite in float16: a * b has at most 22 significant bits; if
+    |a * b + c| < 65520 then |a * b| < 2^17, so the sum's bits span at most
+    2^17 .. 2^-24 (41 bits).  Larger sums overflow to infinity either way.
+    One rounding of the exact float64 value to float16 (round to nearest
+    even) is therefore the fused operation's result."""
+    a, b, c = np.broadcast_arrays(np.asarray(a, F16), np.asarray(b, F16), np.asarray(c, F16))
+    with np.errstate(over="ignore", invalid="ignore"):
+        return (a.astype(F64) * b.astype(F64) + c.astype(F64)).astype(F16)
+
+
+def relu16(x):
+    """relu (infer_mlp.cu:42-45): max(float(x), 0) back to float16; NaN -> 0
+    as fmaxf gives."""
+    return np.fmax(x, F16(0)).astype(F16)
+
+
+def fc16(x, params, off, n_in, n_out):
+    """fc_layer (infer_mlp.cu:80-100) for points x [P, n_in] float16 with the
+    layer's parameters at params[off:]: out[i] = b[i], then
+    out[i] = hfma(W[i][j], x[j], out[i]) for j = 0 .. n_in-1."""
+    W = params[off:off + n_in * n_out].reshape(n_out, n_in)
+    b = params[off + n_in * n_out:off + n_in * n_out + n_out]
+    acc = np.broadcast_to(b, (x.shape[0], n_out)).astype(F16)
+    for j in range(n_in):
+        acc = hfma(W[None, :, j], x[:, j, None], acc)
+    return acc
+
+
+def _mlp(x, params, off, layers, last_relu=True):
+    for k, (n_in, n_out) in enumerate(layers):
+        x = fc16(x, params, off, n_in, n_out)
+        off += n_in * n_out + n_out
+        if last_relu or k + 1 < len(layers):
+            x = relu16(x)
+    return x
+
+
+def density_feat(points_z, points_tpsdf, feats_geo, params):
+    """density_feat_kernel: per point-view (z, t_psdf, 16 geometry features)
+    -> (64 density features, 8 geometry features), float32 outputs of the
+    float16 network.  Inputs [P], [P], [P, 16] float32."""
+    params = np.asarray(params, F16)
+    x = np.concatenate([np.asarray(points_z, F32).reshape(-1, 1), np.asarray(points_tpsdf, F32).reshape(-1, 1),
+                        np.asarray(feats_geo, F32).reshape(-1, 16)], axis=1).astype(F16)
+    dens = _mlp(x, params, 0, FEAT_LAYERS)
+    geo = _mlp(x, params, GEO_OFFSET, GEO_LAYERS)
+    return dens.astype(F32), geo.astype(F32)
+
+
+def sigmoid16(x):
+    """sigmoid (infer_mlp.cu:48-50): 1 / (1 + exp(-x)) in float32 from the
+    float16 input, rounded to float16 (exp evaluated in float64 and rounded
+    to float32; CUDA's expf is within 2 ulp of that)."""
+    xf = np.asarray(x, F16).astype(F32)
+    e = np.exp(-xf.astype(F64)).astype(F32)
+    return (F32(1.0) / (F32(1.0) + e)).astype(F16)
+
+
+def density_sigma(mean_feats, params):
+    """density_sigma_kernel: 64 mean density features [P, 64] float32 ->
+    density [P] float32 (the sigmoid of the float16 network's output)."""
+    params = np.asarray(params, F16)
+    x = np.asarray(mean_feats, F32).reshape(-1, 64).astype(F16)
+    y = _mlp(x, params, SIGMA_OFFSET, SIGMA_LAYERS, last_relu=False)
+    return sigmoid16(y[:, 0]).astype(F32)
+
+
+def infer_density(points_z, points_tpsdf, feats_geo, params, batch_size, num_points, num_views):
+    """infer_density_mlp: inputs [B, V, N, 1|16] (B batches, V views, N
+    points) -> densities [B, 1, N] float32.  The mean over views is the
+    float64 mean rounded to float32 (torch::mean in float32 may differ from
+    it by an ulp, which moves the float16 inputs of the sigma network only
+    at rounding boundaries)."""
+    B, V, N = batch_size, num_views, num_points
+    dens, geo = density_feat(points_z, points_tpsdf, feats_geo, params)
+    mean = dens.reshape(B, V, N, 64).astype(F64).mean(axis=1).astype(F32)
+    return density_sigma(mean.reshape(-1, 64), params).reshape(B, 1, N), geo.reshape(B, V, N, 8)
