@@ -122,3 +122,15 @@ def infer_density(points_z, points_tpsdf, feats_geo, params, batch_size, num_poi
     dens, geo = density_feat(points_z, points_tpsdf, feats_geo, params)
     mean = dens.reshape(B, V, N, 64).astype(F64).mean(axis=1).astype(F32)
     return density_sigma(mean.reshape(-1, 64), params).reshape(B, 1, N), geo.reshape(B, V, N, 8)
+
+
+def composite_occ(sorted_z, occ, feats, t_thres=1e-4):
+    """volume_rendering_occ_kernel (infer_mlp.cu:508-580): pre-sorted depths
+    [..., S], occupancies [..., S] used as alphas, features [..., S, C] ->
+    (features [..., C], depth [..., 1]) in float64; a ray whose last raw
+    depth is negative gives zeros.  The same restatement as the VoxelEncoding
+    occupancy compositing (oracle.composite_fwd, pre-sorted, occupancy mode)
+    with the features' own channel count (30 in FastNerf)."""
+    from . import oracle as orc
+    of, od, _, _, _ = orc.composite_fwd(sorted_z, None, occ, feats, t_thres, occ_mode=True)
+    return of, od

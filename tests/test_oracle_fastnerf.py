@@ -108,3 +108,32 @@ def test_density_network_against_float64():
     assert np.abs(dens.reshape(-1) - s64).max() < 2e-2
     assert np.abs(geo - g64).max() < 5e-2 * max(1.0, np.abs(g64).max())
     assert dens.std() > 1e-3  # the densities are not constant
+
+
+def test_occupancy_compositing_against_loop():
+    """The compositing restatement against a direct loop of the kernel's
+    steps, 30 channels, with padded, invalid and early-terminating rays."""
+    rng = np.random.default_rng(3)
+    R, S, C = 64, 24, 30
+    z = np.sort(rng.uniform(0.5, 3.0, (R, S)), axis=1).astype(np.float32)
+    z[:8, :5] = -1.0  # leading padding
+    z[8:12, -1] = -1.0  # last raw depth negative: an invalid ray
+    occ = rng.uniform(0.0, 0.6, (R, S)).astype(np.float32)
+    occ[12:16] = 0.999  # transmittance falls under the threshold early
+    feats = rng.normal(0, 1, (R, S, C)).astype(np.float32)
+    of, od = fn.composite_occ(z, occ, feats)
+    for r in range(R):
+        f = np.zeros(C)
+        d = 0.0
+        if z[r, -1] >= 0:
+            T = 1.0
+            for i in range(S):
+                if z[r, i] < 0:
+                    continue
+                w = float(occ[r, i]) * T
+                f += w * feats[r, i].astype(np.float64)
+                d += w * float(z[r, i])
+                T *= 1.0 - float(occ[r, i])
+                if T < 1e-4:
+                    break
+        assert np.abs(of[r] - f).max() <= 1e-5 and abs(od[r, 0] - d) <= 1e-5, r
