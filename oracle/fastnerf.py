@@ -114,13 +114,18 @@ def density_sigma(mean_feats, params):
 
 def infer_density(points_z, points_tpsdf, feats_geo, params, batch_size, num_points, num_views):
     """infer_density_mlp: inputs [B, V, N, 1|16] (B batches, V views, N
-    points) -> densities [B, 1, N] float32.  The mean over views is the
-    float64 mean rounded to float32 (torch::mean in float32 may differ from
-    it by an ulp, which moves the float16 inputs of the sigma network only
-    at rounding boundaries)."""
+    points) -> densities [B, 1, N] float32.  The mean over the views is
+    taken as torch's float32 reduction does it for a short axis: a float32
+    sum in view order, times float32(1 / V); another summation order moves
+    a mean by a float32 ulp, which changes the float16 input of the sigma
+    network only next to a float16 rounding boundary."""
     B, V, N = batch_size, num_views, num_points
     dens, geo = density_feat(points_z, points_tpsdf, feats_geo, params)
-    mean = dens.reshape(B, V, N, 64).astype(F64).mean(axis=1).astype(F32)
+    per_view = dens.reshape(B, V, N, 64)
+    acc = np.zeros((B, N, 64), F32)
+    for v in range(V):
+        acc = (acc + per_view[:, v]).astype(F32)
+    mean = (acc * F32(1.0 / V)).astype(F32)
     return density_sigma(mean.reshape(-1, 64), params).reshape(B, 1, N), geo.reshape(B, V, N, 8)
 
 

@@ -56,9 +56,23 @@ _NAMES = {
 }
 
 
+# FastNerf inference kernels (c_lib/FastNerf/src/infer_mlp.cu), built on
+# request only (oracle/build.py --fastnerf): looked up apart from the
+# VoxelEncoding kernels so that available() does not wait for them
+_NERF_NAMES = {
+    "nerf_density_feat": ("infer_mlp", "19density_feat_kernel"),
+    "nerf_density_sigma": ("infer_mlp", "20density_sigma_kernel"),
+}
+_NAMES.update(_NERF_NAMES)
+
+
+def nerf_available():
+    return os.path.exists(os.path.join(REF_DIR, "infer_mlp.cubin")) and torch.cuda.is_available()
+
+
 def available():
     return all(os.path.exists(os.path.join(REF_DIR, m + ".cubin"))
-               for m, _ in _NAMES.values()) and torch.cuda.is_available()
+               for k, (m, _) in _NAMES.items() if k not in _NERF_NAMES) and torch.cuda.is_available()
 
 
 class _Driver:
@@ -348,3 +362,26 @@ def rays_calculating(K, R, T, load_size):
                                                      u32(load_size)])
     torch.cuda.synchronize()
     return dict(rays=out, Kinv=kinv, Rinv=rinv)
+
+
+def infer_density_mlp(points_z, points_tpsdf, feats_geo, params, batch_size, num_points, num_views):
+    """infer_density_mlp (infer_mlp.cu:583-636): density_feat_kernel over
+    the B*V*N point-views, the float32 mean of the 64 density features over
+    the views, density_sigma_kernel over the B*N points (256-thread CTAs, as
+    the reference launches them).  params: the float16 parameter vector.
+    Returns (densities [B, 1, N], geometry features [B, V, N, 8])."""
+    d = driver()
+    B, N, V = batch_size, num_points, num_views
+    nv = B * V * N
+    z = _dev(np.reshape(points_z, -1), torch.float32)
+    tp = _dev(np.reshape(points_tpsdf, -1), torch.float32)
+    g = _dev(np.reshape(feats_geo, (-1, 16)), torch.float32)
+    w = _dev(np.asarray(params, np.float16), torch.float16)
+    dens = torch.empty((nv, 64), device="cuda")
+    geo = torch.empty((nv, 8), device="cuda")
+    d.launch("nerf_density_feat", nv, [w, z, tp, g, i32(nv), dens, geo], block=256)
+    mean = dens.view(B, V, N, 64).mean(1).reshape(B * N, 64).contiguous()
+    out = torch.empty((B * N, 1), device="cuda")
+    d.launch("nerf_density_sigma", B * N, [w, mean, i32(B * N), out], block=256)
+    torch.cuda.synchronize()
+    return out.view(B, 1, N), geo.view(B, V, N, 8)

@@ -8,7 +8,9 @@ they lie; this script only loads the cubins):
 
 It writes ``ref_chain_explicit.npz``, ``ref_chain_auto.npz``,
 ``ref_composite.npz``, ``ref_rays.npz`` and ``ref_project.npz`` (``--only rays`` or
-``--only project``: that one alone).  Each holds the seeded inputs
+``--only project``: that one alone; ``--only density_mlp`` writes
+``ref_density_mlp.npz`` from FastNerf's occupancy MLP, whose cubin
+``oracle/build.py --fastnerf`` builds).  Each holds the seeded inputs
 and the reference outputs of fusion, coarse occupancy, the two-level tree
 (as canonical node keys, since the reference's node ids depend on atomic
 ordering), the voxel traversal, the coarse sampling, the sort, compositing
@@ -178,12 +180,34 @@ def project(out_dir):
     print("project done: nodes", used.size, flush=True)
 
 
+def density_mlp(out_dir):
+    """FastNerf's occupancy MLP (infer_density_mlp) on seeded inputs and
+    float16 weights -> ref_density_mlp.npz (needs oracle/build.py
+    --fastnerf)."""
+    assert rc.nerf_available(), "FastNerf cubin or GPU missing"
+    rng = np.random.default_rng(23)
+    B, V, N = 1, 3, 512
+    from oracle import fastnerf as fn
+    params = (rng.normal(0, 1, fn.PARAM_COUNT) * 0.15).astype(np.float16)
+    z = rng.uniform(0.5, 3.0, (B, V, N, 1)).astype(np.float32)
+    tp = rng.uniform(-1.0, 1.0, (B, V, N, 1)).astype(np.float32)
+    g = rng.normal(0, 0.5, (B, V, N, 16)).astype(np.float32)
+    dens, geo = rc.infer_density_mlp(z, tp, g, params, B, N, V)
+    np.savez_compressed(os.path.join(out_dir, "ref_density_mlp.npz"), params=params, points_z=z, points_tpsdf=tp,
+                        feats_geo=g, density=dens.cpu().numpy(), geo_feats=geo.cpu().numpy(),
+                        shape=np.array([B, V, N], np.int32))
+    print("density_mlp done", flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
-    ap.add_argument("--only", choices=["rays", "project"])
+    ap.add_argument("--only", choices=["rays", "project", "density_mlp"])
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
+    if args.only == "density_mlp":
+        density_mlp(args.out)
+        return
     assert rc.available(), "reference cubins or GPU missing"
     if args.only == "project":
         project(args.out)

@@ -2,9 +2,11 @@
 (oracle/fastnerf.py): __hfma's single rounding against exact rational
 arithmetic, the parameter layout, and the network against a float64
 evaluation of the same weights."""
+import os
 from fractions import Fraction
 
 import numpy as np
+import pytest
 
 from oracle import fastnerf as fn
 
@@ -137,3 +139,23 @@ def test_occupancy_compositing_against_loop():
                 if T < 1e-4:
                     break
         assert np.abs(of[r] - f).max() <= 1e-5 and abs(od[r, 0] - d) <= 1e-5, r
+
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_density_mlp.npz")
+
+
+@pytest.mark.skipif(not os.path.exists(GOLDEN), reason="no golden vectors of the reference MLP yet")
+def test_density_mlp_against_reference_golden():
+    """Pin: the restatement against the reference kernels' outputs: the
+    geometry features (float16 network, no mean) bit for bit; the densities
+    within one float16 ulp for nearly all points and within 2e-2 for all
+    (CUDA's expf, and a view mean summed in another order, can move a value
+    across a float16 rounding boundary, and the sigma network carries that
+    on)."""
+    g = np.load(GOLDEN)
+    B, V, N = (int(x) for x in g["shape"])
+    dens, geo = fn.infer_density(g["points_z"], g["points_tpsdf"], g["feats_geo"], g["params"], B, N, V)
+    assert np.array_equal(geo, g["geo_feats"])
+    d16, r16 = dens.astype(F16), g["density"].astype(F16)
+    ulps = np.abs(d16.view(np.int16).astype(np.int32) - r16.view(np.int16).astype(np.int32))
+    assert (ulps <= 1).mean() > 0.99 and np.abs(dens - g["density"]).max() < 2e-2
