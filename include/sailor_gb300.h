@@ -154,11 +154,13 @@ int sg_tree_build(SgTree *tree, int *occ_top, int *occ_bot, void *scratch,
  * and thrust.
  * Returns SG_ERR_CAPACITY, and launches nothing, when
  * sg_tree_scratch_bytes(B, Dt) > SG_TREE_STATIC_SCRATCH_BYTES.  Allocates
- * nothing.  The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) and caches it: make that call before any stream
- * capture on the device.  All calls on a device share the array, so calls
- * that overlap on the GPU race; order them on one stream.  Nothing in the
- * array needs clearing between calls. */
+ * nothing.  Every call looks up the array's device address
+ * (cudaGetSymbolAddress) in the context current at the call, so a device
+ * reset or a caller-made context never leaves it a stale address; the first
+ * call in a context may load the library's device code, so make it before
+ * any stream capture on the device.  All calls in a context share the array,
+ * so calls that overlap on the GPU race; order them on one stream.  Nothing
+ * in the array needs clearing between calls. */
 int sg_tree_build_static(SgTree *tree, int *occ_top, int *occ_bot,
                          SgStatus *status, sg_stream_t stream);
 

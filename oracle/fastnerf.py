@@ -44,12 +44,21 @@ def layer_sizes(layers):
 def hfma(a, b, c):
     """a * b + c rounded once to float16 (__hfma), elementwise.
 
-    The float64 sum of the float16 product and addend is exact whenever the
-    result is finite in float16: a * b has at most 22 significant bits; if
-    |a * b + c| < 65520 then |a * b| < 2^17, so the sum's bits span at most
-    2^17 .. 2^-24 (41 bits).  Larger sums overflow to infinity either way.
-    One rounding of the exact float64 value to float16 (round to nearest
-    even) is therefore the fused operation's result."""
+    The product p = a * b of two float16 values has at most 22 significant
+    bits between 2^32 and 2^-48, so it is exact in float64.  The float64 sum
+    s = fl64(p + c) is then the only extra rounding, and it never changes
+    the float16 result:
+    - If s is exact, rounding it to float16 is the fused operation.
+    - s is inexact only when the exact x = p + c spans more than 53 bits.
+      With |p| >= |c| that needs |p| >= 2^29 (c's last bit is >= 2^-24), and
+      x overflows float16 either way.  With |c| > |p| it needs p's last bit
+      (>= |p| 2^-21) below 2^-52 |c|, so |p| < 2^-30 |c|: x lies within
+      2^-30 |c| of the float16 value c, while every float16 rounding
+      midpoint is at least 2^-12 |c| from c (half an ulp of the binade below
+      c's).  The float64 error, at most 2^-52 |c|, cannot carry x across a
+      midpoint or onto one.
+    So one rounding of s to float16 (nearest, ties to even) gives the fused
+    operation's result, subnormal operands included."""
     a, b, c = np.broadcast_arrays(np.asarray(a, F16), np.asarray(b, F16), np.asarray(c, F16))
     with np.errstate(over="ignore", invalid="ignore"):
         return (a.astype(F64) * b.astype(F64) + c.astype(F64)).astype(F16)

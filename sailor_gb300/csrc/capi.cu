@@ -1,4 +1,6 @@
 // capi.cu -- status strings and version of the C ABI (include/sailor_gb300.h).
+#include <atomic>
+
 #include "common.cuh"
 
 extern "C" const char *sg_status_string(int status) {
@@ -18,9 +20,32 @@ extern "C" int sg_version(void) { return 100; }
 // launch-shape knobs
 // ---------------------------------------------------------------------------
 namespace sg {
-static int g_tune[SG_TUNE_COUNT] = {4, 128, 64, 64, 1};
+// Process-wide: a value set by one thread is seen by launches of every
+// thread after the store (relaxed atomics: each knob is independent).
+static std::atomic<int> g_tune[SG_TUNE_COUNT] = {4, 128, 64, 64, 1};
 
-int tune(int knob) { return (knob >= 0 && knob < SG_TUNE_COUNT) ? g_tune[knob] : 0; }
+int tune(int knob) {
+  return (knob >= 0 && knob < SG_TUNE_COUNT) ? g_tune[knob].load(std::memory_order_relaxed) : 0;
+}
+
+namespace {
+constexpr int kMaxDevices = 64;
+constexpr int kSmsUnknown = 128;  // only when the runtime cannot name the device (the launch fails anyway)
+std::atomic<int> g_sms[kMaxDevices] = {};
+}  // namespace
+
+int num_sms() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return kSmsUnknown;
+  if (dev < kMaxDevices) {
+    const int c = g_sms[dev].load(std::memory_order_relaxed);
+    if (c > 0) return c;
+  }
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) return kSmsUnknown;
+  if (dev < kMaxDevices) g_sms[dev].store(n, std::memory_order_relaxed);
+  return n;
+}
 }  // namespace sg
 
 extern "C" int sg_tune_set(int knob, int value) {
@@ -43,7 +68,7 @@ extern "C" int sg_tune_set(int knob, int value) {
     default:
       return SG_ERR_INVALID_ARG;
   }
-  sg::g_tune[knob] = value;
+  sg::g_tune[knob].store(value, std::memory_order_relaxed);
   return SG_OK;
 }
 

@@ -187,6 +187,11 @@ __device__ __forceinline__ void status_or(SgStatus *st, int f) {
 // launch-shape knobs (sg_tune_set / sg_tune_get, capi.cu)
 int tune(int knob);
 
+// Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount,
+// looked up once per device; capi.cu).  Grid caps of the grid-stride kernels
+// are multiples of it.
+int num_sms();
+
 // ---------------------------------------------------------------------------
 // ray generation (rays_calculating_kernel, sampling_kernel.cu:411-486)
 // ---------------------------------------------------------------------------

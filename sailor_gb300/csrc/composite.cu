@@ -310,7 +310,7 @@ __global__ void __launch_bounds__(256) composite_bwd_kernel(CompParams p) {
 template <int CT>
 int launch_comp(const CompParams &p, bool bwd, int E, sg_stream_t stream) {
   int g = ceil_div(p.R * 32, 256);
-  if (g > 152 * 64) g = 152 * 64;
+  if (g > num_sms() * 64) g = num_sms() * 64;
 #define SG_CASE(EE)                                                              \
   case EE:                                                                       \
     if (bwd) composite_bwd_kernel<EE, CT><<<g, 256, 0, stream>>>(p);             \

@@ -215,7 +215,7 @@ extern "C" int sg_grid_gather(const float *ori, const float *dir, const float *z
   GatherParams p{ori, dir, z, (long)B * N, N, S, grid, D, C, vol_bbox, voxel_size, mode, scale, s, out};
   long n = (long)B * N * S;
   int g = ceil_div(n, 256);
-  if (g > 152 * 64) g = 152 * 64;
+  if (g > num_sms() * 64) g = num_sms() * 64;
   switch (C) {
     case 1: grid_gather_kernel<1><<<g, 256, 0, stream>>>(p); break;
     case 3: grid_gather_kernel<3><<<g, 256, 0, stream>>>(p); break;
@@ -240,7 +240,7 @@ extern "C" int sg_grid_scatter(const float *ori, const float *dir, const float *
                   grad_grid};
   long R = (long)B * N;
   int g = ceil_div(R * 32, 256);
-  if (g > 152 * 32) g = 152 * 32;
+  if (g > num_sms() * 32) g = num_sms() * 32;
   switch (C) {
     case 1: grid_scatter_kernel<1><<<g, 256, 0, stream>>>(p); break;
     case 3: grid_scatter_kernel<3><<<g, 256, 0, stream>>>(p); break;

@@ -264,7 +264,7 @@ extern "C" int sg_intersect(const SgTree *tree, const float *ori, const float *d
   intersect_kernel<<<ceil_div(R, blk), blk, 0, stream>>>(p);
   if (padded) {
     int g = ceil_div(R * 32, 256);
-    if (g > 152 * 64) g = 152 * 64;
+    if (g > num_sms() * 64) g = num_sms() * 64;
     pad_rows_kernel<<<g, 256, 0, stream>>>(R, W, hit_count, hit_idx, hit_t0, hit_t1);
   }
   SG_LAUNCH_CHECK();

@@ -405,7 +405,7 @@ extern "C" int sg_project_sampled_xyz(const SgTree *tree, const float *ray_ori, 
   p.xy = proj_xy;
   p.pz = proj_z;
   long g = (total + 255) / 256;
-  if (g > 152L * 64) g = 152L * 64;
+  if (g > (long)num_sms() * 64) g = (long)num_sms() * 64;
   project_sampled_kernel<<<(int)g, 256, 0, stream>>>(p);
   SG_LAUNCH_CHECK();
   return SG_OK;
@@ -475,7 +475,7 @@ extern "C" int sg_project_gather(const SgProjGather *a, sg_stream_t stream) {
   if (total == 0) return SG_OK;
   if (total > (1L << 40)) return SG_ERR_UNSUPPORTED;
   long g = (total + 255) / 256;
-  if (g > 152L * 64) g = 152L * 64;
+  if (g > (long)num_sms() * 64) g = (long)num_sms() * 64;
   project_gather_kernel<<<(int)g, 256, 0, stream>>>(p);
   SG_LAUNCH_CHECK();
   return SG_OK;

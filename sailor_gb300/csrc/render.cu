@@ -535,7 +535,7 @@ __global__ void __launch_bounds__(256, kBwdMinBlocks<E, TRAIN>) render_bwd_kerne
 
 static int render_grid(long R) {
   long g = (R * 32 + 255) / 256;
-  const long cap = 152L * tune(SG_TUNE_RENDER_WARPS);
+  const long cap = (long)num_sms() * tune(SG_TUNE_RENDER_WARPS);
   return (int)(g < cap ? g : cap);
 }
 

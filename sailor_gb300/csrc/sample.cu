@@ -147,7 +147,7 @@ using namespace sg;
 
 static int grid_for(long R) {
   int g = ceil_div(R * 32, 256);
-  return g > 152 * 64 ? 152 * 64 : g;
+  return g > num_sms() * 64 ? num_sms() * 64 : g;
 }
 
 extern "C" int sg_sample_sorted(const SgTree *tree, const int *hit_idx, const float *hit_t0,

@@ -339,7 +339,7 @@ extern "C" int sg_tree_nodes(const SgTree *tree, int n_nodes, float *out, sg_str
   if (n_nodes == 0) return SG_OK;  // an empty tree: nothing to write (out may be NULL)
   if (!out) return SG_ERR_INVALID_ARG;
   int g = ceil_div(n_nodes, 256);
-  if (g > 152 * 32) g = 152 * 32;
+  if (g > num_sms() * 32) g = num_sms() * 32;
   tree_nodes_kernel<<<g, 256, 0, stream>>>(*tree, n_nodes, out);
   SG_LAUNCH_CHECK();
   return SG_OK;
@@ -368,30 +368,46 @@ extern "C" size_t sg_tree_scratch_bytes(int B, int Dt) {
   return total;
 }
 
-extern "C" int sg_tree_build(SgTree *tree, int *occ_top, int *occ_bot, void *scratch, size_t scratch_bytes,
-                             SgStatus *status, sg_stream_t stream) {
-  if (!tree || !occ_top || !occ_bot || !scratch) return SG_ERR_INVALID_ARG;
-  SgTree t = *tree;
+namespace sg {
+// Argument checks shared by sg_tree_build and sg_tree_build_static.
+static int check_tree_args(const SgTree *tree, const int *occ_top, const int *occ_bot) {
+  if (!tree || !occ_top || !occ_bot) return SG_ERR_INVALID_ARG;
+  const SgTree &t = *tree;
   if (t.B <= 0 || t.Dt <= 0 || t.rate <= 0 || t.Db != t.Dt * t.rate) return SG_ERR_INVALID_ARG;
   if (!t.brick_node || !t.brick_mask || !t.top_key || !t.top_child_base || !t.bot_key || !t.bot_parent ||
       !t.counts)
     return SG_ERR_INVALID_ARG;
   if (t.rate * t.rate * t.rate > 4096) return SG_ERR_UNSUPPORTED;
-  if (scratch_bytes < sg_tree_scratch_bytes(t.B, t.Dt)) return SG_ERR_INVALID_ARG;
+  return SG_OK;
+}
+
+// The five launches of a tree build (classify, tile sums, tile scan, top
+// nodes, children) over scratch of at least sg_tree_scratch_bytes(B, Dt).
+static int launch_tree_build(const SgTree &t, int *occ_top, int *occ_bot, char *scratch, SgStatus *status,
+                             sg_stream_t stream) {
   TreeScratch s;
-  scratch_layout(t.B, t.Dt, (char *)scratch, &s, nullptr);
+  scratch_layout(t.B, t.Dt, scratch, &s, nullptr);
   long nb = (long)t.B * t.Dt * t.Dt * t.Dt;
   int ntiles = ceil_div(nb, kTile);
   int mw = sg_mask_words(t.rate);
   int gw = ceil_div(nb * 32, 256);
-  if (gw > 152 * 64) gw = 152 * 64;
+  if (gw > num_sms() * 64) gw = num_sms() * 64;
   tree_classify_kernel<<<gw, 256, 0, stream>>>(t, occ_top, occ_bot, s, mw);
   tree_tile_sum_kernel<<<ntiles, 256, 0, stream>>>(s, nb);
   tree_tile_scan_kernel<<<1, 1024, 0, stream>>>(s, ntiles, t, status);
   tree_emit_top_kernel<<<ntiles, 256, 0, stream>>>(t, occ_top, s, nb);
-  tree_emit_children_kernel<<<152 * 8, 256, 0, stream>>>(t, occ_bot, mw);
+  tree_emit_children_kernel<<<num_sms() * 8, 256, 0, stream>>>(t, occ_bot, mw);
   SG_LAUNCH_CHECK();
   return SG_OK;
+}
+}  // namespace sg
+
+extern "C" int sg_tree_build(SgTree *tree, int *occ_top, int *occ_bot, void *scratch, size_t scratch_bytes,
+                             SgStatus *status, sg_stream_t stream) {
+  const int rc = check_tree_args(tree, occ_top, occ_bot);
+  if (rc != SG_OK) return rc;
+  if (!scratch || scratch_bytes < sg_tree_scratch_bytes(tree->B, tree->Dt)) return SG_ERR_INVALID_ARG;
+  return launch_tree_build(*tree, occ_top, occ_bot, (char *)scratch, status, stream);
 }
 
 // ---------------------------------------------------------------------------
@@ -410,61 +426,28 @@ extern "C" int sg_tree_build(SgTree *tree, int *occ_top, int *occ_bot, void *scr
 // The array is SG_TREE_STATIC_SCRATCH_BYTES (8 MiB) of device memory that every
 // GPU which loads the library holds until the process exits.  In host code
 // g_tree_static_scratch is only a host-side stand-in for the device array, so
-// its device address is looked up with cudaGetSymbolAddress -- once per
-// device, on the first call made with that device current, and cached.  Make
-// that first call before any stream capture on the device.
+// its device address is looked up with cudaGetSymbolAddress on every call,
+// with the caller's device and context current.  Nothing is cached: after a
+// cudaDeviceReset, or under a context the caller created and made current
+// itself, the lookup gives the array of the context that is current now
+// (a pointer kept from an earlier context would name freed or foreign
+// memory).  The first call in a context may load the library's device code
+// into it; make that first call before any stream capture on the device.
 //
-// Every call shares the one array per device, and the array keeps what the
+// Every call shares the one array per context, and the array keeps what the
 // last call left in it.  Nothing here needs zeroing first: every scratch word
 // a call reads was written earlier in the same call.  Calls whose work
 // overlaps on the GPU (different streams, no ordering between them) race on
 // the array and produce wrong trees; order them on one stream or with events.
 // ---------------------------------------------------------------------------
-#include <mutex>
-
 static __device__ __align__(256) unsigned char g_tree_static_scratch[SG_TREE_STATIC_SCRATCH_BYTES];
-
-namespace {
-constexpr int kMaxStaticDevices = 64;
-std::mutex g_static_mu;
-void *g_static_ptr[kMaxStaticDevices] = {};
-}  // namespace
 
 extern "C" int sg_tree_build_static(SgTree *tree, int *occ_top, int *occ_bot, SgStatus *status,
                                     sg_stream_t stream) {
-  if (!tree || !occ_top || !occ_bot) return SG_ERR_INVALID_ARG;
-  SgTree t = *tree;
-  if (t.B <= 0 || t.Dt <= 0 || t.rate <= 0 || t.Db != t.Dt * t.rate) return SG_ERR_INVALID_ARG;
-  if (!t.brick_node || !t.brick_mask || !t.top_key || !t.top_child_base || !t.bot_key || !t.bot_parent ||
-      !t.counts)
-    return SG_ERR_INVALID_ARG;
-  if (t.rate * t.rate * t.rate > 4096) return SG_ERR_UNSUPPORTED;
-  if (sg_tree_scratch_bytes(t.B, t.Dt) > (size_t)SG_TREE_STATIC_SCRATCH_BYTES) return SG_ERR_CAPACITY;
-  int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess) return SG_ERR_CUDA;
-  if (dev < 0 || dev >= kMaxStaticDevices) return SG_ERR_UNSUPPORTED;
+  const int rc = check_tree_args(tree, occ_top, occ_bot);
+  if (rc != SG_OK) return rc;
+  if (sg_tree_scratch_bytes(tree->B, tree->Dt) > (size_t)SG_TREE_STATIC_SCRATCH_BYTES) return SG_ERR_CAPACITY;
   void *base = nullptr;
-  {
-    std::lock_guard<std::mutex> lock(g_static_mu);
-    if (!g_static_ptr[dev]) {
-      void *p = nullptr;
-      if (cudaGetSymbolAddress(&p, g_tree_static_scratch) != cudaSuccess || !p) return SG_ERR_CUDA;
-      g_static_ptr[dev] = p;
-    }
-    base = g_static_ptr[dev];
-  }
-  TreeScratch s;
-  scratch_layout(t.B, t.Dt, (char *)base, &s, nullptr);
-  long nb = (long)t.B * t.Dt * t.Dt * t.Dt;
-  int ntiles = ceil_div(nb, kTile);
-  int mw = sg_mask_words(t.rate);
-  int gw = ceil_div(nb * 32, 256);
-  if (gw > 152 * 64) gw = 152 * 64;
-  tree_classify_kernel<<<gw, 256, 0, stream>>>(t, occ_top, occ_bot, s, mw);
-  tree_tile_sum_kernel<<<ntiles, 256, 0, stream>>>(s, nb);
-  tree_tile_scan_kernel<<<1, 1024, 0, stream>>>(s, ntiles, t, status);
-  tree_emit_top_kernel<<<ntiles, 256, 0, stream>>>(t, occ_top, s, nb);
-  tree_emit_children_kernel<<<152 * 8, 256, 0, stream>>>(t, occ_bot, mw);
-  SG_LAUNCH_CHECK();
-  return SG_OK;
+  if (cudaGetSymbolAddress(&base, g_tree_static_scratch) != cudaSuccess || !base) return SG_ERR_CUDA;
+  return launch_tree_build(*tree, occ_top, occ_bot, (char *)base, status, stream);
 }

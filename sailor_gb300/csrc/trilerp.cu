@@ -119,7 +119,7 @@ static int tri_launch(const SgTree *tree, const float *ori, const float *dir, co
   TriParams p{*tree, ori, dir, z, idx, feats, gout, out, gin, N, S, C};
   long n = (long)tree->B * C * N * S;
   int g = ceil_div(n, 256);
-  if (g > 152 * 64) g = 152 * 64;
+  if (g > num_sms() * 64) g = num_sms() * 64;
   if (bwd) trilerp_nodes_bwd_kernel<<<g, 256, 0, stream>>>(p);
   else trilerp_nodes_fwd_kernel<<<g, 256, 0, stream>>>(p);
   SG_LAUNCH_CHECK();

@@ -54,6 +54,27 @@ def test_hfma_single_rounding():
         assert got[i] == want or (got[i] == 0 and want == 0), (i, a[i], b[i], c[i], got[i], want)
 
 
+def test_hfma_subnormal_operands():
+    """Products of float16 subnormals reach 2^-48, so the float64 sum with a
+    large addend is inexact; the float16 result must still equal the single
+    rounding of the exact rational value."""
+    rng = np.random.default_rng(1)
+    n = 3000
+    sub = lambda k: (rng.integers(1, 1024, k) * 2.0 ** -24 * rng.choice([-1.0, 1.0], k)).astype(F16)  # noqa: E731
+    a, b = sub(n), rng.normal(0, 1, n).astype(F16)
+    b[:1000] = sub(1000)                                        # subnormal x subnormal
+    c = (rng.uniform(64.0, 60000.0, n) * rng.choice([-1.0, 1.0], n)).astype(F16)
+    c[1000:1500] = (F16(1.0) + F16(2.0 ** -10)) * F16(2.0 ** 10)  # c on a float16 value next to a midpoint
+    c[1500:2000] = sub(500)                                     # small addends, exact sums
+    c[2000:2500] = F16(65504.0)                                 # the largest finite value
+    got = fn.hfma(a, b, c)
+    for i in range(n):
+        q = Fraction(float(a[i])) * Fraction(float(b[i])) + Fraction(float(c[i]))
+        want = _round_half_exact(q)
+        assert got[i] == want or (got[i] == 0 and want == 0), (i, a[i], b[i], c[i], got[i], want)
+    assert np.any(np.abs(a.astype(np.float64) * b) < 2.0 ** -40)  # inexact float64 sums occur
+
+
 def test_hfma_rounds_once():
     # (1 + 2^-10)^2 = 1 + 2^-9 + 2^-20; with c = -2^-9 the exact 1 + 2^-20
     # lies below the midpoint 1 + 2^-11 (rounds to 1), with
