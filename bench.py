@@ -56,9 +56,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="small configuration (256^3, 512^2) for profiling")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
-    ap.add_argument("--workload", default="batch", choices=["batch", "plain", "project"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "plain", "project", "diff"])
     ap.add_argument("--unfused", action="store_true",
                     help="render with four kernels (sample+sort, two field gathers, composite) instead of one")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the oracle parity check of the timed step (run after timing)")
     return ap.parse_args()
 
 
@@ -305,8 +307,10 @@ def near_node_bricks(bp):
     return int(torch.nn.functional.max_pool3d(m, 3, stride=1, padding=1).sum().item())
 
 
-def batch_algorithmic_bytes(bcfg, w, n_hits, R, n_samples, n_clear_bricks=None):
-    """Per-launch algorithmic HBM bytes of each batched stage."""
+def batch_algorithmic_bytes(bcfg, w, n_hits, R, n_samples, n_clear_bricks=None, n_touched=0):
+    """Per-launch algorithmic HBM bytes of each batched stage.  n_touched:
+    voxels whose feature cells the samples tap (read once: 4 C bytes of
+    features and 4 of TSDF; the gradient written once: 4 C bytes)."""
     B, D, C = bcfg["frames"], bcfg["D"], bcfg["C"]
     V, Vt = B * D ** 3, B * (D // bcfg["rate"]) ** 3
     n_pix = sum(d.size for fr in w["frames"] for d in fr["depth"])
@@ -318,9 +322,9 @@ def batch_algorithmic_bytes(bcfg, w, n_hits, R, n_samples, n_clear_bricks=None):
         intersect=24 * R + 24 * R + 12 * n_hits + 8 * R,
         forward=24 * R + 12 * n_hits + 8 * R + 24 * R,  # rays, hit rows, count + valid length in; 24 B/ray out
         # fused training pass: as forward, with the target colour in and the
-        # per-ray loss out; the atomic adds into the feature-gradient grid
-        # are not counted
-        train=24 * R + 12 * n_hits + 8 * R + 12 * R + 24 * R + 4 * R,
+        # per-ray loss out, plus the touched cells of the TSDF and feature
+        # grids read once and the feature-gradient cells written once
+        train=24 * R + 12 * n_hits + 8 * R + 12 * R + 24 * R + 4 * R + n_touched * (4 * C + 4 + 4 * C),
         # clear of the feature-gradient grid near the previous pass's nodes
         # (side stream, beside fusion): 4 C bytes per voxel of those bricks
         zero_grad=4 * C * bcfg["rate"] ** 3 * (n_clear_bricks if n_clear_bricks is not None else Vt),
@@ -378,6 +382,252 @@ def cpu_baseline_batch(w, bcfg, feat, head, ray_sample=2048, fusion_slab=8, fz=N
                         f"traversal/sampling/sort/field taps/compositing forward and backward + grid scatter "
                         f"of {ray_sample} rays of target 0 scaled to {R} rays"),
                 stage_s=dict(fusion=t_fuse, tree=t_tree, render=t_render))
+
+
+# ---------------------------------------------------------------------------
+# parity of the batched step against the oracle (after timing; the oracle is
+# the checker here, never part of a timed region)
+# ---------------------------------------------------------------------------
+def _oracle_frames(w, bcfg):
+    """Oracle fusion + coarse occupancy + tree of every frame (C port)."""
+    from oracle import oracle as orc
+    out = []
+    for b, fr in enumerate(w["frames"]):
+        K, RT, dep, col = padded_views(fr)
+        fz = orc.integrate(K, RT, col, dep, bcfg["D"], w["vol_bbox"][b:b + 1], w["voxel_size"][b:b + 1].reshape(1, 1),
+                           trunc_weight=w["trunc_weight"])
+        top, _ = orc.merge(fz["occ"], bcfg["rate"])
+        out.append(dict(fusion=fz, tree=orc.build_tree(top, fz["occ"])))
+    return out
+
+
+def _pipeline_rows(bp, sel):
+    """The pipeline's hit rows of rays sel as the oracle's padded rows
+    (entries past each ray's count -1), with its valid lengths."""
+    import torch
+    st = torch.as_tensor(sel, device=bp.dev)
+    cnt = bp.hit_count[st].cpu().numpy()
+    idx, t0, t1 = (a[st].cpu().numpy().copy() for a in (bp.hit_idx, bp.hit_t0, bp.hit_t1))
+    pad = np.arange(bp.W)[None, :] >= cnt[:, None]
+    idx[pad], t0[pad], t1[pad] = -1, -1.0, -1.0
+    return dict(idx=idx[None], t0=t0[None], t1=t1[None], valid_len=bp.valid_len[st].cpu().numpy()[None, :, None],
+                max_hits=int(cnt.max(initial=0)), flags=np.zeros((1, len(sel)), np.int32))
+
+
+def _pipeline_keys(bp):
+    """Node ids of the pipeline's tree -> canonical (level, frame, x, y, z)."""
+    return dict(Dt=bp.Dt, Db=bp.D, base_top=bp.B * bp.D ** 3, base_bot=0, top_key=bp.top_key.cpu().numpy(),
+                bot_key=bp.bot_key.cpu().numpy())
+
+
+def _check_rows(frame, w, b, o, d, rows, keys):
+    """The oracle's traversal on its own tree of frame b against the
+    pipeline's rows: (rays the oracle leaves unflagged, rows equal as
+    canonical node sequences, max |t0/t1 difference| on equal rows)."""
+    from oracle import oracle as orc
+    W = rows["idx"].shape[-1]
+    vs, bb = w["voxel_size"][b:b + 1].reshape(1, 1), w["vol_bbox"][b:b + 1]
+    h = orc.voxel_traversal(frame["tree"], o[None], d[None], vs, bb, W=W)
+    ko = orc.node_keys(frame["tree"], h["idx"][0])
+    ko[..., 1] = np.where(h["idx"][0] >= 0, b, -1)
+    kg = orc.node_keys(keys, rows["idx"][0])
+    ok = (h["flags"][0] == 0) & (h["max_hits"] <= W)
+    eq = np.all(ko == kg, axis=(1, 2))
+    m = (h["idx"][0] >= 0) & eq[:, None]
+    terr = max(float(np.abs(h["t0"][0][m] - rows["t0"][0][m]).max(initial=0.0)),
+               float(np.abs(h["t1"][0][m] - rows["t1"][0][m]).max(initial=0.0)))
+    return ok, eq, terr
+
+
+def _samples_on_rows(bp, w, b, rows, S, rands):
+    """The oracle's coarse sampling and sort of the pipeline's hit rows
+    (sample depths [n, S], torch.sort order)."""
+    from oracle import oracle as orc
+    tree = {"Dt": bp.Dt, "Db": bp.D, "base_top": bp.B * bp.D ** 3}
+    _, sz, _ = orc.sample_coarse(tree, rows, rands[None], w["voxel_size"][b:b + 1].reshape(1, 1), S)
+    return orc.sort(sz)[0][0]
+
+
+def _jitter(seed, r, S):
+    """The render's jitter of rays r [n], samples 0..S-1: hashed with seed,
+    the constant 0.5 when seed is 0."""
+    from oracle import oracle as orc
+    if not seed:
+        return np.full((len(r), S), 0.5, np.float32)
+    return orc.hash_uniform(seed, np.asarray(r)[:, None], np.arange(S)[None, :])
+
+
+def _select_rays(hit_count, a, b, n_hit, n_all):
+    """Evenly spaced rays of [a, b): n_hit among those with hits, n_all among all."""
+    hc = hit_count[a:b]
+    hit = np.nonzero(hc > 0)[0]
+    sel = []
+    if len(hit):
+        sel.append(hit[np.linspace(0, len(hit) - 1, min(n_hit, len(hit))).astype(np.int64)])
+    sel.append(np.linspace(0, b - a - 1, min(n_all, b - a)).astype(np.int64))
+    return a + np.unique(np.concatenate(sel))
+
+
+def _near_rays(bp, zs, b, vxyz, frame_of_ray):
+    """Rays of frame b whose samples come within a voxel of voxel vxyz (a
+    superset of the rays whose taps weight it)."""
+    import torch
+    near = torch.zeros(bp.R, dtype=torch.bool, device=bp.dev)
+    bmin_t = bp.vol_bbox[b, :, 0]
+    inv_vs = 1.0 / bp.voxel_size[b]
+    v_t = torch.tensor(vxyz, dtype=torch.float32, device=bp.dev)
+    for a in range(0, bp.R, 1 << 19):
+        e = min(a + (1 << 19), bp.R)
+        zz = zs[a:e]
+        pts = bp.ori[a:e, None, :] + bp.dirs[a:e, None, :] * zz.clamp_min(0)[..., None]
+        u = (pts - bmin_t) * inv_vs
+        near[a:e] = (((u - v_t).abs() <= 1.5).all(-1) & (zz >= 0)).any(-1) & (frame_of_ray[a:e] == b)
+    return torch.nonzero(near).view(-1).cpu().numpy()
+
+
+def _perturbed_features(pts, feat, bmin, vs, vxyz, ch, dv):
+    """float64 features at pts with feature (vxyz, ch) moved by dv (each
+    sample's features change by dv times the voxel's trilinear weight)."""
+    from oracle import oracle as orc
+    fe = orc.grid_gather(pts, feat, bmin, vs)
+    if dv != 0.0:
+        i0, wt = orc.trilinear_cells(pts, bmin, vs)
+        dlt = np.asarray(vxyz)[None, :] - i0
+        inside = ((dlt >= 0) & (dlt <= 1)).all(-1)
+        cr = np.clip((dlt[:, 0] << 2) | (dlt[:, 1] << 1) | dlt[:, 2], 0, 7)
+        fe[:, ch] += np.where(inside, wt[np.arange(len(cr)), cr], 0.0) * dv
+    return fe
+
+
+def parity_batch(bp, w, bcfg, seed, frames=None, n_hit=192, n_all=64, n_fd_entries=48, h=1e-4):
+    """Parity of the batched training step (its last outputs in bp) against
+    the oracle, stage by stage:
+    - fusion of every frame bit for bit (TSDF, weight, colour grids);
+    - per target, n_hit rays with hits and n_all rays overall:
+      * traversal: the oracle's rows on its own tree equal the pipeline's
+        (canonical node sequences) on every ray the oracle does not flag as
+        a near tie, t-intervals within 1e-5 (the GPU's approximate
+        reciprocal moves them by ulps);
+      * sampling: the oracle's coarse sampling (the step's jitter) and sort
+        of the pipeline's rows equal the pipeline's samples bit for bit, on
+        every ray;
+      * compositing: the float64 render of those samples (float32 sample
+        points, FP64 taps, density, colour head, compositing) against the
+        training pass's colour, depth, weight sum and alpha -- max abs error
+        per output on every ray but early-termination ties;
+    - the feature-grid gradient of the step on n_fd_entries entries (the
+      largest and random touched ones) against float64 central differences
+      (step h) of the oracle's loss of every ray whose samples reach the
+      entry (the feature at each affected sample moved by +-h times its
+      trilinear weight, then re-composited).
+    seed: the step's jitter seed (0: constant 0.5).  Returns the dict
+    printed as the bench line's "parity"."""
+    import torch
+    from oracle import oracle as orc
+    t_start = time.perf_counter()
+    if frames is None:
+        frames = _oracle_frames(w, bcfg)
+    B, D, C = bcfg["frames"], bcfg["D"], bcfg["C"]
+    fusion_exact = all(np.array_equal(bp.tsdf[b].cpu().numpy().view(np.uint32), f["fusion"]["tsdf"][0].view(np.uint32))
+                       and np.array_equal(bp.weight[b].cpu().numpy(), f["fusion"]["weight"][0])
+                       and np.array_equal(bp.colorv[b].cpu().numpy(), f["fusion"]["color"][0])
+                       for b, f in enumerate(frames))
+    trunc_m = float(w["voxel_size"][0]) * w["trunc_weight"]
+    sdf_s = bcfg["sdf_s"]
+    head = bp.head.cpu().numpy()
+    hc = bp.hit_count.cpu().numpy()
+    ori, dirs = bp.ori.cpu().numpy(), bp.dirs.cpu().numpy()
+    outs = [t.cpu().numpy().reshape(bp.R, -1) for t in (bp.out_rgb, bp.out_depth, bp.out_ws, bp.out_alpha)]
+    # the samples of every ray (the training pass samples as the forward)
+    zs = torch.empty((bp.R, bp.S), device=bp.dev)
+    nodes = torch.empty((bp.R, bp.S), dtype=torch.int32, device=bp.dev)
+    bp.forward(zs, nodes)
+    del nodes
+    keys = _pipeline_keys(bp)
+    feat = [bp.feat[b:b + 1].cpu().numpy() for b in range(B)]
+    errs = dict(rgb=0.0, depth=0.0, ws=0.0, alpha=0.0)
+    n_rays = rows_flagged = rows_mismatch = z_mismatch = comp_flagged = 0
+    t_err = 0.0
+    for t, (b, n, S) in enumerate(bp.targets):
+        a, e = bp.ray_slices[t]
+        sel = _select_rays(hc, a, e, n_hit, n_all)
+        n_rays += len(sel)
+        rows = _pipeline_rows(bp, sel)
+        ok_rows, eq_rows, terr = _check_rows(frames[b], w, b, ori[sel], dirs[sel], rows, keys)
+        rows_flagged += int((~ok_rows).sum())
+        rows_mismatch += int((ok_rows & ~eq_rows).sum())
+        t_err = max(t_err, terr)
+        srt = _samples_on_rows(bp, w, b, rows, S, _jitter(seed, sel, S))
+        zg = zs[torch.as_tensor(sel, device=bp.dev), :S].cpu().numpy()
+        z_mismatch += int((~np.all(zg.view(np.uint32) == srt.view(np.uint32), axis=1)).sum())
+        r = orc.render_fp64(ori[sel], dirs[sel], srt, frames[b]["fusion"]["tsdf"], w["vol_bbox"][b:b + 1, :, 0],
+                            w["voxel_size"][b:b + 1], trunc_m, sdf_s, feat[b], head, 1e-4)
+        ok = r["flags"] == 0
+        comp_flagged += int((~ok).sum())
+        for k, ref, got in (("rgb", r["rgb"], outs[0][sel]), ("depth", r["depth"], outs[1][sel, 0]),
+                            ("ws", r["ws"], outs[2][sel, 0]), ("alpha", r["alpha"], outs[3][sel, 0])):
+            if ok.any():
+                errs[k] = max(errs[k], float(np.abs(got - ref)[ok].max()))
+    # the feature-grid gradient against float64 central differences of the
+    # loss of every ray that reaches the checked entries
+    loss_scale = 2.0 / (3.0 * bp.R)
+    tgt = bp.target_rgb.cpu().numpy().astype(np.float64)
+    ray_frame = np.empty(bp.R, np.int64)
+    ray_S = np.empty(bp.R, np.int64)
+    for t, (b, n, S) in enumerate(bp.targets):
+        a, e = bp.ray_slices[t]
+        ray_frame[a:e] = b
+        ray_S[a:e] = S
+
+    def loss_of_rays(rays, b, vxyz, ch, dv):
+        """float64 loss of rays (all of frame b) with feature (vxyz, ch)
+        moved by dv; samples: the oracle's sampling of the pipeline's rows."""
+        tot = 0.0
+        for S in np.unique(ray_S[rays]):
+            rr = rays[ray_S[rays] == S]
+            srt = _samples_on_rows(bp, w, b, _pipeline_rows(bp, rr), int(S), _jitter(seed, rr, int(S)))
+            bmin, vs = w["vol_bbox"][b:b + 1, :, 0], w["voxel_size"][b:b + 1]
+            base = orc.render_fp64(ori[rr], dirs[rr], srt, frames[b]["fusion"]["tsdf"], bmin, vs, trunc_m, sdf_s,
+                                   feat[b], head, 1e-4)
+            pts = orc.sample_points(ori[rr], dirs[rr], srt).reshape(-1, 3)
+            fe = _perturbed_features(pts, feat[b], bmin, vs, vxyz, ch, dv)
+            rgb_s = np.where((srt >= 0)[..., None], (fe @ head.T.astype(np.float64)).reshape(len(rr), int(S), 3), 0)
+            c = orc.composite_sorted_fp64(srt, base["sigma"], rgb_s, 1e-4)[0]
+            tot += 0.5 * loss_scale * ((c - tgt[rr]) ** 2).sum()
+            loss_of_rays.flagged += int((base["flags"] != 0).sum())
+        return tot
+    loss_of_rays.flagged = 0
+
+    flat = bp.grad_feat.view(-1)
+    top = torch.topk(flat.abs(), n_fd_entries // 2).indices
+    nz = torch.nonzero(flat).view(-1)
+    gen = torch.Generator(device="cpu").manual_seed(int(seed) + 1)
+    rnd = nz[torch.randint(0, nz.numel(), (n_fd_entries - top.numel(),), generator=gen).to(nz.device)]
+    entries = torch.unique(torch.cat([top, rnd])).cpu().numpy()
+    g_gpu = flat[torch.as_tensor(entries, device=bp.dev)].double().cpu().numpy()
+    rf = torch.as_tensor(ray_frame, device=bp.dev)
+    g_fd = np.zeros(len(entries))
+    n_rays_fd = 0
+    for k, ent in enumerate(entries):
+        b, rem = divmod(int(ent), D ** 3 * C)
+        vox, ch = divmod(rem, C)
+        vxyz = (vox // (D * D), (vox // D) % D, vox % D)
+        rays = _near_rays(bp, zs, b, vxyz, rf)
+        n_rays_fd += len(rays)
+        g_fd[k] = (loss_of_rays(rays, b, vxyz, ch, h) - loss_of_rays(rays, b, vxyz, ch, -h)) / (2.0 * h)
+    del zs
+    gmax = float(np.abs(g_fd).max())
+    gerr = float(np.abs(g_gpu - g_fd).max())
+    return dict(fusion_frames_bit_exact=bool(fusion_exact), rays=n_rays,
+                traversal=dict(rays_flagged=rows_flagged, unflagged_row_mismatches=rows_mismatch,
+                               t_max_abs_err=t_err),
+                sample_mismatches=z_mismatch,
+                composite_max_abs_err=errs, composite_rays_flagged=comp_flagged, composite_atol=1e-5,
+                composite_within_atol=all(v <= 1e-5 for v in errs.values()),
+                grad_fd=dict(entries=len(entries), rays=n_rays_fd, h=h, max_abs_err=gerr, max_abs_fd=gmax,
+                             rel_err=gerr / gmax if gmax > 0 else None,
+                             ray_evaluations_flagged=loss_of_rays.flagged),
+                seconds=time.perf_counter() - t_start)
 
 
 def plain_per_frame_forward(VE, fields, w, bcfg, dev, feat, head_t, vbb, vvs, W_hits=256):
@@ -565,7 +815,8 @@ def run_batch(args):
     if rank == 0:
         pk, pk_kind = peaks()
         S_all = sum(n * s for _, n, s in targets)
-        ab = batch_algorithmic_bytes(bcfg, w, n_hits, R, S_all, near_node_bricks(bp))
+        n_touched = int((bp.grad_feat != 0).any(-1).sum().item())  # voxels the step's samples tap
+        ab = batch_algorithmic_bytes(bcfg, w, n_hits, R, S_all, near_node_bricks(bp), n_touched)
         rl = {k: ab[k] / (stages[k] / 1000.0) / 1e9 for k in ab if stages.get(k)}
         dom = max(rl, key=lambda k: stages[k])
         traffic = None
@@ -588,7 +839,7 @@ def run_batch(args):
             plain_per_frame_fwd=dict(value=plain_value, unit=UNIT, ms_per_step=plain_ms,
                                      ratio_batched_fwd_bwd=value / plain_value),
             tsdf_gvox_s=bcfg["frames"] * bcfg["D"] ** 3 / (stages["fusion"] / 1000.0) / 1e9,
-            hits_per_ray=n_hits / R, peak_hbm_bytes=peak_mem,
+            hits_per_ray=n_hits / R, peak_hbm_bytes=peak_mem, touched_voxels=n_touched,
             roofline=dict(bound="hbm", kernel=dom, achieved=rl[dom], peak=pk["hbm_gbs"], unit="GB/s",
                           frac=rl[dom] / pk["hbm_gbs"], traffic=traffic, peak_kind=pk_kind,
                           algorithmic_bytes=ab[dom]),
@@ -611,9 +862,304 @@ def run_batch(args):
             cpu_baseline_batch(w, bcfg, feat0, head, fz=fz0)
             cb = cpu_baseline_batch(w, bcfg, feat0, head, fz=fz0)
             out["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        if not args.no_parity:
+            out["parity"] = parity_batch(bp, w, bcfg, bcfg["seed"] + 1)
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# differentiation workload: 2^20 random rays through the plain small volume,
+# compositing forward + adjoint and the trilinear gathers + adjoint
+# ---------------------------------------------------------------------------
+DIFF = dict(views=4, res=512, prims=12, D=256, rate=8, trunc=0.03, rays=1 << 20, S=96, C=16, W=256, sdf_s=0.005,
+            seed=17)
+
+
+def diff_rays(seed, n, radius=3.0):
+    """Seeded rays: origins uniform on a sphere of `radius` metres about the
+    cube's centre, each aimed at a uniform point of the 2 m cube."""
+    rng = np.random.default_rng(seed)
+    v = rng.normal(size=(n, 3))
+    o = radius * v / np.linalg.norm(v, axis=1, keepdims=True)
+    d = rng.uniform(-1.0, 1.0, (n, 3)) - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return o.astype(np.float32), d.astype(np.float32)
+
+
+def diff_setup(cfg, dev):
+    """The differentiation workload in a one-frame BatchPipeline: the fused
+    volume, 2^20 rays (one segment of S samples), a seeded 256^3 x 16 feature
+    grid ~ N(0, 0.1), a colour head ~ N(0, 0.5), upstream gradients ~ N(0, 1)
+    on colour, depth and alpha (0 on the weight sum)."""
+    import torch
+
+    from sailor_gb300 import synthetic as syn
+    from sailor_gb300.batch import BatchPipeline
+    sc = syn.make_scene(seed=cfg["seed"], n_views=cfg["views"], res=cfg["res"], n_prims=cfg["prims"], D=cfg["D"],
+                        trunc=cfg["trunc"])
+    ori, dirs = diff_rays(cfg["seed"], cfg["rays"])
+    frame = dict(K=list(sc["K"][0]), RT=list(sc["RT"][0]), depth=list(sc["depths"][0]), color=list(sc["colors"][0]))
+    n, S = len(ori), cfg["S"]
+    bp = BatchPipeline([[d.shape for d in frame["depth"]]], [(0, n, S)], D=cfg["D"], rate=cfg["rate"], C=cfg["C"],
+                       W_hits=cfg["W"], train_tsdf=True, device=dev)
+    bp.load_views([frame], sc["vol_bbox"], sc["voxel_size"].reshape(-1), sc["trunc_weight"])
+    bp.load_rays([(ori, dirs)])
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(cfg["seed"])
+    bp.feat.normal_(0.0, 0.1, generator=gen)
+    bp.set_fields(head=torch.randn((3, cfg["C"]), generator=gen, device=dev) * 0.5)
+    trunc_m = float(sc["voxel_size"][0, 0]) * sc["trunc_weight"]
+    bp.render_args(trunc_m, sdf_s=cfg["sdf_s"], t_thres=1e-4, rand_seed=cfg["seed"])
+    g = dict(g_rgb=torch.randn((n, 3), generator=gen, device=dev), g_depth=torch.randn(n, generator=gen, device=dev),
+             g_ws=torch.zeros(n, device=dev), g_alpha=torch.randn(n, generator=gen, device=dev))
+    gs = torch.empty((n, S), device=dev)
+    gr = torch.empty((n, S, 3), device=dev)
+    w = dict(frames=[frame], vol_bbox=sc["vol_bbox"], voxel_size=sc["voxel_size"].reshape(-1),
+             trunc_weight=sc["trunc_weight"])
+    return dict(bp=bp, sc=sc, w=w, grads=g, grad_sigma=gs, grad_rgb=gr, trunc_m=trunc_m)
+
+
+def diff_step(d):
+    """One step: intersection, forward render, backward (per-sample sigma and
+    colour gradients, and the feature and TSDF grid gradients)."""
+    bp = d["bp"]
+    bp.intersect()
+    bp.forward()
+    g = d["grads"]
+    bp.backward(g["g_rgb"], g["g_depth"], g["g_ws"], g["g_alpha"], grad_sigma=d["grad_sigma"],
+                grad_rgb=d["grad_rgb"], tsdf_grad=True, zero=True)
+
+
+def parity_diff(d, cfg, n_rays=512, h=1e-4, n_entries=24, autograd_rays=None):
+    """Checks of the differentiation step (after timing):
+    - fusion bit for bit; on n_rays rays with hits: traversal rows against
+      the oracle's (unflagged rays), samples against the oracle's sampling
+      of the pipeline's rows (bit for bit), the forward outputs against the
+      float64 oracle render of those samples, and the per-sample sigma and
+      colour gradients against float64 central differences (step h) of L =
+      g_rgb . rgb + g_depth depth + g_ws ws + g_alpha alpha;
+    - on every ray (or the first autograd_rays): the per-sample gradients
+      against float64 autograd of a plain PyTorch compositing (the kernel's
+      semantics: sorted samples, last delta 1e10, early termination) fed with
+      the modular chain's float32 sigma and colour at the same samples;
+    - on n_entries feature- and TSDF-grid entries: the grid gradients against
+      float64 central differences of L over every ray reaching the entry."""
+    import torch
+
+    from oracle import oracle as orc
+    from sailor_gb300.fields import grid_gather, tsdf_density
+    t_start = time.perf_counter()
+    bp, w = d["bp"], d["w"]
+    D, C, S = cfg["D"], cfg["C"], cfg["S"]
+    frames = _oracle_frames(w, dict(D=D, rate=cfg["rate"]))
+    fr = frames[0]
+    fusion_exact = bool(np.array_equal(bp.tsdf[0].cpu().numpy().view(np.uint32), fr["fusion"]["tsdf"][0].view(
+        np.uint32)))
+    trunc_m, sdf_s, seed = d["trunc_m"], cfg["sdf_s"], cfg["seed"]
+    head = bp.head.cpu().numpy().astype(np.float64)
+    feat = bp.feat.cpu().numpy()
+    ori, dirs = bp.ori.cpu().numpy(), bp.dirs.cpu().numpy()
+    g = {k: v.cpu().numpy().astype(np.float64) for k, v in d["grads"].items()}
+    bmin, vs = w["vol_bbox"][:, :, 0], w["voxel_size"]
+    hc = bp.hit_count.cpu().numpy()
+    sel = _select_rays(hc, 0, bp.R, n_rays, 0)
+    outs = [t.cpu().numpy().reshape(bp.R, -1)[sel] for t in (bp.out_rgb, bp.out_depth, bp.out_ws, bp.out_alpha)]
+    z = torch.empty((bp.R, S), device=bp.dev)
+    node = torch.empty((bp.R, S), dtype=torch.int32, device=bp.dev)
+    bp.forward(z, node)  # the same samples and outputs as the timed step's forward
+    del node
+    rows = _pipeline_rows(bp, sel)
+    ok_rows, eq_rows, t_err = _check_rows(fr, w, 0, ori[sel], dirs[sel], rows, _pipeline_keys(bp))
+    srt = _samples_on_rows(bp, w, 0, rows, S, _jitter(seed, sel, S))
+    zg = z[torch.as_tensor(sel, device=bp.dev)].cpu().numpy()
+    z_mismatch = int((~np.all(zg.view(np.uint32) == srt.view(np.uint32), axis=1)).sum())
+    base = orc.render_fp64(ori[sel], dirs[sel], srt, fr["fusion"]["tsdf"], bmin, vs, trunc_m, sdf_s, feat, head,
+                           1e-4)
+    ok = base["flags"] == 0
+    fwd_err = dict(rgb=float(np.abs(outs[0] - base["rgb"])[ok].max()),
+                   depth=float(np.abs(outs[1][:, 0] - base["depth"])[ok].max()),
+                   ws=float(np.abs(outs[2][:, 0] - base["ws"])[ok].max()),
+                   alpha=float(np.abs(outs[3][:, 0] - base["alpha"])[ok].max()))
+
+    def L(sig, rgb):
+        c, dd, ws, a, _ = orc.composite_sorted_fp64(srt, sig, rgb, 1e-4)
+        return ((c * g["g_rgb"][sel]).sum(1) + dd * g["g_depth"][sel] + ws * g["g_ws"][sel]
+                + a * g["g_alpha"][sel])
+
+    fs = np.zeros((len(sel), S))
+    fr_ = np.zeros((len(sel), S, 3))
+    for q in range(S):
+        sp, sm = base["sigma"].copy(), base["sigma"].copy()
+        sp[:, q] += h
+        sm[:, q] -= h
+        fs[:, q] = (L(sp, base["rgb_s"]) - L(sm, base["rgb_s"])) / (2 * h)
+        for k in range(3):
+            rp, rm = base["rgb_s"].copy(), base["rgb_s"].copy()
+            rp[:, q, k] += h
+            rm[:, q, k] -= h
+            fr_[:, q, k] = (L(base["sigma"], rp) - L(base["sigma"], rm)) / (2 * h)
+    gs = d["grad_sigma"].cpu().numpy()[sel]
+    gr = d["grad_rgb"].cpu().numpy()[sel]
+    sample_fd = dict(rays=int(ok.sum()), sigma_max_abs_err=float(np.abs(gs - fs)[ok].max()),
+                     sigma_max_abs=float(np.abs(fs[ok]).max()), rgb_max_abs_err=float(np.abs(gr - fr_)[ok].max()),
+                     rgb_max_abs=float(np.abs(fr_[ok]).max()))
+    # autograd of a plain PyTorch compositing on the GPU in float64
+    R = bp.R if autograd_rays is None else min(bp.R, autograd_rays)
+    ag_err_s = ag_err_r = ag_max_s = ag_max_r = 0.0
+    ag_checked = 0
+    for a in range(0, R, 1 << 18):
+        e = min(a + (1 << 18), R)
+        zz = z[a:e][None].contiguous()
+        o, dr = bp.ori[a:e][None], bp.dirs[a:e][None]
+        with torch.no_grad():
+            sig = tsdf_density(bp.tsdf[:1], o, dr, zz, bp.vol_bbox[:1], bp.voxel_size[:1], trunc_m, sdf_s)[0]
+            rgb = grid_gather(bp.feat[:1], o, dr, zz, bp.vol_bbox[:1], bp.voxel_size[:1])[0] @ bp.head.T
+        sd = sig.double().requires_grad_(True)
+        rd = rgb.double().requires_grad_(True)
+        z64 = zz[0].double()
+        valid = z64 >= 0
+        nxt = torch.cat([z64[:, 1:], torch.full_like(z64[:, :1], 1e10)], 1)
+        delta = torch.where(torch.arange(S, device=z.device) == S - 1, torch.full_like(z64, 1e10), nxt - z64)
+        alpha = torch.where(valid, 1 - torch.exp(-sd * delta), torch.zeros_like(sd))
+        f = torch.where(valid, 1 - alpha, torch.ones_like(alpha))
+        t_after = torch.cumprod(f, 1)
+        t_before = torch.cat([torch.ones_like(f[:, :1]), t_after[:, :-1]], 1)
+        below = valid & (t_after < 1e-4)
+        first = torch.where(below.any(1), below.float().argmax(1), torch.full_like(below[:, 0], S, dtype=torch.long))
+        used = valid & (torch.arange(S, device=z.device)[None, :] <= first[:, None])
+        tie = (used & ((t_after - 1e-4).abs() <= 1e-4 * 1e-4)).any(1)
+        wgt = torch.where(used, alpha * t_before, torch.zeros_like(alpha))
+        loss = ((wgt[..., None] * rd).sum(1) * d["grads"]["g_rgb"][a:e].double()).sum() + \
+            ((wgt * torch.where(valid, z64, torch.zeros_like(z64))).sum(1) * d["grads"]["g_depth"][a:e].double()).sum() \
+            + (wgt.sum(1) * d["grads"]["g_ws"][a:e].double()).sum() + \
+            ((wgt * alpha).sum(1) * d["grads"]["g_alpha"][a:e].double()).sum()
+        loss.backward()
+        m = ~tie
+        ag_checked += int(m.sum())
+        ag_err_s = max(ag_err_s, float((d["grad_sigma"][a:e].double() - sd.grad)[m].abs().max()))
+        ag_err_r = max(ag_err_r, float((d["grad_rgb"][a:e].double() - rd.grad)[m].abs().max()))
+        ag_max_s = max(ag_max_s, float(sd.grad[m].abs().max()))
+        ag_max_r = max(ag_max_r, float(rd.grad[m].abs().max()))
+    autograd = dict(rays=ag_checked, sigma_max_abs_err=ag_err_s, sigma_max_abs=ag_max_s, rgb_max_abs_err=ag_err_r,
+                    rgb_max_abs=ag_max_r)
+
+    # grid gradients against float64 central differences over the rays reaching each entry
+    def loss_rays(rays, grid, vxyz, ch, dv):
+        srt_r = _samples_on_rows(bp, w, 0, _pipeline_rows(bp, rays), S, _jitter(seed, rays, S))
+        pts = orc.sample_points(ori[rays], dirs[rays], srt_r).reshape(-1, 3)
+        tsdf4 = fr["fusion"]["tsdf"][..., None]
+        if grid == "feat":
+            t = orc.grid_gather(pts, tsdf4, bmin, vs)[:, 0]
+            fe = _perturbed_features(pts, feat, bmin, vs, vxyz, ch, dv)
+        else:
+            t = _perturbed_features(pts, tsdf4, bmin, vs, vxyz, 0, dv)[:, 0]
+            fe = orc.grid_gather(pts, feat, bmin, vs)
+        n = len(rays)
+        sig = np.where(srt_r >= 0, (1.0 / (1.0 + np.exp(t * (trunc_m / sdf_s))) / sdf_s).reshape(n, S), 0.0)
+        rgb_s = np.where((srt_r >= 0)[..., None], (fe @ head.T).reshape(n, S, 3), 0.0)
+        c, dd, ws, a, f2 = orc.composite_sorted_fp64(srt_r, sig, rgb_s, 1e-4)
+        loss_rays.flagged += int((f2 != 0).sum())
+        return float(((c * g["g_rgb"][rays]).sum(1) + dd * g["g_depth"][rays] + ws * g["g_ws"][rays]
+                      + a * g["g_alpha"][rays]).sum())
+    loss_rays.flagged = 0
+
+    res = {}
+    rf = torch.zeros(bp.R, dtype=torch.long, device=bp.dev)
+    for grid, gt, nch in (("feat", bp.grad_feat, C), ("tsdf", bp.grad_tsdf, 1)):
+        flat = gt.reshape(-1)
+        top = torch.topk(flat.abs(), n_entries // 2).indices
+        nz = torch.nonzero(flat).view(-1)
+        gen = torch.Generator(device="cpu").manual_seed(seed)
+        rnd = nz[torch.randint(0, nz.numel(), (n_entries - top.numel(),), generator=gen).to(nz.device)]
+        entries = torch.unique(torch.cat([top, rnd])).cpu().numpy()
+        g_gpu = flat[torch.as_tensor(entries, device=bp.dev)].double().cpu().numpy()
+        g_fd = np.zeros(len(entries))
+        n_fd_rays = 0
+        for k, ent in enumerate(entries):
+            vox, ch = divmod(int(ent), nch)
+            vxyz = (vox // (D * D), (vox // D) % D, vox % D)
+            rays = _near_rays(bp, z, 0, vxyz, rf)
+            n_fd_rays += len(rays)
+            g_fd[k] = (loss_rays(rays, grid, vxyz, ch, h) - loss_rays(rays, grid, vxyz, ch, -h)) / (2 * h)
+        gmax = float(np.abs(g_fd).max())
+        res[grid] = dict(entries=len(entries), rays=n_fd_rays, max_abs_err=float(np.abs(g_gpu - g_fd).max()),
+                         max_abs_fd=gmax)
+    return dict(fusion_bit_exact=fusion_exact, rays=len(sel),
+                traversal=dict(rays_flagged=int((~ok_rows).sum()),
+                               unflagged_row_mismatches=int((ok_rows & ~eq_rows).sum()), t_max_abs_err=t_err),
+                sample_mismatches=z_mismatch, composite_rays_flagged=int((~ok).sum()),
+                forward_max_abs_err=fwd_err, sample_grad_fd=sample_fd, sample_grad_autograd=autograd,
+                grid_grad_fd=res, grid_fd_ray_evaluations_flagged=loss_rays.flagged,
+                seconds=time.perf_counter() - t_start)
+
+
+def run_diff(args):
+    import torch
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    cfg = dict(DIFF)
+    if args.small:
+        cfg.update(rays=1 << 16, D=128, res=256)
+    d = diff_setup(cfg, dev)
+    bp = d["bp"]
+    bp.build()
+    torch.cuda.synchronize()
+    warm = max(args.warmup, 3)
+    for _ in range(warm):
+        diff_step(d)
+    torch.cuda.synchronize()
+    if bp.status[0].item() & 1:
+        raise RuntimeError("hit rows overflowed")
+    n_hits = int(bp.hit_count.sum().item())
+    import tempfile
+    clk = ClockSampler(os.path.join(tempfile.gettempdir(), "sg_clocks_diff.csv"))
+    with clk:
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            diff_step(d)
+        e1.record()
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    stage_sum = {}
+    for _ in range(args.steps):
+        bp.events = []
+        diff_step(d)
+        for k, v in bp.stage_times().items():
+            stage_sum[k] = stage_sum.get(k, 0.0) + v
+    bp.events = None
+    stages = {k: v / args.steps for k, v in stage_sum.items()}
+    R, S, C = bp.R, cfg["S"], cfg["C"]
+    n_touched = int(((bp.grad_feat[0] != 0).any(-1) | (bp.grad_tsdf[0] != 0)).sum().item())
+    n_samples = int((d["grad_rgb"].abs().sum(-1) != 0).sum().item())
+    pk, pk_kind = peaks()
+    # backward: rays (ori/dir, count, valid length, hit rows) and upstream
+    # gradients in; per-sample sigma / colour gradients out (16 B x S per
+    # ray); touched cells: features + TSDF read, their gradients written
+    ab = dict(forward=24 * R + 8 * R + 12 * n_hits + 24 * R + n_touched * (4 * C + 4),
+              backward=24 * R + 8 * R + 12 * n_hits + 16 * R + 16 * R * S + n_touched * 2 * (4 * C + 4),
+              grad_prep=4 * (C + 1) * cfg["D"] ** 3)
+    rl = {k: ab[k] / (stages[k] / 1000.0) / 1e9 for k in ab if stages.get(k)}
+    dom = max(rl, key=lambda k: stages[k])
+    out = dict(metric="rays/s differentiation step (2^20 random rays, S=96, 256^3x16 grid): fwd+bwd",
+               value=R / (ms / 1000.0), unit="rays/s", n_gpus=1, steps=args.steps, warmup=warm, ms_per_step=ms,
+               higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32",
+               data="synthetic (seeded scene, random rays, N(0,0.1) features, N(0,1) upstream gradients)",
+               config=dict(workload=f"{R} random rays through the {cfg['D']}^3 fused volume (8^3 bricks), S={S}, "
+                                    f"{cfg['D']}^3x{C} feature grid + TSDF grid, intersection + fused forward + "
+                                    f"exact adjoint with grid scatters", l2="grids 1.1 GB >> L2"),
+               stages_ms=stages, hits_per_ray=n_hits / R, samples_with_gradient=n_samples, touched_voxels=n_touched,
+               roofline=dict(bound="hbm", kernel=dom, achieved=rl[dom], peak=pk["hbm_gbs"], unit="GB/s",
+                             frac=rl[dom] / pk["hbm_gbs"], traffic=None, peak_kind=pk_kind,
+                             algorithmic_bytes=ab[dom]),
+               rooflines={k: dict(achieved=v, frac=v / pk["hbm_gbs"], algorithmic_bytes=ab[k]) for k, v in rl.items()},
+               gpu_launches=3 * args.steps, clocks=clk.summary())  # intersection, forward, backward
+    if not args.no_parity:
+        out["parity"] = parity_diff(d, cfg)
+    print(json.dumps(out), flush=True)
 
 
 def main():
@@ -624,6 +1170,8 @@ def main():
         return run_batch(args)
     if args.workload == "project":
         return run_project(args)
+    if args.workload == "diff":
+        return run_diff(args)
     return run_plain(args)
 
 

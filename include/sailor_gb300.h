@@ -43,6 +43,7 @@ typedef struct SgStatus {
 
 #define SG_FLAG_HIT_OVERFLOW 1
 #define SG_FLAG_TREE_CAPACITY 2
+#define SG_FLAG_RECORD_CAPACITY 4 /* gradient records exceeded the workspace's slots */
 
 /* Two-level brick tree kept in device memory (replaces the AoS OcTree node
  * array of include/octree.h:30-153 and MultiLayerOctree's buffers
@@ -567,6 +568,58 @@ int sg_render_segments_train(const SgTree *tree, const SgRaySegments *seg,
                              float *out_ws, float *out_alpha, float *out_loss,
                              float *grad_feat, float *grad_tsdf,
                              sg_stream_t stream);
+
+/* ---- deterministic gradient reduction -------------------------------- */
+
+/* Bytes of the workspace of sg_render_segments_train_det for R rays, nseg
+ * segments, C feature channels and `capacity` gradient-record slots (one
+ * slot per sample of every ray with hits: sum over those rays of their S;
+ * the sum over all rays always suffices). */
+size_t sg_train_det_workspace_bytes(long long R, int nseg, int C, long long capacity);
+
+/* The training step of sg_render_segments_train (same outputs and loss)
+ * with grid gradients that are bit-identical from run to run: a segmented
+ * reduction over sorted cell ids instead of float atomics.  The pass visits
+ * only the rays with hits (a scan builds their list; the others get their
+ * outputs directly) and writes one record per used sample -- trilinear cell,
+ * cell fractions, compositing weight, ray, TSDF gradient -- plus, per ray,
+ * head^T times its colour gradient; the records are sorted by cell (a
+ * stable radix sort), and each cell's run is summed in order and added to
+ * its 8 corners, one parity class of cells at a time (cells of a class
+ * share no corner).  The sums are added (+=) into grad_feat [B,Df,Df,Df,C]
+ * and grad_tsdf [B,D,D,D] (may be NULL; needs the feature grid on the TSDF
+ * grid's geometry).  groups: ngroups + 1 host ints, the segment index where
+ * each group of the table starts (one launch of the pass per group, sized
+ * for its largest sample count group_S[g], host ints).  workspace:
+ * sg_train_det_workspace_bytes(seg->total, seg->count, args->C, capacity)
+ * bytes of device memory.  More records than `capacity` set
+ * SG_FLAG_RECORD_CAPACITY in status and leave the gradient incomplete.
+ * No counterpart in the reference: its training path differentiates
+ * per-node corner features (sampling_kernel.cu:237-327), with no dense grid
+ * and no reduction across rays. */
+int sg_render_segments_train_det(const SgTree *tree, const SgRaySegments *seg,
+                                 const SgRenderArgs *args, int ngroups,
+                                 const int *groups, const int *group_S,
+                                 const float *target_rgb, float loss_scale,
+                                 float *out_rgb, float *out_depth, float *out_ws,
+                                 float *out_alpha, float *out_loss,
+                                 float *grad_feat, float *grad_tsdf,
+                                 void *workspace, size_t workspace_bytes,
+                                 long long capacity, SgStatus *status,
+                                 sg_stream_t stream);
+
+/* Stable sort of (keys[i], i), i < *count (a device int, at most capacity),
+ * by the low key_bits bits of the keys: the sorted keys and the indices
+ * into keys_out / vals_out ([capacity] each); keys_tmp / vals_tmp are
+ * [capacity] scratch and scratch sg_sort_pairs_scratch_bytes(capacity)
+ * bytes.  The radix sort of the deterministic gradient reduction, exported
+ * for callers and tests; no counterpart in the reference (it sorts with
+ * torch::sort, sampling_kernel.cu:1321, for the per-ray sample sort). */
+size_t sg_sort_pairs_scratch_bytes(long long capacity);
+int sg_sort_pairs(const uint32_t *keys, const int *count, long long capacity,
+                  int key_bits, uint32_t *keys_out, uint32_t *vals_out,
+                  uint32_t *keys_tmp, uint32_t *vals_tmp, void *scratch,
+                  size_t scratch_bytes, sg_stream_t stream);
 
 #ifdef __cplusplus
 }

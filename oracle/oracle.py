@@ -464,3 +464,112 @@ def chain(scene, D, rate, S, ori, dirs, rands, W=1024, obs_weight=1.0, trunc_wei
     return dict(fusion=fz, top=top, cnt_top=cnt_top, tree=tree, hits=hits, sampled_idx=sidx,
                 sampled_z=sz, flags=flags, sorted_z=sorted_z, sort_idx=sort_idx,
                 vol_bbox=vol_bbox, voxel_size=voxel_size)
+
+
+# --------------------------------------------------------------------------
+# float64 render of sorted samples (the fused render's arithmetic in FP64)
+# --------------------------------------------------------------------------
+def sample_points(ori, dirs, z):
+    """Sample points as the render kernels form them: fma(dir, z, ori) in
+    float32 (one rounding; the float64 product of two floats is exact and
+    its sum with ori is exact at these magnitudes), [R, S, 3] float32."""
+    o = np.asarray(ori, np.float64)[:, None, :]
+    d = np.asarray(dirs, np.float64)[:, None, :]
+    zz = np.maximum(np.asarray(z, np.float64), 0.0)[..., None]
+    return (d * zz + o).astype(np.float32)
+
+
+def composite_sorted_fp64(z, sigma, rgb, t_thres=1e-4):
+    """Density compositing of samples already sorted ascending (padding -1
+    first, as torch.sort leaves it) in float64, with the semantics of
+    volume_rendering_training_forward_kernel (volume_rendering.cu:17-126):
+    delta = next sample's depth - depth (float32 depths, exact difference),
+    the last 1e10; alpha = 1 - exp(-sigma delta); w = alpha T; the sample
+    whose update takes T below t_thres is the last one composited; a ray
+    without a valid sample renders 0.  sigma [R, S], rgb [R, S, C] float64.
+    Returns (rgb [R, C], depth, ws, alpha [R], flags [R]): FLAG_TIE where a
+    composited T lies within a relative 1e-4 of t_thres (the float32 chain
+    may stop one sample earlier or later there)."""
+    z = np.asarray(z, np.float32)
+    R, S = z.shape
+    valid = z >= 0
+    z64 = z.astype(np.float64)
+    delta = np.empty((R, S), np.float64)
+    delta[:, :-1] = z64[:, 1:] - z64[:, :-1]
+    delta[:, -1] = 1e10
+    sig = np.where(valid, np.asarray(sigma, np.float64), 0.0)
+    with np.errstate(over="ignore", invalid="ignore"):
+        alpha = np.where(valid, 1.0 - np.exp(-sig * delta), 0.0)
+    f = np.where(valid, 1.0 - alpha, 1.0)
+    t_after = np.cumprod(f, axis=1)
+    t_before = np.concatenate([np.ones((R, 1)), t_after[:, :-1]], 1)
+    below = valid & (t_after < t_thres)
+    first = np.where(below.any(1), below.argmax(1), S)
+    used = valid & (np.arange(S)[None, :] <= first[:, None])
+    w = np.where(used, alpha * t_before, 0.0)
+    out_rgb = np.einsum("rs,rsc->rc", w, np.asarray(rgb, np.float64))
+    flags = np.where((used & (np.abs(t_after - t_thres) <= 1e-4 * t_thres)).any(1), FLAG_TIE, 0).astype(np.int32)
+    return out_rgb, (w * np.where(valid, z64, 0.0)).sum(1), w.sum(1), (w * alpha).sum(1), flags
+
+
+def render_fp64(ori, dirs, z, tsdf, bbox_min, voxel_size, trunc_m, sdf_s, feat, head=None, t_thres=1e-4,
+                batch=None, feat_bbox_min=None, feat_voxel_size=None):
+    """The fused render (density from the TSDF grid, colour = head @ a
+    trilinear tap of a feature grid, compositing) of sorted samples, in
+    float64 from the float32 sample points: sigma = sigmoid(-t trunc_m /
+    sdf_s) / sdf_s with t the trilinear TSDF; rgb = head @ f (f itself when
+    head is None).  ori, dirs [R, 3]; z [R, S] sorted (-1 padding first);
+    tsdf [B, D, D, D]; feat [B, Df, Df, Df, C]; head [3, C]; batch [R]
+    frame per ray (None: frame 0); the feature grid shares the TSDF grid's
+    box unless feat_bbox_min / feat_voxel_size are given.  Returns dict(rgb
+    [R, 3], depth, ws, alpha [R], sigma [R, S], rgb_s [R, S, 3], flags [R])."""
+    z = np.asarray(z, np.float32)
+    R, S = z.shape
+    pts = sample_points(ori, dirs, z).reshape(-1, 3)
+    bt = None if batch is None else np.repeat(np.asarray(batch, np.int32), S)
+    t = grid_gather(pts, np.asarray(tsdf, np.float32)[..., None], bbox_min, voxel_size, batch=bt)[:, 0]
+    sig = (1.0 / (1.0 + np.exp(t * (float(trunc_m) / float(sdf_s)))) / float(sdf_s)).reshape(R, S)
+    fb = bbox_min if feat_bbox_min is None else feat_bbox_min
+    fv = voxel_size if feat_voxel_size is None else feat_voxel_size
+    fe = grid_gather(pts, feat, fb, fv, batch=bt)
+    rgb_s = (fe @ np.asarray(head, np.float64).T if head is not None else fe[:, :3]).reshape(R, S, 3)
+    valid = z >= 0
+    sig = np.where(valid, sig, 0.0)
+    rgb_s = np.where(valid[..., None], rgb_s, 0.0)
+    c, d, ws, a, flags = composite_sorted_fp64(z, sig, rgb_s, t_thres)
+    return dict(rgb=c, depth=d, ws=ws, alpha=a, sigma=sig, rgb_s=rgb_s, flags=flags)
+
+
+def hash_uniform(seed, r, q):
+    """The render's hashed jitter for ray r, sample q (a splitmix64 finaliser
+    of seed + r * golden-ratio constant + q, top 24 bits / 2^24), as float32
+    in [0, 1); r and q broadcast."""
+    with np.errstate(over="ignore"):
+        x = (np.uint64(seed) + np.asarray(r).astype(np.uint64) * np.uint64(0x9E3779B97F4A7C15)
+             + np.asarray(q).astype(np.uint64))
+        x ^= x >> np.uint64(30)
+        x *= np.uint64(0xBF58476D1CE4E5B9)
+        x ^= x >> np.uint64(27)
+        x *= np.uint64(0x94D049BB133111EB)
+        x ^= x >> np.uint64(31)
+    return (x >> np.uint64(40)).astype(np.float32) * np.float32(1.0 / 16777216.0)
+
+
+def trilinear_cells(pts, bbox_min, voxel_size, batch=None):
+    """Cells and corner weights of trilinear taps in float64, as the gathers
+    form them: u = (p - bbox_min) / voxel_size, lower corner floor(u),
+    weights of corner (dx, dy, dz) = bits (2, 1, 0) of its index.  pts [P, 3]
+    float32.  Returns (i0 [P, 3] int64, w [P, 8] float64)."""
+    pts = np.asarray(pts, np.float32).astype(np.float64)
+    b = np.zeros(len(pts), np.int64) if batch is None else np.asarray(batch, np.int64)
+    bmin = np.asarray(bbox_min, np.float32).reshape(-1, 3).astype(np.float64)[b]
+    vs = np.asarray(voxel_size, np.float32).reshape(-1).astype(np.float64)[b]
+    u = (pts - bmin) / vs[:, None]
+    i0 = np.floor(u)
+    f = u - i0
+    w = np.empty((len(pts), 8))
+    for cr in range(8):
+        dx, dy, dz = (cr >> 2) & 1, (cr >> 1) & 1, cr & 1
+        w[:, cr] = ((f[:, 0] if dx else 1 - f[:, 0]) * (f[:, 1] if dy else 1 - f[:, 1])
+                    * (f[:, 2] if dz else 1 - f[:, 2]))
+    return i0.astype(np.int64), w

@@ -53,6 +53,13 @@ static inline int near_eq(double a, double b) {
   return fabs(a - b) <= TIE_REL * m + 1e-30;
 }
 
+/* A near tie between two DDA crossing times (the axis-parallel sentinel */
+/* 9999999 excepted).                                                     */
+static inline int dda_tie(float a, float b) {
+  if (a == 9999999.0f && b == 9999999.0f) return 0;
+  return near_eq(a, b);
+}
+
 int orc_num_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();
@@ -594,9 +601,12 @@ int orc_voxel_traversal(int B, int N, const float *ori, const float *dir,
         if (nint >= opt_num) break;
       }
       int ax;
-      if ((near_eq(tm[0], tm[1]) && tm[0] != tm[1]) || (near_eq(tm[0], tm[2]) && tm[0] != tm[2]) ||
-          (near_eq(tm[1], tm[2]) && tm[1] != tm[2]))
-        tie = 1;
+      /* exact equality counts too: the GPU reaches tm from a start point   */
+      /* computed with its approximate reciprocal, so two crossings that    */
+      /* coincide here can come out an ulp apart there and step the other  */
+      /* axis first; only the 9999999 of a zero direction component is the  */
+      /* same constant on both                                              */
+      if (dda_tie(tm[0], tm[1]) || dda_tie(tm[0], tm[2]) || dda_tie(tm[1], tm[2])) tie = 1;
       if (tm[0] < tm[1]) ax = (tm[0] < tm[2]) ? 0 : 2;
       else ax = (tm[1] < tm[2]) ? 1 : 2;
       st[ax] += (int)step[ax];

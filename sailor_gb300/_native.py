@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(HERE, "libsailor_gb300.so")
 
 SG_FLAG_HIT_OVERFLOW = 1
 SG_FLAG_TREE_CAPACITY = 2
+SG_FLAG_RECORD_CAPACITY = 4
 
 EXPORTS = (
     "sg_mask_words", "sg_status_string", "sg_version", "sg_auto_bbox", "sg_fuse_tsdf",
@@ -24,7 +25,8 @@ EXPORTS = (
     "sg_grid_scatter", "sg_fuse_tsdf_views", "sg_intersect_segments", "sg_render_segments_fwd",
     "sg_render_segments_bwd", "sg_render_segments_train",
     "sg_camera_params", "sg_rays_from_cameras", "sg_segment_rays", "sg_zero_near_nodes",
-    "sg_project_sampled_xyz", "sg_project_gather",
+    "sg_project_sampled_xyz", "sg_project_gather", "sg_train_det_workspace_bytes", "sg_render_segments_train_det",
+    "sg_sort_pairs_scratch_bytes", "sg_sort_pairs",
 )
 
 
@@ -109,6 +111,13 @@ def _load():
     lib.sg_render_segments_fwd.argtypes = [T, G, A, p, p, p, p, p, p, p]
     lib.sg_render_segments_bwd.argtypes = [T, G, A, p, p, p, p, p, p, p, p, p]
     lib.sg_render_segments_train.argtypes = [T, G, A, p, f, p, p, p, p, p, p, p, p]
+    ll = C.c_longlong
+    lib.sg_train_det_workspace_bytes.argtypes = [ll, i, i, ll]
+    lib.sg_train_det_workspace_bytes.restype = sz
+    lib.sg_render_segments_train_det.argtypes = [T, G, A, i, p, p, p, f, p, p, p, p, p, p, p, p, sz, ll, p, p]
+    lib.sg_sort_pairs_scratch_bytes.argtypes = [ll]
+    lib.sg_sort_pairs_scratch_bytes.restype = sz
+    lib.sg_sort_pairs.argtypes = [p, p, ll, i, p, p, p, p, p, sz, p]
     lib.sg_camera_params.argtypes = [p, p, p, i, p, p]
     lib.sg_rays_from_cameras.argtypes = [p, p, p, i, i, i, i, p, p]
     lib.sg_segment_rays.argtypes = [C.POINTER(SgRaySegments), p, p, p]

@@ -71,13 +71,18 @@ def capacity_layout(targets):
 
 class BatchPipeline:
     def __init__(self, view_hw, targets, D=256, rate=8, C=16, W_hits=64, train_tsdf=False, target_widths=None,
-                 device="cuda"):
+                 device="cuda", deterministic=True, record_capacity=None):
         """view_hw: per frame, a list of (H, W) per view.  targets: list of
         (frame, n_rays, S).  train_tsdf: train_step also scatters the gradient
         of the TSDF grid (the feature grid is always trained).  target_widths:
         per target the image width in pixels -- the targets are then cameras
         (n_rays = width x height, ray = pixel in row-major order) given by
-        load_cameras instead of ray buffers given by load_rays."""
+        load_cameras instead of ray buffers given by load_rays.
+        deterministic: train_step reduces the grid gradients by a sort over
+        cell ids (sg_render_segments_train_det: bit-identical gradients on
+        every run) instead of float atomics (sg_render_segments_train).
+        record_capacity: gradient-record slots of that reduction (default:
+        the sum of S over all rays, which always suffices)."""
         self.B = B = len(view_hw)
         self.D, self.rate, self.C, self.W = D, rate, C, W_hits
         self.train_tsdf = bool(train_tsdf)
@@ -192,6 +197,14 @@ class BatchPipeline:
         self.target_rgb = torch.zeros((R, 3), **f32)
         self.g_rgb = torch.empty((R, 3), **f32)
         self.out_loss = torch.empty(R, **f32)
+        # workspace of the deterministic gradient reduction
+        self.deterministic = bool(deterministic)
+        self.record_capacity = int(record_capacity if record_capacity is not None
+                                   else sum(n * s_ for _, n, s_ in self.targets))
+        self.det_ws = None
+        if self.deterministic:
+            nbytes = int(N.lib.sg_train_det_workspace_bytes(R, T, C, self.record_capacity))
+            self.det_ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
         self.args = None
         self.trunc_weight = None
         self.events = None
@@ -264,6 +277,9 @@ class BatchPipeline:
             seg = N.SgRaySegments(g1 - g0, int(rb[g1]), self.seg_begin.data_ptr() + 4 * g0,
                                   self.seg_frame.data_ptr() + 4 * g0, self.seg_samples.data_ptr() + 4 * g0)
             self._group_launch.append((seg, args(sm)))
+        ng = len(self._groups)
+        self._det_groups = (C.c_int * (ng + 1))(*([g0 for g0, _, _ in self._groups] + [len(self.targets)]))
+        self._det_group_S = (C.c_int * ng)(*[sm for _, _, sm in self._groups])
         return self.args
 
     def _mark(self, name):
@@ -359,12 +375,21 @@ class BatchPipeline:
         self.build(before_tree=lambda: main.wait_stream(self.side))
         self.intersect()
         self._mark("grad_prep")
-        for seg, args in self._group_launch:
-            N.check(N.lib.sg_render_segments_train(
-                C.byref(self.tree), C.byref(seg), C.byref(args), N.ptr(self.target_rgb),
-                2.0 / (3.0 * self.R), N.ptr(self.out_rgb), N.ptr(self.out_depth), N.ptr(self.out_ws),
-                N.ptr(self.out_alpha), N.ptr(self.out_loss), N.ptr(self.grad_feat),
-                N.ptr(self.grad_tsdf) if self.train_tsdf else None, N.stream()), "render_train")
+        loss_scale = 2.0 / (3.0 * self.R)
+        tsdf = N.ptr(self.grad_tsdf) if self.train_tsdf else None
+        if self.deterministic:
+            N.check(N.lib.sg_render_segments_train_det(
+                C.byref(self.tree), C.byref(self.seg), C.byref(self.args), len(self._groups), self._det_groups,
+                self._det_group_S, N.ptr(self.target_rgb), loss_scale, N.ptr(self.out_rgb), N.ptr(self.out_depth),
+                N.ptr(self.out_ws), N.ptr(self.out_alpha), N.ptr(self.out_loss), N.ptr(self.grad_feat), tsdf,
+                N.ptr(self.det_ws), self.det_ws.numel(), self.record_capacity, N.ptr(self.status), N.stream()),
+                "render_train_det")
+        else:
+            for seg, args in self._group_launch:
+                N.check(N.lib.sg_render_segments_train(
+                    C.byref(self.tree), C.byref(seg), C.byref(args), N.ptr(self.target_rgb), loss_scale,
+                    N.ptr(self.out_rgb), N.ptr(self.out_depth), N.ptr(self.out_ws), N.ptr(self.out_alpha),
+                    N.ptr(self.out_loss), N.ptr(self.grad_feat), tsdf, N.stream()), "render_train")
         self.grad_bricks.copy_(self.brick_node)
         self._mark("train")
 

@@ -60,7 +60,8 @@ __global__ void __launch_bounds__(256) grid_gather_kernel(GatherParams p) {
       float pt[3];
 #pragma unroll
       for (int a = 0; a < 3; a++) pt[a] = __fmaf_rn(__ldg(p.dir + r * 3 + a), zz, __ldg(p.ori + r * 3 + a));
-      grid_tap<C>(p.grid + (size_t)b * p.D * p.D * p.D * C, p.D, bmin, 1.0f / __ldg(p.voxel_size + b), pt, acc);
+      grid_tap<C>(p.grid + (size_t)b * p.D * p.D * p.D * C, p.D, bmin, __ldg(p.voxel_size + b),
+                  1.0f / __ldg(p.voxel_size + b), pt, acc);
       if (p.mode == 1) acc[0] = tsdf_density(acc[0], p.scale / p.s, 1.0f / p.s);
     }
 #pragma unroll
@@ -110,7 +111,8 @@ __global__ void __launch_bounds__(256) grid_scatter_kernel(ScatterParams p) {
     const int b = (int)(r / p.N);
     const float *bb = p.vol_bbox + 6 * b;
     const float bmin[3] = {bb[0], bb[2], bb[4]};
-    const float inv_vs = 1.0f / __ldg(p.voxel_size + b);
+    const float vs = __ldg(p.voxel_size + b);
+    const float inv_vs = 1.0f / vs;
     float acc[NSLOT];
 #pragma unroll
     for (int q = 0; q < NSLOT; q++) acc[q] = 0.0f;
@@ -125,7 +127,7 @@ __global__ void __launch_bounds__(256) grid_scatter_kernel(ScatterParams p) {
         int i0[3];
 #pragma unroll
         for (int a = 0; a < 3; a++) pt[a] = __fmaf_rn(__ldg(p.dir + r * 3 + a), zz, __ldg(p.ori + r * 3 + a));
-        tap_cell(bmin, inv_vs, pt, i0, wc);
+        tap_cell(bmin, vs, inv_vs, pt, i0, wc);
 #pragma unroll
         for (int cr = 0; cr < 8; cr++) s_w[w8][lane][cr] = wc[cr];
         s_cell[w8][lane][0] = i0[0];

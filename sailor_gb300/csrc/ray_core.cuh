@@ -383,7 +383,7 @@ __device__ __forceinline__ void ray_alpha(const float (&z)[E], const float (&sg)
           delta = s_z[m] - z[e];
         }
         dl[e] = delta;
-        al[e] = 1.0f - __expf(-sg[e] * delta);
+        al[e] = 1.0f - expf(-sg[e] * delta);
       }
     }
   } else {
@@ -499,23 +499,49 @@ __device__ __forceinline__ void ray_transmittance(const float (&al)[E], unsigned
 // (x,y,z) centred at bbox_min + (x,y,z) * vs, outside corners contribute 0)
 // ---------------------------------------------------------------------------
 // Cell (lower corner index) and the eight corner weights of a trilinear tap
-// at pt (u = (pt - bmin) * inv_vs in voxel units); corner cr = (dx, dy, dz)
-// = bits (2, 1, 0) of cr.
-__device__ __forceinline__ void tap_cell(const float bmin[3], float inv_vs, const float pt[3], int (&i0)[3],
-                                         float (&w)[8]) {
-  float f[3];
+// at pt, in voxel units u = (pt - bmin) / vs; corner cr = (dx, dy, dz) =
+// bits (2, 1, 0) of cr.  The fraction of u is formed to about 1e-7 of a
+// voxel: pt - bmin as an exact two-term sum (Knuth's two-sum), then the
+// quotient's remainder from a fused multiply-add carried into the
+// fraction.  A plain (pt - bmin) * inv_vs is off by up to ~3e-5 voxel at
+// u ~ 250, which the steep density transform turns into density errors of
+// ~1e-3 and composited errors above 1e-5.
+__device__ __forceinline__ void tap_frac(const float bmin[3], float vs, float inv_vs, const float pt[3],
+                                         int (&i0)[3], float (&f)[3]) {
 #pragma unroll
   for (int a = 0; a < 3; a++) {
-    const float u = (pt[a] - bmin[a]) * inv_vs;
-    const float fl = floorf(u);
+    const float nb = -bmin[a];
+    const float dh = pt[a] + nb;                         // pt - bmin, rounded
+    const float bv = dh - pt[a];
+    const float dl = (pt[a] - (dh - bv)) + (nb - bv);    // its rounding error (two-sum)
+    const float uh = dh * inv_vs;
+    const float ul = (__fmaf_rn(-uh, vs, dh) + dl) * inv_vs;  // (pt - bmin) / vs - uh
+    float fl = floorf(uh);
+    float fr = (uh - fl) + ul;
+    if (fr < 0.0f) {
+      fl -= 1.0f;
+      fr += 1.0f;
+    } else if (fr >= 1.0f) {
+      fl += 1.0f;
+      fr -= 1.0f;
+    }
     i0[a] = (int)fl;
-    f[a] = u - fl;
+    f[a] = fr;
   }
+}
+
+// Weight of corner cr = (dx, dy, dz) = bits (2, 1, 0) of cr at fractions f.
+__device__ __forceinline__ float corner_weight(const float (&f)[3], int cr) {
+  const int dx = (cr >> 2) & 1, dy = (cr >> 1) & 1, dz = cr & 1;
+  return (dx ? f[0] : 1.0f - f[0]) * (dy ? f[1] : 1.0f - f[1]) * (dz ? f[2] : 1.0f - f[2]);
+}
+
+__device__ __forceinline__ void tap_cell(const float bmin[3], float vs, float inv_vs, const float pt[3],
+                                         int (&i0)[3], float (&w)[8]) {
+  float f[3];
+  tap_frac(bmin, vs, inv_vs, pt, i0, f);
 #pragma unroll
-  for (int cr = 0; cr < 8; cr++) {
-    const int dx = (cr >> 2) & 1, dy = (cr >> 1) & 1, dz = cr & 1;
-    w[cr] = (dx ? f[0] : 1.0f - f[0]) * (dy ? f[1] : 1.0f - f[1]) * (dz ? f[2] : 1.0f - f[2]);
-  }
+  for (int cr = 0; cr < 8; cr++) w[cr] = corner_weight(f, cr);
 }
 
 __device__ __forceinline__ bool corner_inside(const int (&i0)[3], int cr, int D, size_t &off) {
@@ -554,11 +580,11 @@ __device__ __forceinline__ void grid_tap_cell(const float *__restrict__ grid, in
 }
 
 template <int C>
-__device__ __forceinline__ void grid_tap(const float *__restrict__ grid, int D, const float bmin[3], float inv_vs,
-                                         const float pt[3], float (&acc)[C]) {
+__device__ __forceinline__ void grid_tap(const float *__restrict__ grid, int D, const float bmin[3], float vs,
+                                         float inv_vs, const float pt[3], float (&acc)[C]) {
   int i0[3];
   float w[8];
-  tap_cell(bmin, inv_vs, pt, i0, w);
+  tap_cell(bmin, vs, inv_vs, pt, i0, w);
   grid_tap_cell<C>(grid, D, i0, w, acc);
 }
 
@@ -566,7 +592,7 @@ __device__ __forceinline__ void grid_tap(const float *__restrict__ grid, int D, 
 // k = scale / s and inv_s = 1 / s folded by the caller.  tsdf_sigmoid is
 // the sigmoid factor (kept by the adjoint: d sigma / d t = -k inv_s sg (1 - sg)).
 __device__ __forceinline__ float tsdf_sigmoid(float t, float k) {
-  return __fdividef(1.0f, 1.0f + __expf(t * k));
+  return 1.0f / (1.0f + expf(t * k));
 }
 __device__ __forceinline__ float tsdf_density(float t, float k, float inv_s) { return tsdf_sigmoid(t, k) * inv_s; }
 

@@ -29,6 +29,7 @@
 #include <climits>
 
 #include "ray_core.cuh"
+#include "scatter.cuh"
 
 namespace sg {
 
@@ -58,6 +59,17 @@ struct RenderParams {
   const float *target_rgb;
   float loss_scale;
   float *out_loss;
+  // gradient records instead of the scatter (deterministic reduction,
+  // scatter.cu): the launch's rays are hit_ray[k], k in [*k_begin, *k_end);
+  // the sample at sorted position q of ray k goes to record slot
+  // hit_slot[k] + q (below rec_cap)
+  const int *hit_ray, *hit_slot, *k_begin, *k_end;
+  uint32_t *rec_key;
+  float4 *rec_f;
+  int2 *rec_kt;
+  float *ray_g;  // [k][C]: head^T (colour gradient of ray k)
+  long rec_cap;
+  RecordKeys keys;
 };
 
 __device__ __forceinline__ void ray_frame(const RenderParams &p, long r, int &b, int &S, int &s) {
@@ -101,10 +113,10 @@ __device__ __forceinline__ void eval_ray(const RenderParams &p, long r, int b, i
   warp_sort_samples<E, POS>(sm.z, sm.p, S, ev.done);
   const float *bb = p.sp.t.vol_bbox + 6 * b;
   const float bmin[3] = {bb[0], bb[2], bb[4]};
-  const float inv_vs = 1.0f / __ldg(p.sp.t.voxel_size + b);
+  const float vs = __ldg(p.sp.t.voxel_size + b), inv_vs = 1.0f / vs;
   const float *fb = p.fbbox + 6 * b;
   const float fmin[3] = {fb[0], fb[2], fb[4]};
-  const float inv_fvs = 1.0f / __ldg(p.fvs + b);
+  const float fvs = __ldg(p.fvs + b), inv_fvs = 1.0f / fvs;
   const float *tsdf = p.tsdf + (size_t)b * p.D * p.D * p.D;
   const float *feat = p.feat + (size_t)b * p.Df * p.Df * p.Df * C;
   const float o[3] = {__ldg(p.ori + r * 3), __ldg(p.ori + r * 3 + 1), __ldg(p.ori + r * 3 + 2)};
@@ -121,12 +133,12 @@ __device__ __forceinline__ void eval_ray(const RenderParams &p, long r, int b, i
                            __fmaf_rn(dr[2], ev.z[e], o[2])};
       int i0[3];
       float wc[8];
-      tap_cell(bmin, inv_vs, pt, i0, wc);
+      tap_cell(bmin, vs, inv_vs, pt, i0, wc);
       float t1[1];
       grid_tap_cell<1>(tsdf, p.D, i0, wc, t1);
       ev.s01[e] = tsdf_sigmoid(t1[0], p.dk);  // kept for the adjoint
       ev.sg[e] = ev.s01[e] * p.inv_s;
-      if (!p.shared) tap_cell(fmin, inv_fvs, pt, i0, wc);
+      if (!p.shared) tap_cell(fmin, fvs, inv_fvs, pt, i0, wc);
       float fe[C];
       grid_tap_cell<C>(feat, p.Df, i0, wc, fe);
       if (p.head) {
@@ -263,6 +275,58 @@ __device__ __forceinline__ void flush_tsdf(const RenderParams &p, int b, const C
   acc = 0.0f;
 }
 
+// Records of ray r (compact index k) for the deterministic reduction of the
+// grid gradients.  The colour head is linear, so the feature gradient of
+// the sample at sorted position i is w_i G with G = head^T g_c (g_c: the
+// gradient of the ray's colour, w_i its compositing weight): G goes to
+// ray_g[k] once per ray, and each used sample's record holds its cell (the
+// key), its cell fractions and w_i, the ray and its TSDF gradient.  Positions
+// without a contribution get the key no cell has.
+template <int E, int C>
+__device__ __forceinline__ void emit_records(const RenderParams &p, long k, long r, int b, int S,
+                                             const RayEval<E> &ev, const float (&w)[E], const float (&gsig)[E],
+                                             const float (&gc)[3]) {
+  const int lane = lane_id();
+  if (lane < C) {
+    float g;
+    if (p.head)
+      g = __fmaf_rn(__ldg(p.head + 2 * C + lane), gc[2], __fmaf_rn(__ldg(p.head + C + lane), gc[1],
+                                                                    __ldg(p.head + lane) * gc[0]));
+    else
+      g = lane < 3 ? gc[lane] : 0.0f;
+    p.ray_g[k * C + lane] = g;
+  }
+  const long base = __ldg(p.hit_slot + k);
+  const float *fb = p.fbbox + 6 * b;
+  const float fmin[3] = {fb[0], fb[2], fb[4]};
+  const float fvs = __ldg(p.fvs + b), inv_fvs = 1.0f / fvs;
+  const float o[3] = {__ldg(p.ori + r * 3), __ldg(p.ori + r * 3 + 1), __ldg(p.ori + r * 3 + 2)};
+  const float dr[3] = {__ldg(p.dir + r * 3), __ldg(p.dir + r * 3 + 1), __ldg(p.dir + r * 3 + 2)};
+  const float dsdt_k = -p.dk * p.inv_s;
+  const unsigned used = ev.proc & ev.valid;
+#pragma unroll
+  for (int e = 0; e < E; e++) {
+    const int i = e * 32 + lane;
+    const long slot = base + i;
+    if (i >= S || slot >= p.rec_cap) continue;
+    uint32_t key = p.keys.invalid;
+    if ((used >> e) & 1u) {
+      const float pt[3] = {__fmaf_rn(dr[0], ev.z[e], o[0]), __fmaf_rn(dr[1], ev.z[e], o[1]),
+                           __fmaf_rn(dr[2], ev.z[e], o[2])};
+      int i0[3];
+      float f[3];
+      tap_frac(fmin, fvs, inv_fvs, pt, i0, f);
+      key = record_key(p.keys, b, i0);
+      if (key != p.keys.invalid) {
+        const float gt = p.grad_tsdf ? gsig[e] * (ev.s01[e] * (1.0f - ev.s01[e]) * dsdt_k) : 0.0f;
+        p.rec_f[slot] = make_float4(f[0], f[1], f[2], w[e]);
+        p.rec_kt[slot] = make_int2((int)k, __float_as_int(gt));
+      }
+    }
+    p.rec_key[slot] = key;
+  }
+}
+
 // TRAIN: the upstream gradient is formed in the kernel from the ray's own
 // outputs (loss = loss_scale / 2 * |rgb - target|^2 per ray, so d loss /
 // d rgb = loss_scale * (rgb - target)); the outputs and per-ray loss are
@@ -274,25 +338,36 @@ __device__ __forceinline__ void flush_tsdf(const RenderParams &p, int b, const C
 template <int E, bool TRAIN>
 constexpr int kBwdMinBlocks = !TRAIN ? 2 : (E == 1 ? 4 : (E == 2 ? 3 : 2));
 
-template <int E, int C, bool TRAIN>
+// REC: the rays are the compact list of rays with hits and the grid
+// gradients leave the kernel as per-sample records (emit_records) for the
+// deterministic reduction, instead of the in-kernel scatter with atomics.
+template <int E, int C, bool TRAIN, bool REC>
 __global__ void __launch_bounds__(256, kBwdMinBlocks<E, TRAIN>) render_bwd_kernel(RenderParams p) {
   static_assert(C == 3 || C == 16, "feature grids of 3 or 16 channels");
   SG_RENDER_SMEM(E)
-  __shared__ float s_wf[8][32][9], s_wt[8][32][9];
-  __shared__ __align__(16) float s_g[8][32][C == 16 ? 20 : 4];
-  __shared__ long long s_kf[8][32], s_kt[8][32];  // packed cell keys, -1: no contribution
+  __shared__ float s_wf[REC ? 1 : 8][32][9], s_wt[REC ? 1 : 8][32][9];
+  __shared__ __align__(16) float s_g[REC ? 1 : 8][32][C == 16 ? 20 : 4];
+  __shared__ long long s_kf[REC ? 1 : 8][32], s_kt[REC ? 1 : 8][32];  // packed cell keys, -1: no contribution
   const int lane = lane_id();
   const int Smax = p.sp.S;
   // a segment table covers rays [ray_begin[0], total): a sub-table of
   // consecutive segments is a group of targets
-  const long r0 = p.nseg > 0 ? (long)__ldg(p.seg_begin) : 0;
-  for (long r = r0 + (((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5); r < p.R;
-       r += ((long)gridDim.x * blockDim.x) >> 5) {
+  const long it0 = REC ? (long)__ldg(p.k_begin) : (p.nseg > 0 ? (long)__ldg(p.seg_begin) : 0);
+  const long it1 = REC ? (long)__ldg(p.k_end) : p.R;
+  for (long it = it0 + (((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5); it < it1;
+       it += ((long)gridDim.x * blockDim.x) >> 5) {
+    const long r = REC ? (long)__ldg(p.hit_ray + it) : it;
     int b, S, sgm;
     ray_frame(p, r, b, S, sgm);
     RayEval<E> ev;
     eval_ray<E, C, false>(p, r, b, S, sgm, sm, ev);
     if (ev.done == 0) {
+      if (REC) {
+        // no sample: the ray's record slots carry no cell
+        const long base = __ldg(p.hit_slot + it);
+        for (int i = lane; i < S; i += 32)
+          if (base + i < p.rec_cap) p.rec_key[base + i] = p.keys.invalid;
+      }
       if (p.grad_sigma) {
         for (int i = lane; i < Smax; i += 32) {
           p.grad_sigma[(size_t)r * Smax + i] = 0.0f;
@@ -431,6 +506,11 @@ __global__ void __launch_bounds__(256, kBwdMinBlocks<E, TRAIN>) render_bwd_kerne
         for (int k = 0; k < 3; k++) p.grad_rgb[((size_t)r * Smax + i) * 3 + k] = 0.0f;
       }
     }
+    if (REC) {
+      emit_records<E, C>(p, it, r, b, S, ev, w, gsig, gc);
+      __syncwarp();
+      continue;
+    }
     if (!p.grad_feat && !p.grad_tsdf) {
       __syncwarp();
       continue;
@@ -438,10 +518,10 @@ __global__ void __launch_bounds__(256, kBwdMinBlocks<E, TRAIN>) render_bwd_kerne
     // scatter into the grids, samples in sorted order
     const float *bb = p.sp.t.vol_bbox + 6 * b;
     const float bmin[3] = {bb[0], bb[2], bb[4]};
-    const float inv_vs = 1.0f / __ldg(p.sp.t.voxel_size + b);
+    const float vs = __ldg(p.sp.t.voxel_size + b), inv_vs = 1.0f / vs;
     const float *fb = p.fbbox + 6 * b;
     const float fmin[3] = {fb[0], fb[2], fb[4]};
-    const float inv_fvs = 1.0f / __ldg(p.fvs + b);
+    const float fvs = __ldg(p.fvs + b), inv_fvs = 1.0f / fvs;
     const float o[3] = {__ldg(p.ori + r * 3), __ldg(p.ori + r * 3 + 1), __ldg(p.ori + r * 3 + 2)};
     const float dr[3] = {__ldg(p.dir + r * 3), __ldg(p.dir + r * 3 + 1), __ldg(p.dir + r * 3 + 2)};
     const float dsdt_k = -p.dk * p.inv_s;
@@ -464,7 +544,7 @@ __global__ void __launch_bounds__(256, kBwdMinBlocks<E, TRAIN>) render_bwd_kerne
                              __fmaf_rn(dr[2], ev.z[e], o[2])};
         int i0[3];
         float wt[8];
-        tap_cell(bmin, inv_vs, pt, i0, wt);
+        tap_cell(bmin, vs, inv_vs, pt, i0, wt);
         if (want_t) {
           kt = cell_key(i0, p.D);
 #pragma unroll
@@ -472,7 +552,7 @@ __global__ void __launch_bounds__(256, kBwdMinBlocks<E, TRAIN>) render_bwd_kerne
           s_g[w8][lane][C == 16 ? 16 : 3] = gsig[e] * (ev.s01[e] * (1.0f - ev.s01[e]) * dsdt_k);
         }
         if (want_f) {
-          if (!p.shared) tap_cell(fmin, inv_fvs, pt, i0, wt);
+          if (!p.shared) tap_cell(fmin, fvs, inv_fvs, pt, i0, wt);
           kf = cell_key(i0, p.Df);
 #pragma unroll
           for (int cr = 0; cr < 8; cr++) s_wf[w8][lane][cr] = wt[cr];
@@ -539,12 +619,14 @@ static int render_grid(long R) {
   return (int)(g < cap ? g : cap);
 }
 
-// mode 0: forward, 1: backward, 2: training step (forward + loss + backward)
+// mode 0: forward, 1: backward, 2: training step (forward + loss + backward),
+// 3: training step writing gradient records
 template <int E, int C>
 static void launch_render_e(const RenderParams &p, int mode, int g, sg_stream_t stream) {
   if (mode == 0) render_fwd_kernel<E, C><<<g, 256, 0, stream>>>(p);
-  else if (mode == 1) render_bwd_kernel<E, C, false><<<g, 256, 0, stream>>>(p);
-  else render_bwd_kernel<E, C, true><<<g, 256, 0, stream>>>(p);
+  else if (mode == 1) render_bwd_kernel<E, C, false, false><<<g, 256, 0, stream>>>(p);
+  else if (mode == 2) render_bwd_kernel<E, C, true, false><<<g, 256, 0, stream>>>(p);
+  else render_bwd_kernel<E, C, true, true><<<g, 256, 0, stream>>>(p);
 }
 
 template <int C>
@@ -712,4 +794,73 @@ extern "C" int sg_render_segments_train(const SgTree *tree, const SgRaySegments 
   p.grad_feat = grad_feat;
   p.grad_tsdf = grad_tsdf;
   return launch_render_c(p, args->C, 2, stream);
+}
+
+// ---------------------------------------------------------------------------
+// training step with the deterministic gradient reduction (scatter.cu)
+// ---------------------------------------------------------------------------
+extern "C" size_t sg_train_det_workspace_bytes(long long R, int nseg, int C, long long capacity) {
+  if (R < 0 || nseg < 0 || C <= 0 || capacity < 0) return 0;
+  return det_layout((long)R, nseg, C, (long)(capacity > 0 ? capacity : 1), nullptr, nullptr);
+}
+
+extern "C" int sg_render_segments_train_det(const SgTree *tree, const SgRaySegments *seg, const SgRenderArgs *args,
+                                            int ngroups, const int *groups, const int *group_S,
+                                            const float *target_rgb, float loss_scale, float *out_rgb,
+                                            float *out_depth, float *out_ws, float *out_alpha, float *out_loss,
+                                            float *grad_feat, float *grad_tsdf, void *workspace,
+                                            size_t workspace_bytes, long long capacity, SgStatus *status,
+                                            sg_stream_t stream) {
+  RenderParams p;
+  int rc = segment_params(tree, seg, args, p);
+  if (rc != SG_OK) return rc;
+  if (!target_rgb || !out_rgb || !out_depth || !out_ws || !out_alpha || !grad_feat || !workspace) return SG_ERR_INVALID_ARG;
+  if (ngroups <= 0 || !groups || !group_S || groups[0] != 0 || groups[ngroups] != seg->count) return SG_ERR_INVALID_ARG;
+  for (int g = 0; g < ngroups; g++)
+    if (groups[g + 1] <= groups[g] || group_S[g] <= 0 || group_S[g] > args->S) return SG_ERR_INVALID_ARG;
+  if (capacity <= 0 || capacity >= (1ll << 31)) return SG_ERR_INVALID_ARG;
+  if (grad_tsdf && !p.shared) return SG_ERR_UNSUPPORTED;
+  if (args->C != 3 && args->C != 16) return SG_ERR_UNSUPPORTED;
+  if (!record_keys_fit(tree->B, args->Df)) return SG_ERR_UNSUPPORTED;
+  const long R = seg->total;
+  if (workspace_bytes < det_layout(R, seg->count, args->C, (long)capacity, nullptr, nullptr))
+    return SG_ERR_INVALID_ARG;
+  if (((uintptr_t)workspace) % 256 != 0) return SG_ERR_INVALID_ARG;
+  if (R == 0) return SG_OK;
+  if (!args->hit_count) return SG_ERR_INVALID_ARG;  // the ray scan reads the hit counts
+  DetWork w;
+  det_layout(R, seg->count, args->C, (long)capacity, (char *)workspace, &w);
+  DetTrainOut o{target_rgb, loss_scale, out_rgb, out_depth, out_ws, out_alpha, out_loss};
+  rc = launch_det_prepare(w, *seg, args->S, args->hit_count, R, (long)capacity, o, status, stream);
+  if (rc != SG_OK) return rc;
+  p.target_rgb = target_rgb;
+  p.loss_scale = loss_scale;
+  p.out_loss = out_loss;
+  p.out_rgb = out_rgb;
+  p.out_depth = out_depth;
+  p.out_ws = out_ws;
+  p.out_alpha = out_alpha;
+  p.grad_feat = grad_feat;
+  p.grad_tsdf = grad_tsdf;
+  p.hit_ray = w.hit_ray;
+  p.hit_slot = w.hit_slot;
+  p.rec_key = w.rec_key;
+  p.rec_f = w.rec_f;
+  p.rec_kt = w.rec_kt;
+  p.ray_g = w.ray_g;
+  p.rec_cap = (long)capacity;
+  p.keys = make_record_keys(tree->B, args->Df);
+  for (int g = 0; g < ngroups; g++) {
+    RenderParams pg = p;
+    pg.sp.S = group_S[g];
+    pg.k_begin = w.seg_hit + groups[g];
+    pg.k_end = w.seg_hit + groups[g + 1];
+    // the group's count of rays with hits is on the device: the grid is the
+    // persistent cap, its warps striding over the compact range
+    const int gsz = render_grid(R);
+    if (args->C == 3) rc = launch_render<3>(pg, 3, gsz, stream);
+    else rc = launch_render<16>(pg, 3, gsz, stream);
+    if (rc != SG_OK) return rc;
+  }
+  return launch_det_reduce(w, p.keys, (long)capacity, args->C, grad_feat, grad_tsdf, stream);
 }

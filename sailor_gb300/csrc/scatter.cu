@@ -1,0 +1,277 @@
+// scatter.cu -- deterministic reduction of the training pass's grid
+// gradients: a segmented reduction over the sampled cells, sorted.
+//
+// The in-kernel scatter of the render backward adds each cell run's
+// gradient into the grids with float atomics, so the summation order -- and
+// the last bits of the gradient -- change from run to run.  Here the
+// training pass (render.cu, record mode) writes one record per used sample
+// instead: the sample's trilinear cell as a 32-bit key (frame and lower
+// corner, grouped by parity class), its cell fractions, its compositing
+// weight, its ray and its TSDF gradient; the ray's colour-head factor of the
+// feature gradient goes to a per-ray table.  Then
+//   1. the keys are sorted, stably, with the record slots as values
+//      (segsort.cu): records of one cell become one run, in slot order (ray
+//      order, then sorted sample order -- fixed by the ray layout);
+//   2. run heads are flagged and scanned into the list of distinct cells;
+//   3. for each of the 8 parity classes in turn, one warp per cell sums its
+//      run in order into the 8 corners x C channels it touches (lane = corner
+//      x 4 channels) and adds the sums into the grids.  Cells of one class
+//      share no corner, so every grid value is updated by one warp per
+//      class, classes in a fixed order.
+// Every grid value is therefore the same sum in the same order on every run:
+// the gradients are bit-identical across runs, launch shapes and graph
+// replays.
+//
+// Before the training pass, a scan over the rays (rays with hits, and their
+// record slots: S per ray with hits) builds the compact list of rays the
+// pass visits; rays without hits get their outputs (0, and the loss of the
+// target alone) here.
+#include "ray_core.cuh"
+#include "scatter.cuh"
+#include "segsort.cuh"
+
+namespace sg {
+
+__device__ __forceinline__ long ray_samples(const SgRaySegments &seg, int S_max, long r, int &s) {
+  s = segment_of(seg.ray_begin, seg.count, r);
+  const int S = __ldg(seg.samples + s);
+  return S < S_max ? S : S_max;
+}
+
+// hit flag and record slots per ray
+__global__ void det_ray_counts_kernel(SgRaySegments seg, int S_max, const int *__restrict__ hit_count, long R,
+                                      int *__restrict__ hitb, int *__restrict__ slotb) {
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < R; r += (long)gridDim.x * blockDim.x) {
+    int s;
+    const long S = ray_samples(seg, S_max, r, s);
+    const bool h = __ldg(hit_count + r) > 0;
+    hitb[r] = h ? 1 : 0;
+    slotb[r] = h ? (int)S : 0;
+  }
+}
+
+// compact ray list and slots; outputs of rays without hits
+__global__ void det_ray_emit_kernel(long R, const int *__restrict__ hit_count, const int *__restrict__ hitb,
+                                    const int *__restrict__ slotb, int *__restrict__ hit_ray,
+                                    int *__restrict__ hit_slot, DetTrainOut o) {
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < R; r += (long)gridDim.x * blockDim.x) {
+    if (__ldg(hit_count + r) > 0) {
+      const int k = hitb[r];
+      hit_ray[k] = (int)r;
+      hit_slot[k] = slotb[r];
+    } else if (o.out_rgb) {
+      float l = 0.0f;
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const float t = __ldg(o.target_rgb + r * 3 + c);
+        o.out_rgb[r * 3 + c] = 0.0f;
+        l += t * t;
+      }
+      o.out_depth[r] = o.out_ws[r] = o.out_alpha[r] = 0.0f;
+      if (o.out_loss) o.out_loss[r] = 0.5f * o.loss_scale * l;
+    }
+  }
+}
+
+// compact index of each segment's first ray; slots used (clamped to the
+// capacity) and the capacity flag
+__global__ void det_seg_kernel(SgRaySegments seg, long R, const int *__restrict__ hitb, int *__restrict__ cnt,
+                               int *__restrict__ seg_hit, long cap, SgStatus *st) {
+  for (int s = threadIdx.x; s <= seg.count; s += blockDim.x) {
+    const long rb = __ldg(seg.ray_begin + s);
+    seg_hit[s] = rb < R ? hitb[rb] : cnt[kDetHits];
+  }
+  if (threadIdx.x == 0) {
+    const int need = cnt[kDetSlotsNeeded];
+    cnt[kDetSlots] = need < cap ? need : (int)cap;
+    if (need > cap && st) {
+      atomicOr(&st->flags, SG_FLAG_RECORD_CAPACITY);
+    }
+  }
+}
+
+// head flags of the sorted keys' runs (cells), over the live records
+__global__ void det_heads_kernel(const uint32_t *__restrict__ key, const int *__restrict__ cnt, uint32_t invalid,
+                                 int *__restrict__ head) {
+  const long n = cnt[kDetSlots];
+  for (long j = (long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x) {
+    const uint32_t k = __ldg(key + j);
+    head[j] = (k != invalid && (j == 0 || __ldg(key + j - 1) != k)) ? 1 : 0;
+  }
+}
+
+// distinct cells: key and first sorted position; the end of the last run
+__global__ void det_unique_kernel(const uint32_t *__restrict__ key, const int *__restrict__ head_scan,
+                                  const int *__restrict__ cnt, uint32_t invalid, uint32_t *__restrict__ ukey,
+                                  int *__restrict__ ustart) {
+  const long n = cnt[kDetSlots];
+  const int nu = cnt[kDetCells];
+  for (long j = (long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x) {
+    const uint32_t k = __ldg(key + j);
+    if (k == invalid) continue;
+    if (j == 0 || __ldg(key + j - 1) != k) {
+      const int u = head_scan[j];
+      ukey[u] = k;
+      ustart[u] = (int)j;
+    }
+    if (j + 1 == n || __ldg(key + j + 1) == invalid) ustart[nu] = (int)(j + 1);
+  }
+}
+
+__device__ __forceinline__ int lower_bound_u32(const uint32_t *a, int n, uint32_t v) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(a + mid) < v) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Cells of parity class cls: warp per cell, its run summed in order, the
+// sums added into the 8 corner voxels of the feature grid (and TSDF grid).
+template <int C>
+__global__ void __launch_bounds__(256) det_class_kernel(DetReduceParams q, int cls) {
+  __shared__ int s_rng[2];
+  const int nu = q.cnt[kDetCells];
+  if (threadIdx.x == 0) {
+    s_rng[0] = lower_bound_u32(q.ukey, nu, (uint32_t)cls * q.keys.cls);
+    s_rng[1] = lower_bound_u32(q.ukey, nu, (uint32_t)(cls + 1) * q.keys.cls);
+  }
+  __syncthreads();
+  const int lo = s_rng[0], hi = s_rng[1];
+  const int lane = lane_id();
+  // lane -> (corner, channels): C == 16: corner lane / 4, channels 4 (lane % 4)..+3;
+  // C == 3: lanes < 24, corner lane / 3, channel lane % 3.  TSDF: corner = lane (< 8).
+  const int cr = C == 16 ? (lane >> 2) : (lane < 24 ? lane / 3 : 0);
+  const int ch = C == 16 ? 4 * (lane & 3) : (lane < 24 ? lane % 3 : 0);
+  const bool fown = C == 16 || lane < 24;
+  const long D = q.keys.D;
+  for (long u = lo + (((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5); u < hi;
+       u += ((long)gridDim.x * blockDim.x) >> 5) {
+    const int j0 = __ldg(q.ustart + u), j1 = __ldg(q.ustart + u + 1);
+    float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float acct = 0.0f;
+    for (int j = j0; j < j1; j++) {
+      const uint32_t slot = __ldg(q.sorted_slot + j);
+      const float4 fw = __ldg(q.rec_f + slot);
+      const int2 kt = __ldg(q.rec_kt + slot);
+      const float f[3] = {fw.x, fw.y, fw.z};
+      const float wc = corner_weight(f, cr);
+      const float a = wc * fw.w;
+      if (C == 16) {
+        const float4 g = __ldg(reinterpret_cast<const float4 *>(q.ray_g + (size_t)kt.x * C + ch));
+        acc.x = __fmaf_rn(a, g.x, acc.x);
+        acc.y = __fmaf_rn(a, g.y, acc.y);
+        acc.z = __fmaf_rn(a, g.z, acc.z);
+        acc.w = __fmaf_rn(a, g.w, acc.w);
+      } else if (fown) {
+        acc.x = __fmaf_rn(a, __ldg(q.ray_g + (size_t)kt.x * C + ch), acc.x);
+      }
+      if (q.grad_tsdf && lane < 8) acct = __fmaf_rn(corner_weight(f, lane), __int_as_float(kt.y), acct);
+    }
+    int b, i0[3];
+    record_cell(q.keys, __ldg(q.ukey + u), b, i0);
+    const int vx = i0[0] + ((cr >> 2) & 1), vy = i0[1] + ((cr >> 1) & 1), vz = i0[2] + (cr & 1);
+    if (fown && vx >= 0 && vy >= 0 && vz >= 0 && vx < D && vy < D && vz < D) {
+      float *g = q.grad_feat + ((((size_t)b * D + vx) * D + vy) * D + vz) * C + ch;
+      if (C == 16) {
+        float4 v = *reinterpret_cast<float4 *>(g);
+        v.x += acc.x;
+        v.y += acc.y;
+        v.z += acc.z;
+        v.w += acc.w;
+        *reinterpret_cast<float4 *>(g) = v;
+      } else {
+        *g += acc.x;
+      }
+    }
+    if (q.grad_tsdf && lane < 8) {
+      const int tx = i0[0] + ((lane >> 2) & 1), ty = i0[1] + ((lane >> 1) & 1), tz = i0[2] + (lane & 1);
+      if (tx >= 0 && ty >= 0 && tz >= 0 && tx < D && ty < D && tz < D)
+        q.grad_tsdf[(((size_t)b * D + tx) * D + ty) * D + tz] += acct;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// workspace
+// ---------------------------------------------------------------------------
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+size_t det_layout(long R, int nseg, int C, long cap, char *base, DetWork *w) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char *p = base ? base + off : nullptr;
+    off += align256(bytes);
+    return p;
+  };
+  DetWork d{};
+  d.cnt = (int *)take(kDetCounters * sizeof(int));
+  d.hitb = (int *)take((size_t)R * 4);
+  d.slotb = (int *)take((size_t)R * 4);
+  d.hit_ray = (int *)take((size_t)R * 4);
+  d.hit_slot = (int *)take((size_t)R * 4);
+  d.seg_hit = (int *)take((size_t)(nseg + 1) * 4);
+  d.ray_g = (float *)take((size_t)R * C * 4);
+  d.rec_key = (uint32_t *)take((size_t)cap * 4);
+  d.rec_f = (float4 *)take((size_t)cap * 16);
+  d.rec_kt = (int2 *)take((size_t)cap * 8);
+  // one more than cap: after the sort, one of the pairs holds the distinct
+  // cells' first positions and the end of the last run
+  d.ka = (uint32_t *)take((size_t)(cap + 1) * 4);
+  d.va = (uint32_t *)take((size_t)(cap + 1) * 4);
+  d.kb = (uint32_t *)take((size_t)(cap + 1) * 4);
+  d.vb = (uint32_t *)take((size_t)(cap + 1) * 4);
+  d.sort_scratch = take(radix_scratch_bytes(cap));
+  const size_t sc = scan_scratch_ints(R) > scan_scratch_ints(cap) ? scan_scratch_ints(R) : scan_scratch_ints(cap);
+  d.scan_scratch = (int *)take(sc * 4);
+  if (w) *w = d;
+  return off;
+}
+
+static int grid_for(long n, int per_sm = 8) {
+  long g = (n + 255) / 256;
+  const long cap = (long)num_sms() * per_sm;
+  if (g > cap) g = cap;
+  return (int)(g < 1 ? 1 : g);
+}
+
+int launch_det_prepare(const DetWork &w, const SgRaySegments &seg, int S_max, const int *hit_count, long R,
+                       long cap, const DetTrainOut &o, SgStatus *status, sg_stream_t stream) {
+  det_ray_counts_kernel<<<grid_for(R), 256, 0, stream>>>(seg, S_max, hit_count, R, w.hitb, w.slotb);
+  launch_excl_scan(w.hitb, R, w.hitb, w.scan_scratch, w.cnt + kDetHits, stream);
+  launch_excl_scan(w.slotb, R, w.slotb, w.scan_scratch, w.cnt + kDetSlotsNeeded, stream);
+  det_ray_emit_kernel<<<grid_for(R), 256, 0, stream>>>(R, hit_count, w.hitb, w.slotb, w.hit_ray, w.hit_slot, o);
+  det_seg_kernel<<<1, 256, 0, stream>>>(seg, R, w.hitb, w.cnt, w.seg_hit, cap, status);
+  SG_LAUNCH_CHECK();
+  return SG_OK;
+}
+
+int launch_det_reduce(const DetWork &w, const RecordKeys &keys, long cap, int C, float *grad_feat, float *grad_tsdf,
+                      sg_stream_t stream) {
+  int key_bits = 1;
+  while (key_bits < 32 && ((uint64_t)1 << key_bits) <= (uint64_t)keys.invalid) key_bits++;
+  const int passes = launch_radix_sort(w.rec_key, w.cnt + kDetSlots, cap, key_bits, w.ka, w.va, w.kb, w.vb,
+                                       w.sort_scratch, stream);
+  const uint32_t *skey = (passes & 1) ? w.ka : w.kb;
+  const uint32_t *sval = (passes & 1) ? w.va : w.vb;
+  // the other pair is free now: head flags and their scan in one buffer,
+  // the distinct cells' first positions in the other; their keys where the
+  // unsorted keys were
+  int *heads = (int *)((passes & 1) ? w.kb : w.ka);
+  int *ustart = (int *)((passes & 1) ? w.vb : w.va);
+  uint32_t *ukey = w.rec_key;
+  det_heads_kernel<<<grid_for(cap, 16), 256, 0, stream>>>(skey, w.cnt, keys.invalid, heads);
+  launch_excl_scan_dev(heads, cap, w.cnt + kDetSlots, heads, w.scan_scratch, w.cnt + kDetCells, stream);
+  det_unique_kernel<<<grid_for(cap, 16), 256, 0, stream>>>(skey, heads, w.cnt, keys.invalid, ukey, ustart);
+  DetReduceParams q{keys, w.cnt, ukey, ustart, sval, w.rec_f, w.rec_kt, w.ray_g, grad_feat, grad_tsdf};
+  for (int cls = 0; cls < 8; cls++) {
+    if (C == 16) det_class_kernel<16><<<num_sms() * 8, 256, 0, stream>>>(q, cls);
+    else det_class_kernel<3><<<num_sms() * 8, 256, 0, stream>>>(q, cls);
+  }
+  SG_LAUNCH_CHECK();
+  return SG_OK;
+}
+
+}  // namespace sg

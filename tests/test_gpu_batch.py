@@ -252,23 +252,109 @@ def test_fused_backward_matches_modular_autograd(work):
         assert (gs[a:b, Sr:] == 0).all()
 
 
-def test_train_step_graph_replay(work):
+@pytest.mark.parametrize("train_tsdf", [False, True])
+def test_train_step_graph_replay(work, train_tsdf):
+    """A CUDA-graph replay of train_step gives the eager step's outputs and
+    gradients bit for bit (the deterministic gradient reduction), after the
+    grids held stale values where the step clears."""
     bp = _pipeline(work)
+    bp.train_tsdf = train_tsdf
     bp.train_step()
     torch.cuda.synchronize()
-    ref = [t.clone() for t in (bp.out_rgb, bp.out_depth, bp.tsdf, bp.grad_feat, bp.grad_tsdf)]
+    ref = [t.clone() for t in (bp.out_rgb, bp.out_depth, bp.tsdf, bp.grad_feat, bp.grad_tsdf, bp.out_loss)]
+    assert ref[3].abs().max().item() > 0 and (not train_tsdf or ref[4].abs().max().item() > 0)
     g = bp.capture()
-    # stale values where the step clears (the grids are 0 elsewhere by contract)
     near = torch.as_tensor(_near_node_voxels(bp.grad_bricks.cpu().numpy(), bp.B, bp.Dt, RATE), device="cuda")
     for _ in range(2):
         bp.out_rgb.zero_()
         bp.grad_feat.masked_fill_(near[..., None], 7.0)
+        bp.grad_tsdf.masked_fill_(near, 7.0)
         g.replay()
         torch.cuda.synchronize()
-        assert torch.equal(bp.out_rgb, ref[0]) and torch.equal(bp.out_depth, ref[1])
-        assert torch.equal(bp.tsdf, ref[2])
-        for got, r in ((bp.grad_feat, ref[3]), (bp.grad_tsdf, ref[4])):
-            assert (got - r).abs().max().item() <= 1e-5 * max(r.abs().max().item(), 1e-12)
+        for got, r in zip((bp.out_rgb, bp.out_depth, bp.tsdf, bp.grad_feat, bp.grad_tsdf, bp.out_loss), ref):
+            assert torch.equal(got, r)
+
+
+def test_det_gradients_match_atomics_and_launch_shapes(work):
+    """The deterministic reduction against the atomic scatter: outputs and
+    loss bit for bit (the same per-ray pass), feature- and TSDF-grid
+    gradients within 1e-5 of the largest; and the same gradients bit for bit
+    under every training-pass grid size."""
+    from sailor_gb300 import autotune
+    bp = _pipeline(work)
+    bp.train_tsdf = True
+    bp.deterministic = False
+    bp.train_step()
+    torch.cuda.synchronize()
+    ref = [t.clone() for t in (bp.out_rgb, bp.out_depth, bp.out_ws, bp.out_alpha, bp.out_loss, bp.grad_feat,
+                               bp.grad_tsdf)]
+    det = _pipeline(work)
+    det.train_tsdf = True
+    saved = autotune.current()
+    outs = []
+    try:
+        for warps in (64, 7, 16):
+            autotune.set_knob("render_warps", warps)
+            det.zero_grads()
+            det.train_step()
+            torch.cuda.synchronize()
+            outs.append([t.clone() for t in (det.out_rgb, det.out_depth, det.out_ws, det.out_alpha, det.out_loss,
+                                             det.grad_feat, det.grad_tsdf)])
+    finally:
+        for k, v in saved.items():
+            autotune.set_knob(k, v)
+    for a, b in zip(outs[0][:5], ref[:5]):
+        assert torch.equal(a, b)
+    for a, b in zip(outs[0][5:], ref[5:]):
+        m = b.abs().max().item()
+        assert m > 0 and (a - b).abs().max().item() <= 1e-5 * m
+    for o in outs[1:]:
+        for a, b in zip(o, outs[0]):
+            assert torch.equal(a, b)
+
+
+def test_record_capacity_reported(work):
+    """Fewer record slots than the step's samples: the status carries
+    SG_FLAG_RECORD_CAPACITY, nothing is written past the workspace, and the
+    outputs are still the full step's."""
+    from sailor_gb300 import _native as N
+    full = _pipeline(work)
+    full.train_step()
+    torch.cuda.synchronize()
+    assert not (full.status[0].item() & N.SG_FLAG_RECORD_CAPACITY)
+    from sailor_gb300.batch import BatchPipeline
+    view_hw = [[d.shape for d in fr["depth"]] for fr in work["frames"]]
+    targets = [(t["frame"], t["ori"].shape[0], t["S"]) for t in work["targets"]]
+    bp = BatchPipeline(view_hw, targets, D=D, rate=RATE, C=CF, W_hits=96, record_capacity=1000)
+    bp.load_views(work["frames"], work["vol_bbox"], work["voxel_size"], work["trunc_weight"])
+    bp.load_rays([(t["ori"], t["dir"]) for t in work["targets"]])
+    bp.set_fields(feat=full.feat, head=full.head, target_rgb=full.target_rgb)
+    bp.render_args(float(work["voxel_size"][0]) * work["trunc_weight"], sdf_s=0.01, t_thres=1e-4)
+    bp.train_step()
+    torch.cuda.synchronize()
+    assert bp.status[0].item() & N.SG_FLAG_RECORD_CAPACITY
+    assert torch.equal(bp.out_rgb, full.out_rgb)
+
+
+@pytest.mark.parametrize("n,cap,bits", [(1, 16, 8), (5000, 8192, 12), (300000, 300000, 31), (70000, 100000, 20)])
+def test_sort_pairs_stable(n, cap, bits):
+    """sg_sort_pairs (the reduction's radix sort) against numpy's stable
+    argsort: keys with many repeats, a live count below the capacity held
+    in device memory, 1 to 4 passes."""
+    from sailor_gb300 import _native as N
+    rng = np.random.default_rng(n)
+    keys = rng.integers(0, min(2 ** bits, 3 * n + 7), cap, dtype=np.int64).astype(np.uint32)
+    kt = torch.as_tensor(keys.view(np.int32), device="cuda")
+    cnt = torch.tensor([n], dtype=torch.int32, device="cuda")
+    ko, vo, kt2, vt2 = (torch.full((cap,), -1, dtype=torch.int32, device="cuda") for _ in range(4))
+    nb = int(N.lib.sg_sort_pairs_scratch_bytes(cap))
+    scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    N.check(N.lib.sg_sort_pairs(N.ptr(kt), N.ptr(cnt), cap, bits, N.ptr(ko), N.ptr(vo), N.ptr(kt2), N.ptr(vt2),
+                                N.ptr(scratch), nb, N.stream()), "sort_pairs")
+    torch.cuda.synchronize()
+    order = np.argsort(keys[:n], kind="stable")
+    assert np.array_equal(vo.cpu().numpy()[:n].astype(np.int64), order)
+    assert np.array_equal(ko.cpu().numpy()[:n].view(np.uint32), keys[:n][order])
 
 
 def test_fused_train_step_matches_unfused(work):
@@ -355,3 +441,28 @@ def test_train_step_clears_previous_gradients(work, train_tsdf):
     if train_tsdf:
         mt = fresh.grad_tsdf.abs().max().item()
         assert mt > 0 and (bp.grad_tsdf - fresh.grad_tsdf).abs().max().item() <= 1e-5 * mt
+
+
+@pytest.mark.parametrize("seed", [0, 77])
+def test_parity_batch_against_oracle(work, seed):
+    """bench.parity_batch on the small workload: fusion of every frame bit for
+    bit; traversal rows equal the oracle's on every unflagged ray
+    (t-intervals within 1e-5); samples equal the oracle's sampling of the
+    same rows bit for bit (constant and hashed jitter); the training pass's
+    colour, depth, weight sum and alpha within 1e-5 of the float64 oracle
+    render; the feature-grid gradient within a relative 1e-4 of float64
+    central differences (h = 1e-4) of the oracle's loss."""
+    import bench
+    bp = _pipeline(work, seed=seed)
+    bp.train_step()
+    torch.cuda.synchronize()
+    bcfg = dict(frames=bp.B, D=D, rate=RATE, C=CF, sdf_s=0.01)
+    par = bench.parity_batch(bp, work, bcfg, seed, n_hit=64, n_all=16, n_fd_entries=24)
+    print(par)
+    assert par["fusion_frames_bit_exact"]
+    tr = par["traversal"]
+    assert tr["unflagged_row_mismatches"] == 0 and tr["rays_flagged"] < 0.2 * par["rays"]
+    assert tr["t_max_abs_err"] <= 1e-5
+    assert par["sample_mismatches"] == 0 and par["composite_rays_flagged"] < 0.01 * par["rays"]
+    assert par["composite_within_atol"], par["composite_max_abs_err"]
+    assert par["grad_fd"]["max_abs_fd"] > 0 and par["grad_fd"]["rel_err"] <= 1e-4, par["grad_fd"]
