@@ -152,23 +152,35 @@ __global__ void __launch_bounds__(256) det_class_kernel(DetReduceParams q, int c
     const int j0 = __ldg(q.ustart + u), j1 = __ldg(q.ustart + u + 1);
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     float acct = 0.0f;
-    for (int j = j0; j < j1; j++) {
-      const uint32_t slot = __ldg(q.sorted_slot + j);
-      const float4 fw = __ldg(q.rec_f + slot);
-      const int2 kt = __ldg(q.rec_kt + slot);
-      const float f[3] = {fw.x, fw.y, fw.z};
-      const float wc = corner_weight(f, cr);
-      const float a = wc * fw.w;
-      if (C == 16) {
-        const float4 g = __ldg(reinterpret_cast<const float4 *>(q.ray_g + (size_t)kt.x * C + ch));
-        acc.x = __fmaf_rn(a, g.x, acc.x);
-        acc.y = __fmaf_rn(a, g.y, acc.y);
-        acc.z = __fmaf_rn(a, g.z, acc.z);
-        acc.w = __fmaf_rn(a, g.w, acc.w);
-      } else if (fown) {
-        acc.x = __fmaf_rn(a, __ldg(q.ray_g + (size_t)kt.x * C + ch), acc.x);
+    for (int c0 = j0; c0 < j1; c0 += 32) {
+      // lane jj loads the record of the run's sample c0 + jj (all loads in
+      // flight at once); then the samples are summed in run order
+      float4 fw = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      int2 kt = make_int2(0, 0);
+      if (c0 + lane < j1) {
+        const uint32_t slot = __ldg(q.sorted_slot + c0 + lane);
+        fw = __ldg(q.rec_f + slot);
+        kt = __ldg(q.rec_kt + slot);
       }
-      if (q.grad_tsdf && lane < 8) acct = __fmaf_rn(corner_weight(f, lane), __int_as_float(kt.y), acct);
+      const int m = min(32, j1 - c0);
+#pragma unroll 4
+      for (int jj = 0; jj < m; jj++) {
+        const float f[3] = {__shfl_sync(SG_FULL, fw.x, jj), __shfl_sync(SG_FULL, fw.y, jj),
+                            __shfl_sync(SG_FULL, fw.z, jj)};
+        const float a = corner_weight(f, cr) * __shfl_sync(SG_FULL, fw.w, jj);
+        const int k = __shfl_sync(SG_FULL, kt.x, jj);
+        const float gt = __int_as_float(__shfl_sync(SG_FULL, kt.y, jj));
+        if (C == 16) {
+          const float4 g = __ldg(reinterpret_cast<const float4 *>(q.ray_g + (size_t)k * C + ch));
+          acc.x = __fmaf_rn(a, g.x, acc.x);
+          acc.y = __fmaf_rn(a, g.y, acc.y);
+          acc.z = __fmaf_rn(a, g.z, acc.z);
+          acc.w = __fmaf_rn(a, g.w, acc.w);
+        } else if (fown) {
+          acc.x = __fmaf_rn(a, __ldg(q.ray_g + (size_t)k * C + ch), acc.x);
+        }
+        if (q.grad_tsdf && lane < 8) acct = __fmaf_rn(corner_weight(f, lane), gt, acct);
+      }
     }
     int b, i0[3];
     record_cell(q.keys, __ldg(q.ukey + u), b, i0);

@@ -140,10 +140,21 @@ void launch_excl_scan(const int *in, long n, int *out, int *scratch, int *total,
 // ---------------------------------------------------------------------------
 // radix sort
 // ---------------------------------------------------------------------------
+// meta[0]: live tiles ceil(n / kSortTile), meta[1]: live table entries
+// (kDigits x live tiles).  The digit-major tables hold the live tiles only,
+// so their scans cover the live items, not the capacity.
+__global__ void radix_meta_kernel(const int *__restrict__ n_dev, int *__restrict__ meta) {
+  const int ntl = (int)ceil_div(*n_dev, kSortTile);
+  meta[0] = ntl;
+  meta[1] = ntl * kDigits;
+}
+
 __global__ void __launch_bounds__(256) radix_hist_kernel(const uint32_t *__restrict__ keys,
-                                                         const int *__restrict__ n_dev, int shift, int ntiles,
-                                                         int *__restrict__ hist) {
+                                                         const int *__restrict__ n_dev, int shift,
+                                                         const int *__restrict__ meta, int *__restrict__ hist) {
   __shared__ int s_h[kDigits];
+  const int ntiles = meta[0];
+  if ((int)blockIdx.x >= ntiles) return;
   s_h[threadIdx.x] = 0;
   __syncthreads();
   const long n = *n_dev;
@@ -154,18 +165,21 @@ __global__ void __launch_bounds__(256) radix_hist_kernel(const uint32_t *__restr
     if (i < n) atomicAdd(&s_h[(__ldg(keys + i) >> shift) & 0xff], 1);
   }
   __syncthreads();
-  hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = s_h[threadIdx.x];
+  hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = s_h[threadIdx.x];  // digit-major, live tiles
 }
 
 // vals == nullptr: the values are the item indices.
 __global__ void __launch_bounds__(256) radix_scatter_kernel(const uint32_t *__restrict__ keys,
                                                             const uint32_t *__restrict__ vals,
-                                                            const int *__restrict__ n_dev, int shift, int ntiles,
+                                                            const int *__restrict__ n_dev, int shift,
+                                                            const int *__restrict__ meta,
                                                             const int *__restrict__ offs,
                                                             uint32_t *__restrict__ keys_out,
                                                             uint32_t *__restrict__ vals_out) {
   constexpr int R = kSortTile / 256;  // rounds per warp
   __shared__ int s_cnt[8][kDigits];   // per-warp running count per digit
+  const int ntiles = meta[0];
+  if ((int)blockIdx.x >= ntiles) return;
   const int lane = lane_id(), w = threadIdx.x >> 5;
   for (int d = lane; d < kDigits; d += 32) s_cnt[w][d] = 0;
   __syncwarp();
@@ -219,7 +233,7 @@ __global__ void __launch_bounds__(256) radix_scatter_kernel(const uint32_t *__re
 size_t radix_scratch_bytes(long cap) {
   const long ntiles = ceil_div(cap, kSortTile) > 0 ? ceil_div(cap, kSortTile) : 1;
   const long table = ntiles * kDigits;
-  return (size_t)(2 * table + (long)scan_scratch_ints(table) + 4) * sizeof(int);
+  return (size_t)(2 * table + (long)scan_scratch_ints(table) + 8) * sizeof(int);
 }
 
 int launch_radix_sort(const uint32_t *keys_in, const int *n_dev, long cap, int key_bits, uint32_t *keys_a,
@@ -230,15 +244,17 @@ int launch_radix_sort(const uint32_t *keys_in, const int *n_dev, long cap, int k
   int *offs = hist + table;
   int *ss = offs + table;
   int *tot = ss + scan_scratch_ints(table);
+  int *meta = tot + 2;
   const int passes = key_bits <= 0 ? 1 : (key_bits + 7) / 8;
   const uint32_t *ki = keys_in;
   const uint32_t *vi = nullptr;
+  radix_meta_kernel<<<1, 1, 0, stream>>>(n_dev, meta);
   for (int p = 0; p < passes; p++) {
     uint32_t *ko = (p & 1) ? keys_b : keys_a;
     uint32_t *vo = (p & 1) ? vals_b : vals_a;
-    radix_hist_kernel<<<ntiles, 256, 0, stream>>>(ki, n_dev, 8 * p, ntiles, hist);
-    launch_excl_scan(hist, table, offs, ss, tot, stream);
-    radix_scatter_kernel<<<ntiles, 256, 0, stream>>>(ki, vi, n_dev, 8 * p, ntiles, offs, ko, vo);
+    radix_hist_kernel<<<ntiles, 256, 0, stream>>>(ki, n_dev, 8 * p, meta, hist);
+    launch_excl_scan_dev(hist, table, meta + 1, offs, ss, tot, stream);
+    radix_scatter_kernel<<<ntiles, 256, 0, stream>>>(ki, vi, n_dev, 8 * p, meta, offs, ko, vo);
     ki = ko;
     vi = vo;
   }

@@ -268,7 +268,8 @@ def test_train_step_graph_replay(work, train_tsdf):
     for _ in range(2):
         bp.out_rgb.zero_()
         bp.grad_feat.masked_fill_(near[..., None], 7.0)
-        bp.grad_tsdf.masked_fill_(near, 7.0)
+        if train_tsdf:
+            bp.grad_tsdf.masked_fill_(near, 7.0)
         g.replay()
         torch.cuda.synchronize()
         for got, r in zip((bp.out_rgb, bp.out_depth, bp.tsdf, bp.grad_feat, bp.grad_tsdf, bp.out_loss), ref):
