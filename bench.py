@@ -220,20 +220,23 @@ def run_reference(args):
     if rank != 0:
         return
     if args.workload == "batch":
-        from oracle import oracle as orc
         bcfg = dict(BATCH_SMALL if args.small else BATCH)
         w = batch_workload(bcfg)
-        rng = np.random.default_rng(bcfg["seed"] + 5)
-        D, C = bcfg["D"], bcfg["C"]
-        feat0 = rng.standard_normal((1, D, D, D, C), dtype=np.float32) * np.float32(0.1)
-        head = rng.standard_normal((3, C), dtype=np.float32) * np.float32(0.5)
-        K, RT, dep, col = padded_views(w["frames"][0])
-        fz = orc.integrate(K, RT, col, dep, D, w["vol_bbox"][:1], w["voxel_size"][:1].reshape(1, 1),
-                           trunc_weight=w["trunc_weight"])
-        run = lambda: cpu_baseline_batch(w, bcfg, feat0, head, fz=fz)  # noqa: E731
         R = sum(t["ori"].shape[0] for t in w["targets"])
-        workload = ("batched training step (CPU port, bounded sample): %d frames, %d targets (%d rays)" %
-                    (bcfg["frames"], bcfg["targets"], R))
+        runs = cpu_baseline_isolated(w, bcfg, reps=args.warmup + args.steps)[args.warmup:]
+        cb = summarize_cpu_baseline(runs)
+        v = cb["value"]
+        ms = 1000.0 * float(np.median([r["sample_wall_s"] for r in runs]))
+        out = dict(metric=METRIC, value=v, unit=UNIT, impl="reference", n_gpus=args.gpus, steps=args.steps,
+                   warmup=args.warmup, ms_per_step=ms, higher_is_better=True, scaling="weak", vs_baseline=None,
+                   dtype="f32", data="synthetic",
+                   config=dict(workload=("batched training step (CPU port): %d frames, %d targets (%d rays); each "
+                                         "step a bounded sample scaled to the whole step (ms_per_step: the "
+                                         "sample's wall time)" % (bcfg["frames"], bcfg["targets"], R)),
+                               l2="inputs > L2"),
+                   cpu_baseline=cb, e2e=dict(value=v, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+        print(json.dumps(out), flush=True)
+        return
     else:
         cfg = dict(CFG)
         if args.small:
@@ -331,57 +334,114 @@ def batch_algorithmic_bytes(bcfg, w, n_hits, R, n_samples, n_clear_bricks=None, 
     )
 
 
-def cpu_baseline_batch(w, bcfg, feat, head, ray_sample=2048, fusion_slab=8, fz=None):
-    """The oracle (a C port of the reference kernels, OpenMP on all host
-    cores) on a bounded sample of the batched step, scaled to the whole step:
-    fusion of an x-slab of frame 0, coarse occupancy + tree of frame 0 (x
-    frames), and forward + backward of a ray subset of target 0."""
+def cpu_batch_setup(w, bcfg):
+    """Untimed set-up of the CPU baseline of the batched step: every frame
+    fused by the oracle (the tree and render stages need complete grids), one
+    seeded feature grid [1, D, D, D, C] ~ N(0, 0.1) shared by the frames (its
+    values do not change the work) and a colour head ~ N(0, 0.5)."""
     from oracle import oracle as orc
-    D, rate, B = bcfg["D"], bcfg["rate"], bcfg["frames"]
-    fr = w["frames"][0]
-    K, RT, dep, col = padded_views(fr)
-    bb, vs = w["vol_bbox"][:1], w["voxel_size"][:1].reshape(1, 1)
-    n_views_all = sum(len(f["K"]) for f in w["frames"])
+    D, C = bcfg["D"], bcfg["C"]
+    fz = []
+    for b, fr in enumerate(w["frames"]):
+        K, RT, dep, col = padded_views(fr)
+        fz.append(orc.integrate(K, RT, col, dep, D, w["vol_bbox"][b:b + 1], w["voxel_size"][b:b + 1].reshape(1, 1),
+                                trunc_weight=w["trunc_weight"]))
+    rng = np.random.default_rng(bcfg["seed"] + 5)
+    feat = rng.standard_normal((1, D, D, D, C), dtype=np.float32) * np.float32(0.1)
+    head = rng.standard_normal((3, C), dtype=np.float32) * np.float32(0.5)
+    return dict(fz=fz, feat=feat, head=head)
+
+
+def cpu_baseline_batch(w, bcfg, setup, n_rays=4096, fusion_slab=8):
+    """The oracle (a C port of the reference kernels, OpenMP on all host
+    cores) on a bounded sample of the batched training step, scaled to the
+    whole step: fusion of an x-slab of fusion_slab voxels of every frame
+    (x D / fusion_slab), coarse occupancy + tree of every frame, and for
+    every target a share of n_rays rays proportional to its rays x samples
+    (evenly spaced over its rays, at least 8): traversal, coarse sampling,
+    sort, TSDF and feature taps, colour head, compositing forward and
+    backward, grid scatter -- each target's time scaled by its rays over the
+    sampled ones.  Returns the rate, the stage times and the wall time of the
+    sample itself."""
+    from oracle import oracle as orc
+    D, rate = bcfg["D"], bcfg["rate"]
+    t_wall = time.perf_counter()
     t0 = time.perf_counter()
-    orc.integrate_slab(K, RT, col, dep, D, bb, vs, 0, fusion_slab, trunc_weight=w["trunc_weight"])
-    t_fuse = (time.perf_counter() - t0) * (D / fusion_slab) * (n_views_all / len(fr["K"]))
-    if fz is None:
-        fz = orc.integrate(K, RT, col, dep, D, bb, vs, trunc_weight=w["trunc_weight"])
+    for b, fr in enumerate(w["frames"]):
+        K, RT, dep, col = padded_views(fr)
+        orc.integrate_slab(K, RT, col, dep, D, w["vol_bbox"][b:b + 1], w["voxel_size"][b:b + 1].reshape(1, 1), 0,
+                           fusion_slab, trunc_weight=w["trunc_weight"])
+    t_fuse = (time.perf_counter() - t0) * (D / fusion_slab)
     t0 = time.perf_counter()
-    top, _ = orc.merge(fz["occ"], rate)
-    tree = orc.build_tree(top, fz["occ"])
-    t_tree = (time.perf_counter() - t0) * B
-    tg = w["targets"][0]
-    sel = np.linspace(0, tg["ori"].shape[0] - 1, ray_sample).astype(np.int64)
-    o, d = tg["ori"][sel][None], tg["dir"][sel][None]
-    S = tg["S"]
-    R = sum(t["ori"].shape[0] for t in w["targets"])
-    t0 = time.perf_counter()
-    hits = orc.voxel_traversal(tree, o, d, vs, bb, W=bcfg["W_hits"])
-    _, sz, _ = orc.sample_coarse(tree, hits, np.full((1, ray_sample, S), 0.5, np.float32), vs, S)
-    srt, _ = orc.sort(sz)
-    pts = (o[0][:, None, :] + d[0][:, None, :] * np.maximum(srt[0], 0)[..., None]).reshape(-1, 3)
-    t = orc.grid_gather(pts, fz["tsdf"][..., None], bb[:, :, 0], vs[:, 0])[:, 0]
-    sdf = t * float(vs[0, 0]) * w["trunc_weight"]
-    sigma = (1.0 / (1.0 + np.exp(sdf / bcfg["sdf_s"])) / bcfg["sdf_s"]).astype(np.float32)
-    fe = orc.grid_gather(pts, feat[:1], bb[:, :, 0], vs[:, 0])
-    rgb = (fe @ head.T.astype(np.float64)).astype(np.float32)
-    sig4 = sigma.reshape(1, ray_sample, S, 1)
-    rgb4 = rgb.reshape(1, ray_sample, S, 3)
-    fo = orc.composite_fwd(srt, None, sig4, rgb4, 1e-4, False)[:4]
-    g = [np.ones(x.shape, np.float32) for x in fo]
-    ident = np.broadcast_to(np.arange(S, dtype=np.int32), srt.shape)
-    gf, gs = orc.composite_bwd_ref(*g, *fo, srt, ident, sig4, rgb4, 1e-4, False)
-    gfe = (gf.reshape(-1, 3).astype(np.float64) @ head.astype(np.float64)).astype(np.float32)
-    orc.grid_scatter(pts, gfe, 1, D, bb[:, :, 0], vs[:, 0])
-    t_render = (time.perf_counter() - t0) * R / ray_sample
+    trees = []
+    for fz in setup["fz"]:
+        top, _ = orc.merge(fz["occ"], rate)
+        trees.append(orc.build_tree(top, fz["occ"]))
+    t_tree = time.perf_counter() - t0
+    tg_all = w["targets"]
+    R = sum(t["ori"].shape[0] for t in tg_all)
+    work = np.array([t["ori"].shape[0] * t["S"] for t in tg_all], np.float64)
+    feat, head = setup["feat"], setup["head"]
+    t_render = 0.0
+    n_sampled = 0
+    for t, tg in enumerate(tg_all):
+        b, S, n = tg["frame"], tg["S"], tg["ori"].shape[0]
+        ns = int(min(n, max(8, round(n_rays * work[t] / work.sum()))))
+        sel = np.linspace(0, n - 1, ns).astype(np.int64)
+        o, d = tg["ori"][sel][None], tg["dir"][sel][None]
+        bb, vs = w["vol_bbox"][b:b + 1], w["voxel_size"][b:b + 1].reshape(1, 1)
+        t0 = time.perf_counter()
+        hits = orc.voxel_traversal(trees[b], o, d, vs, bb, W=bcfg["W_hits"])
+        _, sz, _ = orc.sample_coarse(trees[b], hits, np.full((1, ns, S), 0.5, np.float32), vs, S)
+        srt, _ = orc.sort(sz)
+        pts = (o[0][:, None, :] + d[0][:, None, :] * np.maximum(srt[0], 0)[..., None]).reshape(-1, 3)
+        tv = orc.grid_gather(pts, setup["fz"][b]["tsdf"][..., None], bb[:, :, 0], vs[:, 0])[:, 0]
+        sdf = tv * float(vs[0, 0]) * w["trunc_weight"]
+        sigma = (1.0 / (1.0 + np.exp(sdf / bcfg["sdf_s"])) / bcfg["sdf_s"]).astype(np.float32)
+        fe = orc.grid_gather(pts, feat, bb[:, :, 0], vs[:, 0])
+        rgb = (fe @ head.T.astype(np.float64)).astype(np.float32)
+        sig4, rgb4 = sigma.reshape(1, ns, S, 1), rgb.reshape(1, ns, S, 3)
+        fo = orc.composite_fwd(srt, None, sig4, rgb4, 1e-4, False)[:4]
+        g = [np.ones(x.shape, np.float32) for x in fo]
+        ident = np.broadcast_to(np.arange(S, dtype=np.int32), srt.shape)
+        gf, _ = orc.composite_bwd_ref(*g, *fo, srt, ident, sig4, rgb4, 1e-4, False)
+        gfe = (gf.reshape(-1, 3).astype(np.float64) @ head.astype(np.float64)).astype(np.float32)
+        orc.grid_scatter(pts, gfe, 1, D, bb[:, :, 0], vs[:, 0])
+        t_render += (time.perf_counter() - t0) * n / ns
+        n_sampled += ns
     t_step = t_fuse + t_tree + t_render
     return dict(value=R / t_step, unit=UNIT, cores=orc.num_threads(), kind="port",
-                sample=(f"oracle (C port, OpenMP) on host cores: fusion of x-slab {fusion_slab}/{D} of frame 0 "
-                        f"scaled to all {n_views_all} views, coarse occupancy + tree of frame 0 x{B}, "
-                        f"traversal/sampling/sort/field taps/compositing forward and backward + grid scatter "
-                        f"of {ray_sample} rays of target 0 scaled to {R} rays"),
-                stage_s=dict(fusion=t_fuse, tree=t_tree, render=t_render))
+                sample=(f"oracle (C port, OpenMP) on host cores: fusion of x-slab {fusion_slab}/{D} of every frame "
+                        f"(x{D // fusion_slab}), coarse occupancy + tree of every frame, traversal / sampling / "
+                        f"sort / field taps / compositing forward and backward / grid scatter of {n_sampled} rays "
+                        f"from all {len(tg_all)} targets (shares by rays x samples) scaled to {R} rays"),
+                stage_s=dict(fusion=t_fuse, tree=t_tree, render=t_render),
+                sample_wall_s=time.perf_counter() - t_wall)
+
+
+def _cpu_baseline_job(w, bcfg, reps):
+    """Child-process body of cpu_baseline_isolated."""
+    setup = cpu_batch_setup(w, bcfg)
+    return [cpu_baseline_batch(w, bcfg, setup) for _ in range(reps)]
+
+
+def cpu_baseline_isolated(w, bcfg, reps=5):
+    """reps timed samples of cpu_baseline_batch in a fresh spawned process
+    (no GPU context or framework threads sharing its cores), after the
+    untimed set-up there.  Returns the list of per-sample results."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    with cf.ProcessPoolExecutor(max_workers=1, mp_context=mp.get_context("spawn")) as ex:
+        return ex.submit(_cpu_baseline_job, w, bcfg, reps).result()
+
+
+def summarize_cpu_baseline(runs):
+    """Median of the samples' rates (the bench line's cpu_baseline)."""
+    v = float(np.median([r["value"] for r in runs]))
+    r0 = runs[0]
+    return dict(value=v, unit=r0["unit"], cores=r0["cores"], kind=r0["kind"],
+                sample=r0["sample"] + f"; median of {len(runs)} samples in a separate process",
+                samples=[r["value"] for r in runs])
 
 
 # ---------------------------------------------------------------------------
@@ -630,6 +690,53 @@ def parity_batch(bp, w, bcfg, seed, frames=None, n_hit=192, n_all=64, n_fd_entri
                 seconds=time.perf_counter() - t_start)
 
 
+def frame_tree(bp, b):
+    """SgTree view of frame b of a BatchPipeline's tree (B = 1): the frame's
+    brick map, masks, voxel size and box; node ids stay the pipeline's."""
+    import ctypes as C
+
+    from sailor_gb300 import _native as N
+    t, Dt, mw = bp.tree, bp.Dt, N.mask_words(bp.rate)
+    return N.SgTree(1, t.Dt, t.Db, t.rate, t.base_top, t.base_bot, t.cap_top, t.cap_bot,
+                    bp.brick_node.data_ptr() + 4 * b * Dt ** 3, bp.brick_mask.data_ptr() + 4 * b * Dt ** 3 * mw,
+                    t.top_key, t.top_child_base, t.bot_key, t.bot_parent, t.counts,
+                    bp.voxel_size.data_ptr() + 4 * b, C.c_void_p(bp.vol_bbox.data_ptr() + 24 * b))
+
+
+def sample_sort_ms(bp, steps):
+    """Milliseconds per pass of sg_sample_sorted (coarse sampling + per-ray
+    sort, S of each target, jitter 0.5) over every target's hit rows."""
+    import ctypes as C
+
+    import torch
+
+    from sailor_gb300 import _native as N
+    z = torch.empty((bp.R, bp.S), device=bp.dev)
+    idx = torch.empty((bp.R, bp.S), dtype=torch.int32, device=bp.dev)
+    trees = [frame_tree(bp, b) for b in range(bp.B)]
+    W = bp.W
+    vp = lambda t, a, size: C.c_void_p(t.data_ptr() + size * a)  # noqa: E731
+
+    def one():
+        for ti, (f, n, S) in enumerate(bp.targets):
+            a, e = bp.ray_slices[ti]
+            N.check(N.lib.sg_sample_sorted(C.byref(trees[f]), vp(bp.hit_idx, a, 4 * W), vp(bp.hit_t0, a, 4 * W),
+                                           vp(bp.hit_t1, a, 4 * W), vp(bp.hit_count, a, 4), e - a, W, None, 0.5,
+                                           vp(bp.valid_len, a, 4), S, 2, 0, vp(z, a, 4 * bp.S), vp(idx, a, 4 * bp.S),
+                                           N.stream()), "sample_sorted")
+
+    for _ in range(3):
+        one()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        one()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
 def plain_per_frame_forward(VE, fields, w, bcfg, dev, feat, head_t, vbb, vvs, W_hits=256):
     """The reference's per-frame call order through the drop-in API, forward
     only: per frame integrate -> build_multi_res_volumes -> octree, then per
@@ -706,7 +813,8 @@ def run_batch(args):
     if not args.no_autotune:
         from sailor_gb300 import autotune
         autotune.set_knob("fuse_tiled", 1)
-        tuned = autotune.tune({"isect_block": bp.intersect, "render_warps": bp.train_step}, verbose=True)
+        tuned = autotune.tune({"isect_warp": bp.intersect, "isect_block": bp.intersect,
+                               "render_warps": bp.train_step}, verbose=True)
         tuned.update(fuse_tiled=1)
     for _ in range(max(args.warmup - 1, 0)):
         bp.train_step()
@@ -749,6 +857,10 @@ def run_batch(args):
     bp.events = None
     stages = {k: v / args.steps for k, v in stage_sum.items()}
     peak_mem = torch.cuda.max_memory_allocated(dev)
+
+    # standalone sampling + per-ray sort (sg_sample_sorted) of every target's
+    # hit rows, outside the graph: the sampler's own roofline
+    samp_ms = sample_sort_ms(bp, args.steps)
 
     # plain per-frame forward-only launch sequence on the same inputs
     vbb = torch.as_tensor(w["vol_bbox"]).to(dev)
@@ -819,6 +931,10 @@ def run_batch(args):
         ab = batch_algorithmic_bytes(bcfg, w, n_hits, R, S_all, near_node_bricks(bp), n_touched)
         rl = {k: ab[k] / (stages[k] / 1000.0) / 1e9 for k in ab if stages.get(k)}
         dom = max(rl, key=lambda k: stages[k])
+        # the standalone sampler (outside the step): hit rows, count and valid
+        # length in, sorted depth and node id out per sample slot
+        ab["sample_sort"] = 12 * n_hits + 8 * R + 8 * S_all
+        rl["sample_sort"] = ab["sample_sort"] / (samp_ms / 1000.0) / 1e9
         traffic = None
         tpath = os.path.join(ROOT, "profiles", "traffic.json")
         if os.path.exists(tpath) and not args.small:  # figures scaled to the full batch
@@ -834,7 +950,7 @@ def run_batch(args):
                                   (bcfg["frames"], bcfg["targets"], R)) if not args.small else "batch small",
                         frames_per_rank=bcfg["frames"], rays_per_step=R, l2="per-step working set > 10 GB >> L2",
                         parallelism=f"replicas x{world}", launch_shapes=tuned),
-            stages_ms=stages,
+            stages_ms=stages, sample_sort_ms=samp_ms,
             render_rays_s=R / (render_ms / 1000.0),
             plain_per_frame_fwd=dict(value=plain_value, unit=UNIT, ms_per_step=plain_ms,
                                      ratio_batched_fwd_bwd=value / plain_value),
@@ -852,16 +968,8 @@ def run_batch(args):
             clocks=clk.summary(),
         )
         if not args.no_cpu_baseline:
-            # one warm-up run (thread pool, first touch), then the timed one, as
-            # the reference arm times it
-            from oracle import oracle as orc
-            feat0 = bp.feat[:1].cpu().numpy()
-            K0, RT0, dep0, col0 = padded_views(w["frames"][0])
-            fz0 = orc.integrate(K0, RT0, col0, dep0, bcfg["D"], w["vol_bbox"][:1],
-                                w["voxel_size"][:1].reshape(1, 1), trunc_weight=w["trunc_weight"])  # untimed set-up
-            cpu_baseline_batch(w, bcfg, feat0, head, fz=fz0)
-            cb = cpu_baseline_batch(w, bcfg, feat0, head, fz=fz0)
-            out["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+            # the same samples as the reference arm's, in a process of their own
+            out["cpu_baseline"] = summarize_cpu_baseline(cpu_baseline_isolated(w, bcfg, reps=5))
         if not args.no_parity:
             out["parity"] = parity_batch(bp, w, bcfg, bcfg["seed"] + 1)
         print(json.dumps(out), flush=True)

@@ -84,10 +84,14 @@ enum {
   SG_TUNE_FUSE_VPT = 0,      /* voxels per thread in sg_fuse_tsdf: 1, 2, 4 */
   SG_TUNE_FUSE_BLOCK = 1,    /* threads per CTA in sg_fuse_tsdf: 32..256   */
   SG_TUNE_ISECT_BLOCK = 2,   /* threads per CTA in sg_intersect: 32..512   */
-  SG_TUNE_RENDER_WARPS = 3,  /* CTAs per SM (x152) in warp-per-ray kernels */
+  SG_TUNE_RENDER_WARPS = 3,  /* CTAs per SM (x SM count) of warp-per-ray   */
+                             /* kernels                                     */
   SG_TUNE_FUSE_TILED = 4,    /* sg_fuse_tsdf voxel order: 1 = 16^3 tiles,   */
                              /* 0 = linear runs (FUSE_VPT, FUSE_BLOCK)      */
-  SG_TUNE_COUNT = 5
+  SG_TUNE_ISECT_WARP = 5,    /* intersection child tests: 0 = each ray's    */
+                             /* thread, children it can reach (default);    */
+                             /* 1 = a warp per hit brick, every child       */
+  SG_TUNE_COUNT = 6
 };
 int sg_tune_set(int knob, int value);
 int sg_tune_get(int knob);

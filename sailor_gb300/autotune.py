@@ -17,7 +17,7 @@ import torch
 
 from . import _native as N
 
-KNOBS = {"fuse_vpt": 0, "fuse_block": 1, "isect_block": 2, "render_warps": 3, "fuse_tiled": 4}
+KNOBS = {"fuse_vpt": 0, "fuse_block": 1, "isect_block": 2, "render_warps": 3, "fuse_tiled": 4, "isect_warp": 5}
 
 CANDIDATES = {
     "fuse_vpt": (1, 2, 4),
@@ -25,6 +25,7 @@ CANDIDATES = {
     "isect_block": (64, 128, 256),
     "render_warps": (16, 32, 64),
     "fuse_tiled": (0, 1),  # 1: 16^3 voxel tiles; 0: linear runs shaped by fuse_vpt / fuse_block
+    "isect_warp": (0, 1),  # 1: a warp tests each hit brick's children; 0: each ray's thread alone
 }
 
 CACHE = os.path.join(os.path.expanduser("~"), ".cache", "sailor_gb300", "tune.json")
@@ -98,8 +99,8 @@ def tune_pipeline(pipe, build_fn, render_fn, reps=3, cache=True, verbose=False):
     if not (cache and key and _cached(key)):
         set_knob("fuse_tiled", 0)  # the linear shape knobs only act with tiling off
     return tune({"fuse_vpt": build_fn, "fuse_block": build_fn, "fuse_tiled": build_fn,
-                 "isect_block": render_fn, "render_warps": render_fn}, reps=reps, cache_key=key,
-                verbose=verbose)
+                 "isect_warp": render_fn, "isect_block": render_fn, "render_warps": render_fn}, reps=reps,
+                cache_key=key, verbose=verbose)
 
 
 def _cached(key, cache_path=CACHE):

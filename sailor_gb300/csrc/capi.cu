@@ -22,7 +22,7 @@ extern "C" int sg_version(void) { return 100; }
 namespace sg {
 // Process-wide: a value set by one thread is seen by launches of every
 // thread after the store (relaxed atomics: each knob is independent).
-static std::atomic<int> g_tune[SG_TUNE_COUNT] = {4, 128, 64, 64, 1};
+static std::atomic<int> g_tune[SG_TUNE_COUNT] = {4, 128, 64, 64, 1, 0};
 
 int tune(int knob) {
   return (knob >= 0 && knob < SG_TUNE_COUNT) ? g_tune[knob].load(std::memory_order_relaxed) : 0;
@@ -63,6 +63,7 @@ extern "C" int sg_tune_set(int knob, int value) {
       if (value < 1 || value > 64) return SG_ERR_INVALID_ARG;
       break;
     case SG_TUNE_FUSE_TILED:
+    case SG_TUNE_ISECT_WARP:
       if (value != 0 && value != 1) return SG_ERR_INVALID_ARG;
       break;
     default:

@@ -6,11 +6,16 @@
 //
 // One thread per ray walks the top grid with the reference's Amanatides-Woo
 // DDA (same float operations, so the same cells in the same order).  At a
-// kept brick the thread reads the brick's node index from the dense brick
-// map and iterates the set bits of the brick's fine-occupancy mask in
-// ascending order -- the reference's lexicographic children order -- slab-
-// testing each occupied child with geometry recomputed from its index (the
-// reference copies a ~1.1 KB node per test).  Hits are appended to the
+// kept brick the brick's node index comes from the dense brick map and the
+// set bits of the brick's fine-occupancy mask give its children in
+// ascending order -- the reference's lexicographic children order -- each
+// slab-tested with geometry recomputed from its index (the reference copies
+// a ~1.1 KB node per test).  The default variant (intersect_kernel) tests
+// them in the ray's own thread, visiting only the children the ray can
+// reach; the warp-cooperative variant (intersect_warp_kernel, tune knob
+// SG_TUNE_ISECT_WARP) tests every occupied child of a hit brick with the
+// whole warp, one brick at a time -- the same rows, but measured about 8x
+// slower at 8^3 bricks, where the reach test leaves ~1/5 of the children.  Hits are appended to the
 // ray's row; the reference's -1 padding of the row tail is written by a
 // second, warp-per-row kernel with coalesced 16-byte stores.
 //
@@ -113,6 +118,7 @@ __global__ void __launch_bounds__(512) intersect_kernel(IsectParams p) {
               const float tm_ = 1e-4f * (p1 - p0) + 1e-5f * fabsf(p1) + 1e-6f;
               const float tlo = p0 - tm_, thi = p1 + tm_;
               constexpr float kMargin = 0.02f;
+              int rword = 0, rbase = 0;  // set bits of mask words [0, rword)
               for (int a = 0; a < r; a++) {
                 float ta, tb;
                 if (du0 != 0.0f) {
@@ -143,8 +149,10 @@ __global__ void __launch_bounds__(512) intersect_kernel(IsectParams p) {
                              node_coord(gb, bmin[1], st[1] * r + y), node_coord(gb, bmin[2], st[2] * r + z),
                              gb.vs, c0, c1) &&
                         !(c0 < 0.0f || c1 < 0.0f)) {
-                      int rank = __popc(word & ((1u << (c & 31)) - 1u));
-                      for (int w = 0; w < (c >> 5); w++) rank += __popc(__ldg(mask + w));
+                      // children are visited in ascending c: the set bits
+                      // of the words below c's word are counted once each
+                      while (rword < (c >> 5)) rbase += __popc(__ldg(mask + rword++));
+                      const int rank = rbase + __popc(word & ((1u << (c & 31)) - 1u));
                       if (cnt < p.W) {
                         oi[cnt] = cb + rank;
                         o0[cnt] = c0;
@@ -208,6 +216,224 @@ __global__ void __launch_bounds__(512) intersect_kernel(IsectParams p) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Warp-cooperative variant: each lane walks its own ray's DDA (the same
+// float operations, hence the same cells), but the children of a hit brick
+// are tested by the whole warp: lane l takes children 32 i + l (i over the
+// brick's 32-bit mask words), so one warp instruction covers 32 children in
+// lexicographic order; a ballot of the hits and a popcount of the lanes
+// before give each hit its row position, and the mask bits before a child
+// its node rank.  Hit bricks of different lanes in the same DDA step are
+// served one after another in lane order, so every ray's row is in the
+// reference's order (per brick: children in lexicographic order, then the
+// brick).  The valid length is summed hit by hit in row order, as the
+// reference sums it.  The DDA state stays in registers (per-axis selects).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) intersect_warp_kernel(IsectParams p) {
+  const SgTree &t = p.t;
+  const long R = p.R;
+  const int lane = lane_id();
+  const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool in = r < R;
+  int cnt = 0;
+  bool over = false;
+  float vlen = 0.0f;
+  int b = 0;
+  float o[3] = {0.0f, 0.0f, 0.0f}, d[3] = {1.0f, 1.0f, 1.0f}, inv[3] = {1.0f, 1.0f, 1.0f};
+  float bmin[3] = {0.0f, 0.0f, 0.0f};
+  float vs = 1.0f;
+  int st0 = 0, st1 = 0, st2 = 0;
+  float tm0 = 0.0f, tm1 = 0.0f, tm2 = 0.0f, td0 = 0.0f, td1 = 0.0f, td2 = 0.0f;
+  int sp0 = 1, sp1 = 1, sp2 = 1;
+  bool active = false;
+  const long vt = (long)t.Dt * t.Dt * t.Dt;
+  if (in) {
+    const int sgm = p.nseg > 0 ? segment_of(p.seg_begin, p.nseg, r) : 0;
+    b = p.nseg > 0 ? __ldg(p.seg_frame + sgm) : (int)(r / p.N);
+    const float *bb = t.vol_bbox + 6 * b;
+    bmin[0] = bb[0];
+    bmin[1] = bb[2];
+    bmin[2] = bb[4];
+    const float xc = (bb[0] + bb[1]) / 2.0f, yc = (bb[2] + bb[3]) / 2.0f, zc = (bb[4] + bb[5]) / 2.0f;
+    vs = t.voxel_size[b];
+    const float vs_top = vs * (float)(t.Db / t.Dt);
+    const float bst[3] = {bb[0] - vs / 2.0f, bb[2] - vs / 2.0f, bb[4] - vs / 2.0f};
+    segment_ray(p.ori, p.dir, p.cams, p.cam_w, p.seg_begin, sgm, r, o, d);
+#pragma unroll
+    for (int a = 0; a < 3; a++) inv[a] = __fdividef(1.0f, d[a]);
+    float T0, T1;
+    if (slab(o, inv, xc, yc, zc, vs_top * (float)t.Dt, T0, T1) && !(T0 < 0.0f || T1 < 0.0f)) {
+      float so[3];
+      int st[3];
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        float spos = __fmaf_rn(T0, d[a], o[a]);
+        so[a] = spos - bst[a];
+        int s = (int)(so[a] / vs_top);
+        s = s < 0 ? 0 : s;
+        st[a] = s < t.Dt ? s : t.Dt - 1;
+      }
+      float step[3], tm[3], td[3];
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        step[a] = (d[a] >= 0) ? 1.0f : -1.0f;
+        float nb = (step[a] > 0) ? ((float)st[a] + step[a]) * vs_top : (float)st[a] * vs_top;
+        tm[a] = (d[a] != 0) ? (nb - so[a]) / d[a] : 9999999.0f;
+        td[a] = (d[a] != 0) ? vs_top / d[a] * step[a] : 9999999.0f;
+      }
+      st0 = st[0], st1 = st[1], st2 = st[2];
+      tm0 = tm[0], tm1 = tm[1], tm2 = tm[2];
+      td0 = td[0], td1 = td[1], td2 = td[2];
+      sp0 = (int)step[0], sp1 = (int)step[1], sp2 = (int)step[2];
+      active = true;
+    }
+  }
+  int *oi = p.hit_idx + (size_t)(in ? r : 0) * p.W;
+  float *o0 = p.hit_t0 + (size_t)(in ? r : 0) * p.W, *o1 = p.hit_t1 + (size_t)(in ? r : 0) * p.W;
+  const int rate = t.rate, r3 = rate * rate * rate;
+  const int mw = sg_mask_words_dev(rate);
+  bool pre_empty = false, has_valid = false;
+  int nsucc = 0, nint = 0;
+  const int J = 4 * t.Dt;
+  for (int j = 0; j < J; j++) {
+    if (!__any_sync(SG_FULL, active)) break;
+    // this step's brick of every active lane: a node whose box the ray enters
+    bool pend = false;
+    int k = -1;
+    float p0 = 0.0f, p1 = 0.0f;
+    if (active) {
+      const long brick = (long)b * vt + ((long)st0 * t.Dt + st1) * t.Dt + st2;
+      k = t.brick_node[brick];
+      if (k >= 0) {
+        const LevelGeom gt = level_geom(vs, t.Db / t.Dt);
+        pend = slab(o, inv, node_coord(gt, bmin[0], st0), node_coord(gt, bmin[1], st1), node_coord(gt, bmin[2], st2),
+                    gt.vs, p0, p1) &&
+               !(p0 < 0.0f || p1 < 0.0f);
+      }
+    }
+    int rid = -1;
+    if (!p.is_training) {
+      // children of the pending bricks, one brick at a time in lane order
+      unsigned pm = __ballot_sync(SG_FULL, pend);
+      while (pm) {
+        const int L = __ffs(pm) - 1;
+        pm &= pm - 1;
+        const float oL[3] = {__shfl_sync(SG_FULL, o[0], L), __shfl_sync(SG_FULL, o[1], L),
+                             __shfl_sync(SG_FULL, o[2], L)};
+        const float iL[3] = {__shfl_sync(SG_FULL, inv[0], L), __shfl_sync(SG_FULL, inv[1], L),
+                             __shfl_sync(SG_FULL, inv[2], L)};
+        const float bL[3] = {__shfl_sync(SG_FULL, bmin[0], L), __shfl_sync(SG_FULL, bmin[1], L),
+                             __shfl_sync(SG_FULL, bmin[2], L)};
+        const int sx = __shfl_sync(SG_FULL, st0, L), sy = __shfl_sync(SG_FULL, st1, L),
+                  sz = __shfl_sync(SG_FULL, st2, L);
+        const int fL = __shfl_sync(SG_FULL, b, L);
+        const int kL = __shfl_sync(SG_FULL, k, L);
+        const long rL = __shfl_sync(SG_FULL, (long long)(in ? r : 0), L);
+        int base = __shfl_sync(SG_FULL, cnt, L);
+        float vl = __shfl_sync(SG_FULL, vlen, L);
+        const LevelGeom gb = level_geom(__shfl_sync(SG_FULL, vs, L), 1);
+        const long brickL = (long)fL * vt + ((long)sx * t.Dt + sy) * t.Dt + sz;
+        const uint32_t *mask = t.brick_mask + (size_t)brickL * mw;
+        const int cb = t.base_bot + t.top_child_base[kL];
+        int *oiL = p.hit_idx + (size_t)rL * p.W;
+        float *o0L = p.hit_t0 + (size_t)rL * p.W, *o1L = p.hit_t1 + (size_t)rL * p.W;
+        const int x0 = sx * rate, y0 = sy * rate, z0 = sz * rate;
+        int rank0 = 0;
+        bool ovL = false;
+        for (int i = 0; i < mw; i++) {
+          const uint32_t word = __ldg(mask + i);
+          const int c = 32 * i + lane;
+          bool hit = false;
+          float c0 = 0.0f, c1 = 0.0f;
+          if (c < r3 && ((word >> lane) & 1u)) {
+            const int a = c / (rate * rate), y = (c / rate) % rate, z = c % rate;
+            hit = slab(oL, iL, node_coord(gb, bL[0], x0 + a), node_coord(gb, bL[1], y0 + y),
+                       node_coord(gb, bL[2], z0 + z), gb.vs, c0, c1) &&
+                  !(c0 < 0.0f || c1 < 0.0f);
+          }
+          const unsigned hb = __ballot_sync(SG_FULL, hit);
+          if (hit) {
+            const int pos = base + __popc(hb & ((1u << lane) - 1u));
+            if (pos < p.W) {
+              oiL[pos] = cb + rank0 + __popc(word & ((1u << lane) - 1u));
+              o0L[pos] = c0;
+              o1L[pos] = c1;
+            }
+          }
+          // the ray's valid length, hit by hit in row order
+          const float len4 = (c1 - c0) * 4.0f;
+          for (unsigned m = hb; m; m &= m - 1) vl = vl + __shfl_sync(SG_FULL, len4, __ffs(m) - 1);
+          if (base + __popc(hb) > p.W) ovL = true;
+          base += __popc(hb);
+          rank0 += __popc(word);
+        }
+        if (lane == L) {
+          cnt = base;
+          vlen = vl;
+          over = over || ovL;
+        }
+      }
+    }
+    if (pend) {
+      if (cnt < p.W) {
+        oi[cnt] = t.base_top + k;
+        o0[cnt] = p0;
+        o1[cnt] = p1;
+      } else {
+        over = true;
+      }
+      vlen = vlen + (p1 - p0);
+      cnt++;
+      rid = cnt - 1;
+    }
+    if (active) {
+      if (p.th_early_stop > -1) {
+        if (rid == -1) {
+          if (pre_empty && has_valid) nsucc++;
+          pre_empty = true;
+        } else {
+          nsucc = 0;
+          pre_empty = false;
+          has_valid = true;
+        }
+        if ((nsucc + 1) >= p.th_early_stop) active = false;
+      }
+      if (p.opt_num > -1) {
+        if (rid + 1 > 0) nint++;
+        if (nint >= p.opt_num) active = false;
+      }
+    }
+    if (active) {
+      int ax;
+      if (tm0 < tm1) ax = (tm0 < tm2) ? 0 : 2;
+      else ax = (tm1 < tm2) ? 1 : 2;
+      if (ax == 0) {
+        st0 = (int)((float)st0 + (float)sp0);
+        tm0 += td0;
+      } else if (ax == 1) {
+        st1 = (int)((float)st1 + (float)sp1);
+        tm1 += td1;
+      } else {
+        st2 = (int)((float)st2 + (float)sp2);
+        tm2 += td2;
+      }
+      if (st0 < 0 || st0 >= t.Dt || st1 < 0 || st1 >= t.Dt || st2 < 0 || st2 >= t.Dt) active = false;
+    }
+  }
+  if (in) {
+    p.valid_len[r] = vlen;
+    if (p.hit_count) p.hit_count[r] = cnt;
+  }
+  int m = cnt;
+#pragma unroll
+  for (int o2 = 16; o2 > 0; o2 >>= 1) m = max(m, __shfl_xor_sync(SG_FULL, m, o2));
+  const bool anyover = __any_sync(SG_FULL, over);
+  if (lane == 0 && p.st) {
+    if (m > 0) atomicMax(&p.st->max_hits, m);
+    if (anyover) atomicOr(&p.st->flags, SG_FLAG_HIT_OVERFLOW);
+  }
+}
+
 // -1 padding of row tails [count, W): warp per row
 __global__ void pad_rows_kernel(long R, int W, const int *__restrict__ count, int *idx, float *t0,
                                 float *t1) {
@@ -260,8 +486,12 @@ extern "C" int sg_intersect(const SgTree *tree, const float *ori, const float *d
   long R = (long)tree->B * N;
   IsectParams p{*tree, ori, dir, N, W, th_early_stop, opt_num, is_training,
                 hit_idx, hit_t0, hit_t1, valid_len, hit_count, status, R, 0, nullptr, nullptr, nullptr, nullptr};
-  const int blk = tune(SG_TUNE_ISECT_BLOCK);
-  intersect_kernel<<<ceil_div(R, blk), blk, 0, stream>>>(p);
+  if (tune(SG_TUNE_ISECT_WARP)) {
+    intersect_warp_kernel<<<ceil_div(R, 256), 256, 0, stream>>>(p);
+  } else {
+    const int blk = tune(SG_TUNE_ISECT_BLOCK);
+    intersect_kernel<<<ceil_div(R, blk), blk, 0, stream>>>(p);
+  }
   if (padded) {
     int g = ceil_div(R * 32, 256);
     if (g > num_sms() * 64) g = num_sms() * 64;
@@ -282,8 +512,12 @@ extern "C" int sg_intersect_segments(const SgTree *tree, const SgRaySegments *se
   if (seg->total == 0) return SG_OK;
   IsectParams p{*tree, ori, dir, 1, W, -1, -1, 0, hit_idx, hit_t0, hit_t1, valid_len, hit_count, status,
                 (long)seg->total, seg->count, seg->ray_begin, seg->frame, seg->cameras, seg->widths};
-  const int blk = tune(SG_TUNE_ISECT_BLOCK);
-  intersect_kernel<<<ceil_div((long)seg->total, blk), blk, 0, stream>>>(p);
+  if (tune(SG_TUNE_ISECT_WARP)) {
+    intersect_warp_kernel<<<ceil_div((long)seg->total, 256), 256, 0, stream>>>(p);
+  } else {
+    const int blk = tune(SG_TUNE_ISECT_BLOCK);
+    intersect_kernel<<<ceil_div((long)seg->total, blk), blk, 0, stream>>>(p);
+  }
   SG_LAUNCH_CHECK();
   return SG_OK;
 }

@@ -65,8 +65,7 @@ struct RenderParams {
   // hit_slot[k] + q (below rec_cap)
   const int *hit_ray, *hit_slot, *k_begin, *k_end;
   uint32_t *rec_key;
-  float4 *rec_f;
-  int2 *rec_kt;
+  GradRecord *rec;
   float *ray_g;  // [k][C]: head^T (colour gradient of ray k)
   long rec_cap;
   RecordKeys keys;
@@ -319,8 +318,8 @@ __device__ __forceinline__ void emit_records(const RenderParams &p, long k, long
       key = record_key(p.keys, b, i0);
       if (key != p.keys.invalid) {
         const float gt = p.grad_tsdf ? gsig[e] * (ev.s01[e] * (1.0f - ev.s01[e]) * dsdt_k) : 0.0f;
-        p.rec_f[slot] = make_float4(f[0], f[1], f[2], w[e]);
-        p.rec_kt[slot] = make_int2((int)k, __float_as_int(gt));
+        p.rec[slot].fw = make_float4(f[0], f[1], f[2], w[e]);
+        p.rec[slot].kt = make_int4((int)k, __float_as_int(gt), 0, 0);
       }
     }
     p.rec_key[slot] = key;
@@ -845,8 +844,7 @@ extern "C" int sg_render_segments_train_det(const SgTree *tree, const SgRaySegme
   p.hit_ray = w.hit_ray;
   p.hit_slot = w.hit_slot;
   p.rec_key = w.rec_key;
-  p.rec_f = w.rec_f;
-  p.rec_kt = w.rec_kt;
+  p.rec = w.rec;
   p.ray_g = w.ray_g;
   p.rec_cap = (long)capacity;
   p.keys = make_record_keys(tree->B, args->Df);

@@ -6,12 +6,15 @@
 // the last bits of the gradient -- change from run to run.  Here the
 // training pass (render.cu, record mode) writes one record per used sample
 // instead: the sample's trilinear cell as a 32-bit key (frame and lower
-// corner, grouped by parity class), its cell fractions, its compositing
-// weight, its ray and its TSDF gradient; the ray's colour-head factor of the
-// feature gradient goes to a per-ray table.  Then
-//   1. the keys are sorted, stably, with the record slots as values
-//      (segsort.cu): records of one cell become one run, in slot order (ray
-//      order, then sorted sample order -- fixed by the ray layout);
+// corner, grouped by parity class), and a 32-byte record of its cell
+// fractions, its compositing weight, its ray and its TSDF gradient; the
+// ray's colour-head factor of the feature gradient goes to a per-ray table.
+// Then
+//   1. the records with a cell are compacted (slot order kept) and their
+//      keys sorted, stably, with the record slots as values (segsort.cu):
+//      records of one cell become one run, in slot order (ray order, then
+//      sorted sample order -- fixed by the ray layout); the records are
+//      gathered into that order;
 //   2. run heads are flagged and scanned into the list of distinct cells;
 //   3. for each of the 8 parity classes in turn, one warp per cell sums its
 //      run in order into the 8 corners x C channels it touches (lane = corner
@@ -90,31 +93,62 @@ __global__ void det_seg_kernel(SgRaySegments seg, long R, const int *__restrict_
   }
 }
 
-// head flags of the sorted keys' runs (cells), over the live records
-__global__ void det_heads_kernel(const uint32_t *__restrict__ key, const int *__restrict__ cnt, uint32_t invalid,
-                                 int *__restrict__ head) {
+// records with a cell (their keys are not the invalid key)
+__global__ void det_valid_flags_kernel(const uint32_t *__restrict__ key, const int *__restrict__ cnt,
+                                       uint32_t invalid, int *__restrict__ flag) {
+  const long n = cnt[kDetSlots];
+  for (long j = (long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x)
+    flag[j] = __ldg(key + j) != invalid ? 1 : 0;
+}
+
+// the records with a cell, compacted in slot order: key and slot
+__global__ void det_compact_kernel(const uint32_t *__restrict__ key, const int *__restrict__ cnt, uint32_t invalid,
+                                   const int *__restrict__ pos, uint32_t *__restrict__ ckey,
+                                   uint32_t *__restrict__ cslot) {
   const long n = cnt[kDetSlots];
   for (long j = (long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x) {
     const uint32_t k = __ldg(key + j);
-    head[j] = (k != invalid && (j == 0 || __ldg(key + j - 1) != k)) ? 1 : 0;
+    if (k != invalid) {
+      const int i = pos[j];
+      ckey[i] = k;
+      cslot[i] = (uint32_t)j;
+    }
   }
+}
+
+// head flags of the sorted keys' runs (cells)
+__global__ void det_heads_kernel(const uint32_t *__restrict__ key, const int *__restrict__ cnt,
+                                 int *__restrict__ head) {
+  const long n = cnt[kDetValid];
+  for (long j = (long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x)
+    head[j] = (j == 0 || __ldg(key + j - 1) != __ldg(key + j)) ? 1 : 0;
 }
 
 // distinct cells: key and first sorted position; the end of the last run
 __global__ void det_unique_kernel(const uint32_t *__restrict__ key, const int *__restrict__ head_scan,
-                                  const int *__restrict__ cnt, uint32_t invalid, uint32_t *__restrict__ ukey,
+                                  const int *__restrict__ cnt, uint32_t *__restrict__ ukey,
                                   int *__restrict__ ustart) {
-  const long n = cnt[kDetSlots];
+  const long n = cnt[kDetValid];
   const int nu = cnt[kDetCells];
   for (long j = (long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x) {
     const uint32_t k = __ldg(key + j);
-    if (k == invalid) continue;
     if (j == 0 || __ldg(key + j - 1) != k) {
       const int u = head_scan[j];
       ukey[u] = k;
       ustart[u] = (int)j;
     }
-    if (j + 1 == n || __ldg(key + j + 1) == invalid) ustart[nu] = (int)(j + 1);
+    if (j + 1 == n) ustart[nu] = (int)n;
+  }
+}
+
+// the records in sorted key order (one gathered 32-byte sector per record)
+__global__ void det_gather_kernel(const uint32_t *__restrict__ sorted_slot, const int *__restrict__ cnt,
+                                  const GradRecord *__restrict__ rec, GradRecord *__restrict__ pay) {
+  const long n = cnt[kDetValid];
+  for (long j = (long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x) {
+    const uint32_t slot = __ldg(sorted_slot + j);
+    pay[j].fw = __ldg(&rec[slot].fw);
+    pay[j].kt = __ldg(&rec[slot].kt);
   }
 }
 
@@ -150,17 +184,32 @@ __global__ void __launch_bounds__(256) det_class_kernel(DetReduceParams q, int c
   for (long u = lo + (((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5); u < hi;
        u += ((long)gridDim.x * blockDim.x) >> 5) {
     const int j0 = __ldg(q.ustart + u), j1 = __ldg(q.ustart + u + 1);
+    // the cell's corner values are read before its run is summed, so the
+    // read of the grid overlaps the run
+    int b, i0[3];
+    record_cell(q.keys, __ldg(q.ukey + u), b, i0);
+    const int vx = i0[0] + ((cr >> 2) & 1), vy = i0[1] + ((cr >> 1) & 1), vz = i0[2] + (cr & 1);
+    const bool fin = fown && vx >= 0 && vy >= 0 && vz >= 0 && vx < D && vy < D && vz < D;
+    float *gp = fin ? q.grad_feat + ((((size_t)b * D + vx) * D + vy) * D + vz) * C + ch : nullptr;
+    float4 old = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (fin) {
+      if (C == 16) old = *reinterpret_cast<const float4 *>(gp);
+      else old.x = *gp;
+    }
+    const int tx = i0[0] + ((lane >> 2) & 1), ty = i0[1] + ((lane >> 1) & 1), tz = i0[2] + (lane & 1);
+    const bool tin = q.grad_tsdf && lane < 8 && tx >= 0 && ty >= 0 && tz >= 0 && tx < D && ty < D && tz < D;
+    float *tp = tin ? q.grad_tsdf + (((size_t)b * D + tx) * D + ty) * D + tz : nullptr;
+    const float told = tin ? *tp : 0.0f;
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     float acct = 0.0f;
     for (int c0 = j0; c0 < j1; c0 += 32) {
-      // lane jj loads the record of the run's sample c0 + jj (all loads in
-      // flight at once); then the samples are summed in run order
+      // lane jj loads the run's record c0 + jj (the records are in sorted
+      // order: one coalesced load); then the samples are summed in run order
       float4 fw = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      int2 kt = make_int2(0, 0);
+      int4 kt = make_int4(0, 0, 0, 0);
       if (c0 + lane < j1) {
-        const uint32_t slot = __ldg(q.sorted_slot + c0 + lane);
-        fw = __ldg(q.rec_f + slot);
-        kt = __ldg(q.rec_kt + slot);
+        fw = __ldg(&q.pay[c0 + lane].fw);
+        kt = __ldg(&q.pay[c0 + lane].kt);
       }
       const int m = min(32, j1 - c0);
 #pragma unroll 4
@@ -182,27 +231,13 @@ __global__ void __launch_bounds__(256) det_class_kernel(DetReduceParams q, int c
         if (q.grad_tsdf && lane < 8) acct = __fmaf_rn(corner_weight(f, lane), gt, acct);
       }
     }
-    int b, i0[3];
-    record_cell(q.keys, __ldg(q.ukey + u), b, i0);
-    const int vx = i0[0] + ((cr >> 2) & 1), vy = i0[1] + ((cr >> 1) & 1), vz = i0[2] + (cr & 1);
-    if (fown && vx >= 0 && vy >= 0 && vz >= 0 && vx < D && vy < D && vz < D) {
-      float *g = q.grad_feat + ((((size_t)b * D + vx) * D + vy) * D + vz) * C + ch;
-      if (C == 16) {
-        float4 v = *reinterpret_cast<float4 *>(g);
-        v.x += acc.x;
-        v.y += acc.y;
-        v.z += acc.z;
-        v.w += acc.w;
-        *reinterpret_cast<float4 *>(g) = v;
-      } else {
-        *g += acc.x;
-      }
+    if (fin) {
+      if (C == 16)
+        *reinterpret_cast<float4 *>(gp) = make_float4(old.x + acc.x, old.y + acc.y, old.z + acc.z, old.w + acc.w);
+      else
+        *gp = old.x + acc.x;
     }
-    if (q.grad_tsdf && lane < 8) {
-      const int tx = i0[0] + ((lane >> 2) & 1), ty = i0[1] + ((lane >> 1) & 1), tz = i0[2] + (lane & 1);
-      if (tx >= 0 && ty >= 0 && tz >= 0 && tx < D && ty < D && tz < D)
-        q.grad_tsdf[(((size_t)b * D + tx) * D + ty) * D + tz] += acct;
-    }
+    if (tin) *tp = told + acct;
   }
 }
 
@@ -227,8 +262,8 @@ size_t det_layout(long R, int nseg, int C, long cap, char *base, DetWork *w) {
   d.seg_hit = (int *)take((size_t)(nseg + 1) * 4);
   d.ray_g = (float *)take((size_t)R * C * 4);
   d.rec_key = (uint32_t *)take((size_t)cap * 4);
-  d.rec_f = (float4 *)take((size_t)cap * 16);
-  d.rec_kt = (int2 *)take((size_t)cap * 8);
+  d.rec = (GradRecord *)take((size_t)cap * sizeof(GradRecord));
+  d.pay = (GradRecord *)take((size_t)cap * sizeof(GradRecord));
   // one more than cap: after the sort, one of the pairs holds the distinct
   // cells' first positions and the end of the last run
   d.ka = (uint32_t *)take((size_t)(cap + 1) * 4);
@@ -264,7 +299,13 @@ int launch_det_reduce(const DetWork &w, const RecordKeys &keys, long cap, int C,
                       sg_stream_t stream) {
   int key_bits = 1;
   while (key_bits < 32 && ((uint64_t)1 << key_bits) <= (uint64_t)keys.invalid) key_bits++;
-  const int passes = launch_radix_sort(w.rec_key, w.cnt + kDetSlots, cap, key_bits, w.ka, w.va, w.kb, w.vb,
+  const int g = grid_for(cap, 16);
+  // the records with a cell, compacted into the b pair (slot order kept)
+  int *flag = (int *)w.ka;
+  det_valid_flags_kernel<<<g, 256, 0, stream>>>(w.rec_key, w.cnt, keys.invalid, flag);
+  launch_excl_scan_dev(flag, cap, w.cnt + kDetSlots, flag, w.scan_scratch, w.cnt + kDetValid, stream);
+  det_compact_kernel<<<g, 256, 0, stream>>>(w.rec_key, w.cnt, keys.invalid, flag, w.kb, w.vb);
+  const int passes = launch_radix_sort(w.kb, w.vb, w.cnt + kDetValid, cap, key_bits, w.ka, w.va, w.kb, w.vb,
                                        w.sort_scratch, stream);
   const uint32_t *skey = (passes & 1) ? w.ka : w.kb;
   const uint32_t *sval = (passes & 1) ? w.va : w.vb;
@@ -274,10 +315,11 @@ int launch_det_reduce(const DetWork &w, const RecordKeys &keys, long cap, int C,
   int *heads = (int *)((passes & 1) ? w.kb : w.ka);
   int *ustart = (int *)((passes & 1) ? w.vb : w.va);
   uint32_t *ukey = w.rec_key;
-  det_heads_kernel<<<grid_for(cap, 16), 256, 0, stream>>>(skey, w.cnt, keys.invalid, heads);
-  launch_excl_scan_dev(heads, cap, w.cnt + kDetSlots, heads, w.scan_scratch, w.cnt + kDetCells, stream);
-  det_unique_kernel<<<grid_for(cap, 16), 256, 0, stream>>>(skey, heads, w.cnt, keys.invalid, ukey, ustart);
-  DetReduceParams q{keys, w.cnt, ukey, ustart, sval, w.rec_f, w.rec_kt, w.ray_g, grad_feat, grad_tsdf};
+  det_heads_kernel<<<g, 256, 0, stream>>>(skey, w.cnt, heads);
+  launch_excl_scan_dev(heads, cap, w.cnt + kDetValid, heads, w.scan_scratch, w.cnt + kDetCells, stream);
+  det_unique_kernel<<<g, 256, 0, stream>>>(skey, heads, w.cnt, ukey, ustart);
+  det_gather_kernel<<<g, 256, 0, stream>>>(sval, w.cnt, w.rec, w.pay);
+  DetReduceParams q{keys, w.cnt, ukey, ustart, w.pay, w.ray_g, grad_feat, grad_tsdf};
   for (int cls = 0; cls < 8; cls++) {
     if (C == 16) det_class_kernel<16><<<num_sms() * 8, 256, 0, stream>>>(q, cls);
     else det_class_kernel<3><<<num_sms() * 8, 256, 0, stream>>>(q, cls);

@@ -33,6 +33,13 @@ __host__ inline bool record_keys_fit(int B, int D) {
   return (double)B * (double)(D + 1) * (double)(D + 1) * (double)(D + 1) * 8.0 < 4294967295.0;
 }
 
+// One gradient record (32 bytes, one memory sector): the sample's cell
+// fractions and compositing weight, its compact ray and TSDF gradient (bits).
+struct __align__(16) GradRecord {
+  float4 fw;  // f0, f1, f2, w
+  int4 kt;    // k, gt bits, 0, 0
+};
+
 __device__ __forceinline__ uint32_t record_key(const RecordKeys &k, int b, const int (&i0)[3]) {
   if (i0[0] < -1 || i0[1] < -1 || i0[2] < -1 || i0[0] >= k.D || i0[1] >= k.D || i0[2] >= k.D) return k.invalid;
   const uint32_t e = (uint32_t)(k.D + 1);
@@ -57,17 +64,18 @@ __device__ __forceinline__ void record_cell(const RecordKeys &k, uint32_t key, i
 // workspace and launches of the deterministic reduction (scatter.cu)
 // ---------------------------------------------------------------------------
 constexpr int kDetCounters = 8;
-enum { kDetHits = 0, kDetSlotsNeeded = 1, kDetSlots = 2, kDetCells = 3 };
+enum { kDetHits = 0, kDetSlotsNeeded = 1, kDetSlots = 2, kDetCells = 3, kDetValid = 4 };
 
 struct DetWork {
-  int *cnt;                 // counters: rays with hits, slots needed, slots used, distinct cells
+  int *cnt;                 // counters: rays with hits, slots needed, slots used, distinct cells,
+                            // records with a cell
   int *hitb, *slotb;        // [R]: per ray -> exclusive counts of rays with hits / record slots
   int *hit_ray, *hit_slot;  // [R]: compact list of rays with hits, first slot of each
   int *seg_hit;             // [segments + 1]: compact index of each segment's first ray
   float *ray_g;             // [R][C]: per compact ray, head^T (colour gradient)
   uint32_t *rec_key;        // [cap] cell key per slot (later: the distinct cells' keys)
-  float4 *rec_f;            // [cap] cell fractions, compositing weight
-  int2 *rec_kt;             // [cap] compact ray, TSDF gradient (bits)
+  GradRecord *rec;          // [cap] record per slot
+  GradRecord *pay;          // [cap] the records in sorted key order
   uint32_t *ka, *va, *kb, *vb;  // [cap] sort buffers
   void *sort_scratch;
   int *scan_scratch;
@@ -84,9 +92,7 @@ struct DetReduceParams {
   const int *cnt;
   const uint32_t *ukey;
   const int *ustart;
-  const uint32_t *sorted_slot;
-  const float4 *rec_f;
-  const int2 *rec_kt;
+  const GradRecord *pay;
   const float *ray_g;
   float *grad_feat, *grad_tsdf;
 };

@@ -5,7 +5,8 @@
 // training step can be captured in a CUDA graph with no host read-back.
 //
 // Scan: blocks of 1024 ints (256 threads x 4) reduce to block sums, one CTA
-// scans the block sums, every block then scans itself from its offset.
+// scans the block sums, every block then scans itself from its offset; the
+// blocks past the live count are skipped by fixed, SM-sized grids.
 //
 // Radix sort: 8-bit digits, least significant first.  A tile is 4096 items:
 // 8 warps x 16 rounds x 32 lanes in index order.  Pass = per-tile digit
@@ -54,24 +55,32 @@ __device__ __forceinline__ long live_count(long n, const int *n_dev) {
   return m < n ? m : n;
 }
 
+// Blocks of kScanBlock elements up to the live count; a fixed grid strides
+// over them, so a capacity far above the live count costs no launches.
 __global__ void __launch_bounds__(256) scan_block_sums_kernel(const int *__restrict__ in, long n,
                                                               const int *__restrict__ n_dev,
                                                               int *__restrict__ bsum) {
   __shared__ int s_warp[17];
   n = live_count(n, n_dev);
-  const long base = (long)blockIdx.x * kScanBlock + threadIdx.x * 4;
-  int v = 0;
+  const long nb = (n + kScanBlock - 1) / kScanBlock;
+  for (long blk = blockIdx.x; blk < nb; blk += gridDim.x) {
+    const long base = blk * kScanBlock + threadIdx.x * 4;
+    int v = 0;
 #pragma unroll
-  for (int k = 0; k < 4; k++) v += (base + k < n) ? in[base + k] : 0;
-  int total;
-  block_excl_scan_256(v, s_warp, total);
-  if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+    for (int k = 0; k < 4; k++) v += (base + k < n) ? in[base + k] : 0;
+    int total;
+    block_excl_scan_256(v, s_warp, total);
+    if (threadIdx.x == 0) bsum[blk] = total;
+  }
 }
 
-// One CTA of 1024 threads: exclusive scan of nb block sums in place, total
-// into *total.
-__global__ void __launch_bounds__(1024) scan_sums_kernel(int *bsum, int nb, int *total) {
+// One CTA of 1024 threads: exclusive scan of the live block sums in place,
+// total into *total.
+__global__ void __launch_bounds__(1024) scan_sums_kernel(int *bsum, long n, const int *__restrict__ n_dev,
+                                                         int *total) {
   __shared__ int s_w[33];
+  n = live_count(n, n_dev);
+  const int nb = (int)((n + kScanBlock - 1) / kScanBlock);
   const int lane = lane_id(), w = threadIdx.x >> 5;
   int carry = 0;
   for (int c0 = 0; c0 < nb; c0 += 1024) {
@@ -99,20 +108,22 @@ __global__ void __launch_bounds__(256) scan_apply_kernel(const int *__restrict__
                                                          const int *__restrict__ bsum, int *__restrict__ out) {
   __shared__ int s_warp[17];
   n = live_count(n, n_dev);
-  if ((long)blockIdx.x * kScanBlock >= n) return;
-  const long base = (long)blockIdx.x * kScanBlock + threadIdx.x * 4;
-  int v[4], s = 0;
+  const long nb = (n + kScanBlock - 1) / kScanBlock;
+  for (long blk = blockIdx.x; blk < nb; blk += gridDim.x) {
+    const long base = blk * kScanBlock + threadIdx.x * 4;
+    int v[4], s = 0;
 #pragma unroll
-  for (int k = 0; k < 4; k++) {
-    v[k] = (base + k < n) ? in[base + k] : 0;
-    s += v[k];
-  }
-  int total;
-  int run = block_excl_scan_256(s, s_warp, total) + bsum[blockIdx.x];
+    for (int k = 0; k < 4; k++) {
+      v[k] = (base + k < n) ? in[base + k] : 0;
+      s += v[k];
+    }
+    int total;
+    int run = block_excl_scan_256(s, s_warp, total) + bsum[blk];
 #pragma unroll
-  for (int k = 0; k < 4; k++) {
-    if (base + k < n) out[base + k] = run;
-    run += v[k];
+    for (int k = 0; k < 4; k++) {
+      if (base + k < n) out[base + k] = run;
+      run += v[k];
+    }
   }
 }
 
@@ -120,17 +131,18 @@ size_t scan_scratch_ints(long n) { return (size_t)ceil_div(n, kScanBlock) + 1; }
 
 void launch_excl_scan_dev(const int *in, long n, const int *n_dev, int *out, int *scratch, int *total,
                           sg_stream_t stream) {
-  const int nb = ceil_div(n, kScanBlock);
+  const long nb = ceil_div(n, kScanBlock);
   if (nb == 0) {
-    // nothing to scan: a zero total (through a one-thread launch, so that
-    // the call stays a stream operation)
-    scan_sums_kernel<<<1, 1024, 0, stream>>>(scratch, 0, total);
+    // nothing to scan: a zero total (through a one-CTA launch, so that the
+    // call stays a stream operation)
+    scan_sums_kernel<<<1, 1024, 0, stream>>>(scratch, 0, nullptr, total);
     return;
   }
-  // blocks past the live count contribute 0 and write nothing
-  scan_block_sums_kernel<<<nb, 256, 0, stream>>>(in, n, n_dev, scratch);
-  scan_sums_kernel<<<1, 1024, 0, stream>>>(scratch, nb, total);
-  scan_apply_kernel<<<nb, 256, 0, stream>>>(in, n, n_dev, scratch, out);
+  const long cap = (long)num_sms() * 8;
+  const int g = (int)(nb < cap ? nb : cap);
+  scan_block_sums_kernel<<<g, 256, 0, stream>>>(in, n, n_dev, scratch);
+  scan_sums_kernel<<<1, 1024, 0, stream>>>(scratch, n, n_dev, total);
+  scan_apply_kernel<<<g, 256, 0, stream>>>(in, n, n_dev, scratch, out);
 }
 
 void launch_excl_scan(const int *in, long n, int *out, int *scratch, int *total, sg_stream_t stream) {
@@ -154,21 +166,26 @@ __global__ void __launch_bounds__(256) radix_hist_kernel(const uint32_t *__restr
                                                          const int *__restrict__ meta, int *__restrict__ hist) {
   __shared__ int s_h[kDigits];
   const int ntiles = meta[0];
-  if ((int)blockIdx.x >= ntiles) return;
-  s_h[threadIdx.x] = 0;
-  __syncthreads();
   const long n = *n_dev;
-  const long base = (long)blockIdx.x * kSortTile;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    s_h[threadIdx.x] = 0;
+    __syncthreads();
+    const long base = (long)tile * kSortTile;
 #pragma unroll 4
-  for (int k = 0; k < kSortTile / 256; k++) {
-    const long i = base + k * 256 + threadIdx.x;
-    if (i < n) atomicAdd(&s_h[(__ldg(keys + i) >> shift) & 0xff], 1);
+    for (int k = 0; k < kSortTile / 256; k++) {
+      const long i = base + k * 256 + threadIdx.x;
+      if (i < n) atomicAdd(&s_h[(__ldg(keys + i) >> shift) & 0xff], 1);
+    }
+    __syncthreads();
+    hist[(size_t)threadIdx.x * ntiles + tile] = s_h[threadIdx.x];  // digit-major, live tiles
+    __syncthreads();
   }
-  __syncthreads();
-  hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = s_h[threadIdx.x];  // digit-major, live tiles
 }
 
-// vals == nullptr: the values are the item indices.
+// vals == nullptr: the values are the item indices.  The tile's items are
+// first placed in shared memory in their sorted order (digit runs in digit
+// order), then written out with consecutive threads on consecutive
+// destinations of each digit run.
 __global__ void __launch_bounds__(256) radix_scatter_kernel(const uint32_t *__restrict__ keys,
                                                             const uint32_t *__restrict__ vals,
                                                             const int *__restrict__ n_dev, int shift,
@@ -178,55 +195,72 @@ __global__ void __launch_bounds__(256) radix_scatter_kernel(const uint32_t *__re
                                                             uint32_t *__restrict__ vals_out) {
   constexpr int R = kSortTile / 256;  // rounds per warp
   __shared__ int s_cnt[8][kDigits];   // per-warp running count per digit
+  __shared__ int s_start[kDigits];    // first tile position of each digit
+  __shared__ int s_warp[17];
+  __shared__ uint32_t s_key[kSortTile], s_val[kSortTile];
   const int ntiles = meta[0];
-  if ((int)blockIdx.x >= ntiles) return;
   const int lane = lane_id(), w = threadIdx.x >> 5;
-  for (int d = lane; d < kDigits; d += 32) s_cnt[w][d] = 0;
-  __syncwarp();
   const long n = *n_dev;
-  const long wbase = (long)blockIdx.x * kSortTile + (long)w * (R * 32);
-  uint32_t k[R], v[R];
-  int rank[R];
   const unsigned lt = (1u << lane) - 1u;
-#pragma unroll
-  for (int q = 0; q < R; q++) {
-    const long i = wbase + q * 32 + lane;
-    const bool live = i < n;
-    k[q] = live ? __ldg(keys + i) : 0u;
-    v[q] = live ? (vals ? __ldg(vals + i) : (uint32_t)i) : 0u;
-    // inactive lanes match each other on a digit value no live key has
-    const unsigned dg = live ? ((k[q] >> shift) & 0xffu) : 0x100u;
-    const unsigned peers = __match_any_sync(SG_FULL, dg);
-    const int before = __popc(peers & lt);
-    int c = 0;
-    if (live) c = s_cnt[w][dg];
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    for (int d = lane; d < kDigits; d += 32) s_cnt[w][d] = 0;
     __syncwarp();
-    if (live && before == 0) s_cnt[w][dg] = c + __popc(peers);
-    __syncwarp();
-    rank[q] = c + before;
-  }
-  __syncthreads();
-  // warp offsets per digit: counts of the warps before
-  {
-    const int d = threadIdx.x;  // 256 threads, one digit each
-    int run = 0;
+    const long tbase = (long)tile * kSortTile;
+    const long wbase = tbase + (long)w * (R * 32);
+    uint32_t k[R], v[R];
+    int rank[R];
 #pragma unroll
-    for (int ww = 0; ww < 8; ww++) {
-      const int c = s_cnt[ww][d];
-      s_cnt[ww][d] = run;
-      run += c;
+    for (int q = 0; q < R; q++) {
+      const long i = wbase + q * 32 + lane;
+      const bool live = i < n;
+      k[q] = live ? __ldg(keys + i) : 0u;
+      v[q] = live ? (vals ? __ldg(vals + i) : (uint32_t)i) : 0u;
+      // inactive lanes match each other on a digit value no live key has
+      const unsigned dg = live ? ((k[q] >> shift) & 0xffu) : 0x100u;
+      const unsigned peers = __match_any_sync(SG_FULL, dg);
+      const int before = __popc(peers & lt);
+      int c = 0;
+      if (live) c = s_cnt[w][dg];
+      __syncwarp();
+      if (live && before == 0) s_cnt[w][dg] = c + __popc(peers);
+      __syncwarp();
+      rank[q] = c + before;
     }
-  }
-  __syncthreads();
+    __syncthreads();
+    // per digit: the counts of the warps before each warp, and the tile total
+    {
+      const int d = threadIdx.x;  // 256 threads, one digit each
+      int run = 0;
 #pragma unroll
-  for (int q = 0; q < R; q++) {
-    const long i = wbase + q * 32 + lane;
-    if (i < n) {
-      const int dg = (k[q] >> shift) & 0xff;
-      const long dst = (long)offs[(size_t)dg * ntiles + blockIdx.x] + s_cnt[w][dg] + rank[q];
-      keys_out[dst] = k[q];
-      vals_out[dst] = v[q];
+      for (int ww = 0; ww < 8; ww++) {
+        const int c = s_cnt[ww][d];
+        s_cnt[ww][d] = run;
+        run += c;
+      }
+      int total;
+      s_start[d] = block_excl_scan_256(run, s_warp, total);
     }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < R; q++) {
+      const long i = wbase + q * 32 + lane;
+      if (i < n) {
+        const int dg = (k[q] >> shift) & 0xff;
+        const int pos = s_start[dg] + s_cnt[w][dg] + rank[q];
+        s_key[pos] = k[q];
+        s_val[pos] = v[q];
+      }
+    }
+    __syncthreads();
+    const int live = (int)(n - tbase < kSortTile ? n - tbase : kSortTile);
+    for (int i = threadIdx.x; i < live; i += 256) {
+      const uint32_t key = s_key[i];
+      const int dg = (key >> shift) & 0xff;
+      const long dst = (long)offs[(size_t)dg * ntiles + tile] + (i - s_start[dg]);
+      keys_out[dst] = key;
+      vals_out[dst] = s_val[i];
+    }
+    __syncthreads();
   }
 }
 
@@ -236,9 +270,12 @@ size_t radix_scratch_bytes(long cap) {
   return (size_t)(2 * table + (long)scan_scratch_ints(table) + 8) * sizeof(int);
 }
 
-int launch_radix_sort(const uint32_t *keys_in, const int *n_dev, long cap, int key_bits, uint32_t *keys_a,
-                      uint32_t *vals_a, uint32_t *keys_b, uint32_t *vals_b, void *scratch, sg_stream_t stream) {
+int launch_radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, const int *n_dev, long cap, int key_bits,
+                      uint32_t *keys_a, uint32_t *vals_a, uint32_t *keys_b, uint32_t *vals_b, void *scratch,
+                      sg_stream_t stream) {
   const int ntiles = ceil_div(cap, kSortTile) > 0 ? ceil_div(cap, kSortTile) : 1;
+  const int ghist = ntiles < num_sms() * 8 ? ntiles : num_sms() * 8;
+  const int gscat = ntiles < num_sms() * 4 ? ntiles : num_sms() * 4;
   const long table = (long)ntiles * kDigits;
   int *hist = (int *)scratch;
   int *offs = hist + table;
@@ -247,14 +284,14 @@ int launch_radix_sort(const uint32_t *keys_in, const int *n_dev, long cap, int k
   int *meta = tot + 2;
   const int passes = key_bits <= 0 ? 1 : (key_bits + 7) / 8;
   const uint32_t *ki = keys_in;
-  const uint32_t *vi = nullptr;
+  const uint32_t *vi = vals_in;
   radix_meta_kernel<<<1, 1, 0, stream>>>(n_dev, meta);
   for (int p = 0; p < passes; p++) {
     uint32_t *ko = (p & 1) ? keys_b : keys_a;
     uint32_t *vo = (p & 1) ? vals_b : vals_a;
-    radix_hist_kernel<<<ntiles, 256, 0, stream>>>(ki, n_dev, 8 * p, meta, hist);
+    radix_hist_kernel<<<ghist, 256, 0, stream>>>(ki, n_dev, 8 * p, meta, hist);
     launch_excl_scan_dev(hist, table, meta + 1, offs, ss, tot, stream);
-    radix_scatter_kernel<<<ntiles, 256, 0, stream>>>(ki, vi, n_dev, 8 * p, meta, offs, ko, vo);
+    radix_scatter_kernel<<<gscat, 256, 0, stream>>>(ki, vi, n_dev, 8 * p, meta, offs, ko, vo);
     ki = ko;
     vi = vo;
   }
@@ -273,8 +310,8 @@ extern "C" int sg_sort_pairs(const uint32_t *keys, const int *count, long long c
   if (!keys || !count || !keys_out || !vals_out || !keys_tmp || !vals_tmp || !scratch) return SG_ERR_INVALID_ARG;
   if (capacity <= 0 || capacity >= (1ll << 31) || key_bits < 1 || key_bits > 32) return SG_ERR_INVALID_ARG;
   if (scratch_bytes < radix_scratch_bytes((long)capacity)) return SG_ERR_INVALID_ARG;
-  const int passes = launch_radix_sort(keys, count, (long)capacity, key_bits, keys_out, vals_out, keys_tmp,
-                                       vals_tmp, scratch, stream);
+  const int passes = launch_radix_sort(keys, nullptr, count, (long)capacity, key_bits, keys_out, vals_out,
+                                       keys_tmp, vals_tmp, scratch, stream);
   if (passes % 2 == 0) {
     // the last pass wrote the second pair: copy it into the outputs
     cudaMemcpyAsync(keys_out, keys_tmp, (size_t)capacity * 4, cudaMemcpyDeviceToDevice, (cudaStream_t)stream);

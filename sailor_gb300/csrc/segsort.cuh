@@ -21,11 +21,13 @@ void launch_excl_scan_dev(const int *in, long n, const int *n_dev, int *out, int
 // bytes of scratch a radix sort of up to cap items needs
 size_t radix_scratch_bytes(long cap);
 
-// Stable sort of (keys_in[i], i) for i < *n_dev (n_dev <= cap) by the low
-// key_bits bits of the keys, 8 bits a pass; passes alternate between the
-// (keys_a, vals_a) and (keys_b, vals_b) buffers, starting with a.  Returns
+// Stable sort of (keys_in[i], vals_in[i]) for i < *n_dev (n_dev <= cap;
+// vals_in null: the values are i) by the low key_bits bits of the keys, 8
+// bits a pass; passes alternate between the (keys_a, vals_a) and (keys_b,
+// vals_b) buffers, starting with a (the input may be the b pair).  Returns
 // the number of passes: the result is in a when it is odd, in b when even.
-int launch_radix_sort(const uint32_t *keys_in, const int *n_dev, long cap, int key_bits, uint32_t *keys_a,
-                      uint32_t *vals_a, uint32_t *keys_b, uint32_t *vals_b, void *scratch, sg_stream_t stream);
+int launch_radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, const int *n_dev, long cap, int key_bits,
+                      uint32_t *keys_a, uint32_t *vals_a, uint32_t *keys_b, uint32_t *vals_b, void *scratch,
+                      sg_stream_t stream);
 
 }  // namespace sg

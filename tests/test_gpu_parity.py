@@ -161,6 +161,36 @@ def test_axis_aligned_rays(case):
     assert np.array_equal(si.cpu().numpy(), si2) and np.array_equal(sz.cpu().numpy(), sz2)
 
 
+@pytest.mark.parametrize("mode", ["inference", "training", "early_stop", "opt_num"])
+def test_intersection_variants_identical(case, mode):
+    """The warp-cooperative intersection (a warp per hit brick's children)
+    and the thread-per-ray one give the same rows, counts, t-intervals and
+    valid lengths bit for bit, in every traversal mode, with padded rows and
+    with rows too narrow for some rays."""
+    from sailor_gb300 import autotune
+    g = case["g"]
+    octree = g["octree"]
+    args = dict(inference=(-1, False, -1), training=(-1, True, -1), early_stop=(2, False, -1),
+                opt_num=(-1, False, 3))[mode]
+    saved = autotune.current()
+    outs = []
+    try:
+        for wv in (0, 1):
+            autotune.set_knob("isect_warp", wv)
+            for W in (case["W"], 8):
+                idx, t0, t1, vl = octree.voxel_traversal(_t(case["ori"]), _t(case["dirs"]), W, 0, args[0], args[1],
+                                                         args[2])
+                torch.cuda.synchronize()
+                outs.append((idx.clone(), t0.clone(), t1.clone(), vl.clone(), octree._status.clone()))
+    finally:
+        for k, v in saved.items():
+            autotune.set_knob(k, v)
+    for a, b in zip(outs[:2], outs[2:]):
+        for x, y in zip(a, b):
+            assert torch.equal(x, y)
+    assert (outs[0][0] >= 0).sum().item() > 100
+
+
 def test_rays_starting_inside(case):
     """Rays whose origin lies inside the volume (the whole-grid slab test
     clamps the entry to t = 0, so the walk starts in the origin's brick):
