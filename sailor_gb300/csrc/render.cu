@@ -334,14 +334,29 @@ __device__ __forceinline__ void emit_records(const RenderParams &p, long k, long
 // training pass of the smaller sample capacities has less live state, so
 // more of its warps fit (64 and 80 registers, a few bytes spilled; 4 and 3
 // CTAs measured 7 % faster over the batched step than 2 CTAs at 128).
-template <int E, bool TRAIN>
-constexpr int kBwdMinBlocks = !TRAIN ? 2 : (E == 1 ? 4 : (E == 2 ? 3 : 2));
+// The record-mode pass (REC) carries no scatter state, so more of its CTAs
+// fit: 4 / 4 / 3 at up to 32 / 64 / 128 samples (measured 0.27 ms faster on
+// the batched step than 4 / 3 / 2; 5 / 4 / 3 and 6 / 4 / 2 were slower).
+// Build-time settings SG_REC_MINB_E1/E2/E4.
+#ifndef SG_REC_MINB_E1
+#define SG_REC_MINB_E1 4
+#endif
+#ifndef SG_REC_MINB_E2
+#define SG_REC_MINB_E2 4
+#endif
+#ifndef SG_REC_MINB_E4
+#define SG_REC_MINB_E4 3
+#endif
+template <int E, bool TRAIN, bool REC = false>
+constexpr int kBwdMinBlocks = !TRAIN ? 2
+                              : (REC ? (E == 1 ? SG_REC_MINB_E1 : (E == 2 ? SG_REC_MINB_E2 : SG_REC_MINB_E4))
+                                     : (E == 1 ? 4 : (E == 2 ? 3 : 2)));
 
 // REC: the rays are the compact list of rays with hits and the grid
 // gradients leave the kernel as per-sample records (emit_records) for the
 // deterministic reduction, instead of the in-kernel scatter with atomics.
 template <int E, int C, bool TRAIN, bool REC>
-__global__ void __launch_bounds__(256, kBwdMinBlocks<E, TRAIN>) render_bwd_kernel(RenderParams p) {
+__global__ void __launch_bounds__(256, kBwdMinBlocks<E, TRAIN, REC>) render_bwd_kernel(RenderParams p) {
   static_assert(C == 3 || C == 16, "feature grids of 3 or 16 channels");
   SG_RENDER_SMEM(E)
   __shared__ float s_wf[REC ? 1 : 8][32][9], s_wt[REC ? 1 : 8][32][9];

@@ -166,6 +166,11 @@ __device__ __forceinline__ int lower_bound_u32(const uint32_t *a, int n, uint32_
 // sums added into the 8 corner voxels of the feature grid (and TSDF grid).
 template <int C>
 __global__ void __launch_bounds__(256) det_class_kernel(DetReduceParams q, int cls) {
+  // per warp: the current chunk of up to 32 records of a run and the G rows
+  // of their rays, loaded by all lanes at once and read back in run order
+  __shared__ __align__(16) float4 s_g[8][32][4];
+  __shared__ __align__(16) float4 s_f[8][32];
+  __shared__ float s_t[8][32];
   __shared__ int s_rng[2];
   const int nu = q.cnt[kDetCells];
   if (threadIdx.x == 0) {
@@ -174,7 +179,7 @@ __global__ void __launch_bounds__(256) det_class_kernel(DetReduceParams q, int c
   }
   __syncthreads();
   const int lo = s_rng[0], hi = s_rng[1];
-  const int lane = lane_id();
+  const int lane = lane_id(), w8 = threadIdx.x >> 5;
   // lane -> (corner, channels): C == 16: corner lane / 4, channels 4 (lane % 4)..+3;
   // C == 3: lanes < 24, corner lane / 3, channel lane % 3.  TSDF: corner = lane (< 8).
   const int cr = C == 16 ? (lane >> 2) : (lane < 24 ? lane / 3 : 0);
@@ -203,33 +208,41 @@ __global__ void __launch_bounds__(256) det_class_kernel(DetReduceParams q, int c
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     float acct = 0.0f;
     for (int c0 = j0; c0 < j1; c0 += 32) {
-      // lane jj loads the run's record c0 + jj (the records are in sorted
-      // order: one coalesced load); then the samples are summed in run order
-      float4 fw = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      int4 kt = make_int4(0, 0, 0, 0);
+      // lane jj stages the run's record c0 + jj (sorted: one coalesced load)
+      // and its ray's G row; then the samples are summed in run order
       if (c0 + lane < j1) {
-        fw = __ldg(&q.pay[c0 + lane].fw);
-        kt = __ldg(&q.pay[c0 + lane].kt);
+        const float4 fw = __ldg(&q.pay[c0 + lane].fw);
+        const int4 kt = __ldg(&q.pay[c0 + lane].kt);
+        const float *g = q.ray_g + (size_t)kt.x * C;
+        if (C == 16) {
+#pragma unroll
+          for (int v = 0; v < 4; v++) s_g[w8][lane][v] = __ldg(reinterpret_cast<const float4 *>(g) + v);
+        } else {
+          s_g[w8][lane][0] = make_float4(__ldg(g), __ldg(g + 1), __ldg(g + 2), 0.0f);
+        }
+        s_f[w8][lane] = fw;
+        s_t[w8][lane] = __int_as_float(kt.y);
       }
+      __syncwarp();
       const int m = min(32, j1 - c0);
 #pragma unroll 4
       for (int jj = 0; jj < m; jj++) {
-        const float f[3] = {__shfl_sync(SG_FULL, fw.x, jj), __shfl_sync(SG_FULL, fw.y, jj),
-                            __shfl_sync(SG_FULL, fw.z, jj)};
-        const float a = corner_weight(f, cr) * __shfl_sync(SG_FULL, fw.w, jj);
-        const int k = __shfl_sync(SG_FULL, kt.x, jj);
-        const float gt = __int_as_float(__shfl_sync(SG_FULL, kt.y, jj));
+        const float4 fw = s_f[w8][jj];
+        const float f[3] = {fw.x, fw.y, fw.z};
+        const float a = corner_weight(f, cr) * fw.w;
         if (C == 16) {
-          const float4 g = __ldg(reinterpret_cast<const float4 *>(q.ray_g + (size_t)k * C + ch));
+          const float4 g = s_g[w8][jj][lane & 3];
           acc.x = __fmaf_rn(a, g.x, acc.x);
           acc.y = __fmaf_rn(a, g.y, acc.y);
           acc.z = __fmaf_rn(a, g.z, acc.z);
           acc.w = __fmaf_rn(a, g.w, acc.w);
         } else if (fown) {
-          acc.x = __fmaf_rn(a, __ldg(q.ray_g + (size_t)k * C + ch), acc.x);
+          const float4 g = s_g[w8][jj][0];
+          acc.x = __fmaf_rn(a, ch == 0 ? g.x : (ch == 1 ? g.y : g.z), acc.x);
         }
-        if (q.grad_tsdf && lane < 8) acct = __fmaf_rn(corner_weight(f, lane), gt, acct);
+        if (q.grad_tsdf && lane < 8) acct = __fmaf_rn(corner_weight(f, lane), s_t[w8][jj], acct);
       }
+      __syncwarp();
     }
     if (fin) {
       if (C == 16)
