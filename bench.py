@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="small configuration (256^3, 512^2) for profiling")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
-    ap.add_argument("--workload", default="batch", choices=["batch", "plain", "project", "diff"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "plain", "project", "diff", "octree"])
     ap.add_argument("--unfused", action="store_true",
                     help="render with four kernels (sample+sort, two field gathers, composite) instead of one")
     ap.add_argument("--no-parity", action="store_true",
@@ -1270,6 +1270,266 @@ def run_diff(args):
     print(json.dumps(out), flush=True)
 
 
+# --------------------------------------------------------------------------
+# multi-level tree (four levels, rate 2): build, coarse DDA + depth-first
+# descent and fine sampling through the drop-in MultiLayerOctree
+# (octree_traversal / ray_voxels_points_sampling, the reference's
+# only_voxel_traversal=False mode)
+# --------------------------------------------------------------------------
+OCTREE = dict(views=4, res=512, prims=12, D=256, rate=2, levels=4, trunc=0.03, target=512, start=1, S=64, Wf=512,
+              seed=19)
+
+
+def octree_setup(cfg, dev):
+    """The fused 256^3 occupancy (drop-in integrate_in_box), its four-level
+    pyramid (build_multi_res_volumes), a 512^2 target camera's rays and
+    seeded rands.  Returns pristine volumes (the build rewrites its input
+    volumes with node ids, so each step restores them first)."""
+    import torch
+
+    from sailor_gb300 import synthetic as syn
+    from sailor_gb300.dist import VoxelEncoding as VE
+    sc = syn.make_scene(seed=cfg["seed"], n_views=cfg["views"], res=cfg["res"], n_prims=cfg["prims"], D=cfg["D"],
+                        trunc=cfg["trunc"])
+    D, L, rate = cfg["D"], cfg["levels"], cfg["rate"]
+
+    def T(a, dt=torch.float32):
+        return torch.as_tensor(np.ascontiguousarray(a), dtype=dt).to(dev)
+    occ = torch.full((1, D, D, D), -1, dtype=torch.int32, device=dev)
+    cnt = torch.zeros((1, 1), dtype=torch.int32, device=dev)
+    VE.integrate_in_box(occ, cnt, T(sc["K"]), T(sc["RT"]), T(sc["colors"]), T(sc["depths"]), T(sc["vol_bbox"]),
+                        T(sc["voxel_size"]), 1.0, sc["trunc_weight"], 13.5, 13.5, 0)
+    vols = [occ] + [torch.full((1,) + (D // rate ** l,) * 3, -1, dtype=torch.int32, device=dev)
+                    for l in range(1, L)]
+    cnts = [cnt] + [torch.zeros((1, 1), dtype=torch.int32, device=dev) for _ in range(1, L)]
+    VE.build_multi_res_volumes(vols, cnts, L, rate, 0)
+    ori, dirs = syn.target_rays(seed=cfg["seed"], res=cfg["target"])
+    S = cfg["S"]
+    rands = torch.rand((1, ori.shape[1], S), generator=torch.Generator(device=dev).manual_seed(cfg["seed"]),
+                       device=dev)
+    return dict(sc=sc, pristine=[v.clone() for v in vols], vols=vols, cnts=cnts, ori=ori, dirs=dirs, o=T(ori),
+                d=T(dirs), rands=rands, vs=T(sc["voxel_size"]), bbox=T(sc["vol_bbox"]))
+
+
+def octree_tree(d, cfg):
+    from sailor_gb300.dist import VoxelEncoding as VE
+    L = cfg["levels"]
+    totals = [int(c.sum().item()) for c in d["cnts"]]
+    index = [sum(totals[:l]) for l in range(L)]
+    o = VE.MultiLayerOctree(L, 1, cfg["rate"], 0)
+    o.init_octree(d["vols"], totals, d["cnts"], index, d["vs"], d["bbox"])
+    return o
+
+
+def octree_wc(cfg):
+    # coarse rows: three cells per coarse-grid edge (voxel_encoding_helper.py:573)
+    return cfg["D"] * 3 // cfg["rate"] ** (cfg["levels"] - cfg["start"] - 1)
+
+
+def octree_step(o, d, cfg, events=None):
+    """Restore the volumes, build, traverse, sample.  events: a list that
+    receives (name, start, end) CUDA events per stage."""
+    import torch
+
+    def mark():
+        if events is None:
+            return None
+        e = torch.cuda.Event(enable_timing=True)
+        e.record()
+        return e
+    e0 = mark()
+    for a, b in zip(d["vols"], d["pristine"]):
+        a.copy_(b)
+    o.build_octree()
+    e1 = mark()
+    rows = o.octree_traversal(d["o"], d["d"], octree_wc(cfg), cfg["Wf"], cfg["start"], -1, -1)
+    e2 = mark()
+    idx, t0, t1, vl = rows[:4]
+    si, sz = o.ray_voxels_points_sampling(idx, t0, t1, vl, d["rands"], cfg["start"], cfg["S"])
+    e3 = mark()
+    if events is not None:
+        events += [("build", e0, e1), ("traversal", e1, e2), ("sampling", e2, e3)]
+    return rows, si, sz
+
+
+def _cpu_octree_job(cfg, occ0, ori, dirs, vs, bbox, reps, n_rays=4096):
+    """The oracle's C port on the host cores (spawned process): the
+    multi-level build of the whole volume, and traversal + fine sampling of
+    n_rays rays drawn from the target, scaled to all its rays."""
+    import time
+
+    from oracle import oracle as orc
+    L, rate, S = cfg["levels"], cfg["rate"], cfg["S"]
+    R = ori.shape[1]
+    pick = np.random.default_rng(5).choice(R, n_rays, replace=False)
+    rd = np.random.default_rng(6).random((1, n_rays, S), dtype=np.float32)
+    out = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        vols, _ = orc.merge_levels(occ0, (occ0 > -1).sum(), rate, L)
+        t = orc.build_octree(vols, rate)
+        t1 = time.perf_counter()
+        ot = orc.octree_traversal(t, ori[:, pick], dirs[:, pick], vs, bbox, cfg["start"], octree_wc(cfg),
+                                  cfg["Wf"])
+        orc.sample_fine(t, ot["idx"], ot["t0"], ot["t1"], ot["valid_len"], rd, vs, S, cfg["start"])
+        t2 = time.perf_counter()
+        sec = (t1 - t0) + (t2 - t1) * R / n_rays
+        out.append(dict(value=R / sec, sample_wall_s=t2 - t0))
+    return out, orc.num_threads()
+
+
+def cpu_baseline_octree(cfg, occ0, ori, dirs, vs, bbox, reps):
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    with cf.ProcessPoolExecutor(max_workers=1, mp_context=mp.get_context("spawn")) as ex:
+        runs, cores = ex.submit(_cpu_octree_job, cfg, occ0, ori, dirs, vs, bbox, reps).result()
+    return dict(value=float(np.median([r["value"] for r in runs])), unit="rays/s", cores=cores, kind="port",
+                sample="oracle (C port, OpenMP) on host cores: merge + multi-level build of the whole volume, "
+                       "traversal + fine sampling of 4096 of the target's rays scaled to all of them; median of "
+                       f"{len(runs)} samples in a separate process",
+                samples=[r["value"] for r in runs], sample_wall_s=[r["sample_wall_s"] for r in runs])
+
+
+def parity_octree(o, d, cfg, rows, si, sz, n_rays=4096):
+    """After timing: the tree bit-exact, traversal rows of n_rays rays exact
+    on the rays the oracle does not flag (depths within 1e-5 relative), fine
+    samples bit-exact against the oracle run on the GPU's own rows."""
+    import time
+
+    from oracle import oracle as orc
+    t_start = time.perf_counter()
+    L, rate, S, st = cfg["levels"], cfg["rate"], cfg["S"], cfg["start"]
+    vols = [v.cpu().numpy() for v in d["pristine"]]
+    ref = orc.build_octree(vols, rate)
+    tree_ok = all(np.array_equal(d["vols"][l].cpu().numpy(), ref["vols"][l]) for l in range(L))
+    R = d["ori"].shape[1]
+    pick = np.sort(np.random.default_rng(8).choice(R, n_rays, replace=False))
+    vs = d["sc"]["voxel_size"].reshape(-1).astype(np.float32)
+    bb = d["sc"]["vol_bbox"].astype(np.float32)
+    ot = orc.octree_traversal(ref, d["ori"][:, pick], d["dirs"][:, pick], vs, bb, st, octree_wc(cfg), cfg["Wf"])
+    g = [x.cpu().numpy()[:, pick] for x in rows]
+    ok = ot["flags"][0] == 0
+    mism = int(np.any(g[0][0][ok] != ot["idx"][0][ok], 1).sum() + np.any(g[4][0][ok] != ot["idx_c"][0][ok], 1).sum())
+    terr = float(max(np.abs(g[1][0][ok] - ot["t0"][0][ok]).max(), np.abs(g[2][0][ok] - ot["t1"][0][ok]).max()))
+    vrel = float((np.abs(g[3][0, :, 0] - ot["valid_len"][0, :, 0]) /
+                  np.maximum(ot["valid_len"][0, :, 0], 1e-6))[ok].max())
+    rd = d["rands"].cpu().numpy()[:, pick]
+    ri, rz, _ = orc.sample_fine(ref, g[0], g[1], g[2], g[3], rd, vs, S, st)
+    smis = int((si.cpu().numpy()[:, pick] != ri).sum() + (sz.cpu().numpy()[:, pick] != rz).sum())
+    return dict(tree_bit_exact=bool(tree_ok), rays=int(n_rays), rays_flagged=int((~ok).sum()),
+                unflagged_row_mismatches=mism, t_max_abs_err=terr, valid_len_max_rel_err=vrel,
+                sample_mismatches=smis, seconds=time.perf_counter() - t_start)
+
+
+def run_octree(args):
+    import tempfile
+
+    import torch
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    cfg = dict(OCTREE)
+    if args.small:
+        cfg.update(D=128, res=256, target=256)
+    d = octree_setup(cfg, dev)
+    o = octree_tree(d, cfg)
+    warm = max(args.warmup, 3)
+    for _ in range(warm):
+        rows, si, sz = octree_step(o, d, cfg)
+    torch.cuda.synchronize()
+    st = o._ostatus.cpu().numpy()
+    if st[0]:
+        raise RuntimeError(f"octree status {st.tolist()}")
+    clk = ClockSampler(os.path.join(tempfile.gettempdir(), "sg_clocks_octree.csv"))
+    with clk:
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            rows, si, sz = octree_step(o, d, cfg)
+        e1.record()
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    stage_sum = {}
+    for _ in range(args.steps):
+        ev = []
+        rows, si, sz = octree_step(o, d, cfg, ev)
+        torch.cuda.synchronize()
+        for k, a, b in ev:
+            stage_sum[k] = stage_sum.get(k, 0.0) + a.elapsed_time(b)
+    stages = {k: v / args.steps for k, v in stage_sum.items()}
+    R, S, L = d["ori"].shape[1], cfg["S"], cfg["levels"]
+    Wc, Wf = octree_wc(cfg), cfg["Wf"]
+    counts = o._obufs["counts"].cpu().numpy()
+    n_fine = int((rows[0] >= 0).sum().item())
+    n_coarse = int((rows[4] >= 0).sum().item())
+    vox = sum(int(v.numel()) for v in d["vols"])
+    # algorithmic bytes: the build reads every level's volume, writes the
+    # node tables (key, parent, child base, count) and each node's volume
+    # entry (the volume restore is a copy of the same size, counted too);
+    # the traversal reads the rays and writes both padded row sets (the
+    # reference's output contract) and the valid lengths; the sampler reads
+    # the fine entries, valid lengths and rands and writes S samples a ray
+    ab = dict(build=8 * vox + 4 * vox + 20 * int(counts.sum()),
+              traversal=24 * R + 12 * R * (Wc + Wf) + 4 * R,
+              sampling=12 * n_fine + 4 * R + 4 * R * S + 8 * R * S)
+    pk, pk_kind = peaks()
+    rl = {k: ab[k] / (stages[k] / 1000.0) / 1e9 for k in ab if stages.get(k)}
+    dom = max(rl, key=lambda k: stages[k])
+    # e2e through the drop-in API from pinned host buffers: the occupancy
+    # pyramid and the rays up, the samples down
+    host = dict(vols=[v.cpu().pin_memory() for v in d["pristine"]], o=torch.as_tensor(d["ori"]).pin_memory(),
+                d=torch.as_tensor(d["dirs"]).pin_memory(), r=d["rands"].cpu().pin_memory())
+    out_i = torch.empty((1, R, S), dtype=torch.int32).pin_memory()
+    out_z = torch.empty((1, R, S), dtype=torch.float32).pin_memory()
+    h2d = sum(v.numel() * 4 for v in host["vols"]) + host["o"].numel() * 4 * 2 + host["r"].numel() * 4
+    d2h = 2 * out_i.numel() * 4
+
+    def e2e_step():
+        for a, b in zip(d["pristine"], host["vols"]):
+            a.copy_(b, non_blocking=True)
+        d["o"].copy_(host["o"], non_blocking=True)
+        d["d"].copy_(host["d"], non_blocking=True)
+        d["rands"].copy_(host["r"], non_blocking=True)
+        _, a_i, a_z = octree_step(o, d, cfg)
+        out_i.copy_(a_i, non_blocking=True)
+        out_z.copy_(a_z, non_blocking=True)
+    e2e_step()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_e2e = e0.elapsed_time(e1) / args.steps
+    n_scan = 3
+    launches = (2 + n_scan + (L - 1) * (2 + n_scan)) + 3 + 1  # build, traversal + two row pads, sampler
+    out = dict(metric=f"rays/s multi-level traversal + fine sampling ({cfg['D']}^3, rate {cfg['rate']}, {L} levels, "
+                      f"S={S})",
+               value=R / (ms / 1000.0), unit="rays/s", n_gpus=1, steps=args.steps, warmup=warm, ms_per_step=ms,
+               higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32 / i32",
+               data="synthetic (seeded capsule/ellipsoid scene)",
+               config=dict(workload=f"{cfg['views']} views {cfg['res']}^2 fused into {cfg['D']}^3, {L}-level rate-"
+                                    f"{cfg['rate']} tree built every step, {cfg['target']}^2 target ({R} rays) "
+                                    f"traversed from start level {cfg['start']} (coarse rows {Wc}, fine rows {Wf}), "
+                                    f"fine sampling S={S}", l2="padded rows > L2 (2.2 GB)"),
+               stages_ms=stages, coarse_per_ray=n_coarse / R, fine_per_ray=n_fine / R,
+               nodes_per_level=counts.tolist(), max_coarse=int(st[1]), max_fine=int(st[2]),
+               roofline=dict(bound="hbm", kernel=dom, achieved=rl[dom], peak=pk["hbm_gbs"], unit="GB/s",
+                             frac=rl[dom] / pk["hbm_gbs"], traffic=None, peak_kind=pk_kind,
+                             algorithmic_bytes=ab[dom]),
+               rooflines={k: dict(achieved=v, frac=v / pk["hbm_gbs"], algorithmic_bytes=ab[k]) for k, v in rl.items()},
+               e2e=dict(value=R / (ms_e2e / 1000.0), unit="rays/s", h2d_bytes_per_step=h2d, d2h_bytes_per_step=d2h),
+               gpu_launches=launches * args.steps, clocks=clk.summary())
+    if not args.no_cpu_baseline:
+        occ0 = d["pristine"][0].cpu().numpy()
+        out["cpu_baseline"] = cpu_baseline_octree(cfg, occ0, d["ori"], d["dirs"],
+                                                  d["sc"]["voxel_size"].reshape(-1).astype(np.float32),
+                                                  d["sc"]["vol_bbox"].astype(np.float32), reps=5)
+    if not args.no_parity:
+        out["parity"] = parity_octree(o, d, cfg, rows, si, sz)
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -1280,6 +1540,8 @@ def main():
         return run_project(args)
     if args.workload == "diff":
         return run_diff(args)
+    if args.workload == "octree":
+        return run_octree(args)
     return run_plain(args)
 
 

@@ -176,6 +176,120 @@ int sg_tree_build_static(SgTree *tree, int *occ_top, int *occ_bot,
 int sg_tree_nodes(const SgTree *tree, int n_nodes, float *out,
                   sg_stream_t stream);
 
+/* ---- multi-level tree (octree_level >= 2) ------------------------------ */
+
+#define SG_MAX_LEVELS 12
+
+/* Multi-level tree kept in device memory, one node table per level.
+ * Replaces MultiLayerOctree with num_levels = L (octree.h:155-302) as built
+ * by gen_root_octree_nodes + gen_higher_octree_nodes (octree_kernel.cu:
+ * 18-99, 126-239, 654-697).  Level 0 is the finest grid (edge dim[0]),
+ * level l has edge dim[l] = dim[0] / rate^l, level L-1 is the top.  Node ids
+ * keep the reference's id space: node k of level l is base[l] + k, with
+ * base[l] = octree_nodes_index[l] (the sum of the lower levels' occupied
+ * counts).  Within a level, nodes are ordered deterministically: top nodes
+ * by (frame, linear index); every other level's nodes by parent, and the
+ * children of one parent in ascending (x, y, z) order -- the order in which
+ * the reference inserts them (octree_kernel.cu:66-93) -- so a node's
+ * children are the contiguous run child_base[l][k] .. + nchild[l][k] of
+ * level l-1.  The reference's ids come from atomicAdd queues instead. */
+typedef struct SgOctree {
+  int B, L, rate;
+  int dim[SG_MAX_LEVELS];        /* grid edge of each level                  */
+  int base[SG_MAX_LEVELS];       /* node id of each level's node 0           */
+  int cap[SG_MAX_LEVELS];        /* node capacity of each level's tables     */
+  int *vol[SG_MAX_LEVELS];       /* [B*dim^3] occupancy (> -1 occupied);      */
+                                 /* the build writes node ids into it         */
+  int *key[SG_MAX_LEVELS];       /* [cap] frame * dim^3 + linear index       */
+  int *parent[SG_MAX_LEVELS];    /* [cap] parent node id; -1 at the top      */
+  int *child_base[SG_MAX_LEVELS];/* [cap] first child (index into level l-1) */
+  int *nchild[SG_MAX_LEVELS];    /* [cap] number of children (levels >= 1)   */
+  int *counts;                   /* [L] nodes built per level                */
+  const float *voxel_size;       /* [B] finest voxel edge                    */
+  const float *vol_bbox;         /* [B,3,2]                                   */
+} SgOctree;
+
+/* Device status of the multi-level tree calls (zeroed by the caller). */
+typedef struct SgOctreeStatus {
+  int flags;        /* SG_FLAG_HIT_OVERFLOW, SG_FLAG_TREE_CAPACITY            */
+  int max_coarse;   /* largest coarse-row count (num_max_intersected_voxels)  */
+  int max_fine;     /* largest fine-row count (num_max_intersected_voxels_fine)*/
+  int reserved;
+} SgOctreeStatus;
+
+/* Bytes of device scratch sg_octree_build needs. */
+size_t sg_octree_scratch_bytes(const SgOctree *tree);
+
+/* Build every level's node table from the occupancy volumes (dense grids,
+ * value > -1 = occupied, as integrate and build_multi_res_volumes leave
+ * them).  Top voxels without an occupied neighbour in their 3x3x3
+ * neighbourhood are not nodes (if_single_occ_in_neighbors,
+ * octree_kernel.cu:101-122), and neither is anything under them.  Every
+ * built node's entry in its level's volume is overwritten with its node id;
+ * other entries are left as they are (as the reference does).  rate must be
+ * 2, 4 or 8.  A level whose nodes exceed its capacity gets
+ * SG_FLAG_TREE_CAPACITY (counts[] then hold the required numbers).
+ * Runs on the stream without a host synchronisation. */
+int sg_octree_build(SgOctree *tree, void *scratch, size_t scratch_bytes,
+                    SgOctreeStatus *status, sg_stream_t stream);
+
+/* Node table [n_nodes, 6] = (centre x, y, z, edge, valid, frame) per node
+ * id of the multi-level tree (output_all_nodes_tensor,
+ * octree_kernel.cu:309-328, 699-717).  Ids past a level's built nodes are
+ * the reference's invalid placeholder nodes (valid 0). */
+int sg_octree_nodes(const SgOctree *tree, int n_nodes, float *out,
+                    sg_stream_t stream);
+
+/* Coarse DDA plus depth-first descent.  Replaces
+ * MultiLayerOctree::octree_traversal (intersection_kernel.cu:441-643,
+ * 722-826): a DDA over the grid of level s = L-1-start_level records the
+ * nodes of s the ray crosses (coarse rows, idx_c/t0_c/t1_c [B,N,Wc],
+ * ray_voxel_traversal with only_voxel_traversal = false, :286-439 and
+ * RayVoxelIntersectionNodeList :72-126; th_early_stop and opt_num as
+ * there); each coarse node is then descended depth first, children last to
+ * first, recording every descendant the ray hits (fine rows,
+ * idx/t0/t1 [B,N,Wf]): a descendant whose (t0, t1) equals, bit for bit, an
+ * entry already recorded under the same coarse node replaces that entry's
+ * node when it is smaller, else is not recorded; the descent enters only
+ * hit nodes.  valid_len [B,N] = sum over the fine entries of
+ * (t1 - t0) * (edge of s / edge of the entry's node).  Rows are padded with
+ * -1.  The reference runs one thread per (ray, coarse hit) and appends with
+ * atomicAdd, so its fine rows hold the same entries in an order that
+ * changes run to run, and its descent keeps an 8-entry stack and an
+ * 8-entry list per coarse node (N_STACK_MAX_NODES, :15), which overflow for
+ * rate 4 or a descent of more than one level; here fine rows are in coarse
+ * order, each coarse node's entries in descent order, and neither limit
+ * exists.  Rows wider than Wc / Wf keep their first entries and set
+ * SG_FLAG_HIT_OVERFLOW; status->max_coarse / max_fine receive the largest
+ * counts.  cnt_c / cnt_f [B,N] (nullable) receive the row counts. */
+int sg_octree_traversal(const SgOctree *tree, const float *ori,
+                        const float *dir, int N, int start_level, int Wc,
+                        int Wf, int th_early_stop, int opt_num, int *idx_c,
+                        float *t0_c, float *t1_c, int *cnt_c, int *idx,
+                        float *t0, float *t1, int *cnt, float *valid_len,
+                        SgOctreeStatus *status, sg_stream_t stream);
+
+/* Adaptive sampling over fine rows.  Replaces
+ * MultiLayerOctree::ray_voxels_points_sampling -> ray_voxels_sampling_kernel
+ * + ray_voxels_further_sampling_kernel (sampling_kernel.cu:911-1068,
+ * 1178-1248).  Each entry (rows are read up to their first -1) takes
+ * max(1, (int)((t1 - t0) * r * S / valid_len)) samples, r = edge of the
+ * level-(L-1-start_level) node (finest edge x 2^(L-1-start_level), as the
+ * reference computes it) / the entry's node edge, placed at
+ * t0 + off*(j+1) - off/2 + off*rand, off = (t1 - t0)/(n+1), until S are
+ * placed; the slots left are then filled the same way in the entry with the
+ * smallest node, the nearest midpoint among those (the first on a tie).
+ * Slots take rands in entry order; the reference hands slots out with
+ * atomicAdd across its entries, so its slot order (and, with rands that
+ * differ, which jitter each sample takes) changes run to run.
+ * rands / sampled_idx / sampled_z [B,N,S]; entries without a sample
+ * are -1. */
+int sg_sample_fine(const SgOctree *tree, const int *hit_idx,
+                   const float *hit_t0, const float *hit_t1, int N, int W,
+                   const float *valid_len, const float *rands, int S,
+                   int start_level, int *sampled_idx, float *sampled_z,
+                   sg_stream_t stream);
+
 /* ---- ray / tree intersection ---------------------------------------- */
 
 /* Per-ray DDA over the top grid with child slab tests.  Replaces
@@ -624,6 +738,30 @@ int sg_sort_pairs(const uint32_t *keys, const int *count, long long capacity,
                   int key_bits, uint32_t *keys_out, uint32_t *vals_out,
                   uint32_t *keys_tmp, uint32_t *vals_tmp, void *scratch,
                   size_t scratch_bytes, sg_stream_t stream);
+
+/* ---- FastNerf occupancy network (tensor cores) ------------------------- */
+
+/* Number of float16 parameters of the density network: the feature MLP
+ * 18->64->64->64->64 ([0, 13696)), the sigma MLP 64->64->64->1
+ * ([13696, 22081)) and the geometry MLP 18->16->8 ([22081, 22521)), each
+ * layer its weights [out][in] then its bias (infer_mlp.cu:120-240). */
+size_t sg_nerf_param_count(void);
+
+/* FastNerf's occupancy network on the tcgen05 tensor cores.  Replaces
+ * infer_density_mlp (c_lib/FastNerf/src/infer_mlp.cu:583-636) with
+ * density_feat_kernel (:120-199) and density_sigma_kernel (:202-240) and the
+ * torch.mean over the views between them.  params: float16 bits
+ * [sg_nerf_param_count()]; points_z / points_tpsdf [B,V,N], feats_geo
+ * [B,V,N,16] float32 (16-byte aligned); density [B,N] out; geo_feats
+ * [B,V,N,8] out (nullable; the reference computes and drops them).  V <= 128.
+ * Layer outputs are rounded to float16 where the reference rounds them;
+ * products within a layer are summed in float32 (the reference rounds every
+ * partial sum to float16).  error (nullable, a device int) is set to 1 if a
+ * tensor-core wait times out. */
+int sg_nerf_density(const uint16_t *params, const float *points_z,
+                    const float *points_tpsdf, const float *feats_geo, int B,
+                    int N, int V, float *density, float *geo_feats,
+                    int *error, sg_stream_t stream);
 
 #ifdef __cplusplus
 }

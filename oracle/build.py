@@ -1,6 +1,6 @@
 """Build recipe for the oracle (test infrastructure).
 
-``build_oracle()`` compiles ``sailor_oracle.c`` with gcc into
+``build_oracle()`` compiles ``sailor_oracle.c`` and ``octree_oracle.c`` with gcc into
 ``oracle/liboracle.so``; it adds no floating-point contraction of its own
 (``-ffp-contract=off``) so that the explicit ``fmaf`` calls in the source are
 the only fused operations, on x86-64 and aarch64 alike.
@@ -25,12 +25,12 @@ REF_KERNELS = ("fusion_kernel", "octree_kernel", "intersection_kernel",
 
 
 def build_oracle(force=False):
-    src = os.path.join(HERE, "sailor_oracle.c")
+    srcs = [os.path.join(HERE, n) for n in ("sailor_oracle.c", "octree_oracle.c")]
     if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= os.path.getmtime(src)):
+            and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in srcs)):
         return LIB
     cmd = ["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-           "-o", LIB + ".tmp", src, "-lm"]
+           "-o", LIB + ".tmp"] + srcs + ["-lm"]
     subprocess.check_call(cmd)
     os.replace(LIB + ".tmp", LIB)
     return LIB

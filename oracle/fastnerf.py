@@ -148,3 +148,62 @@ def composite_occ(sorted_z, occ, feats, t_thres=1e-4):
     from . import oracle as orc
     of, od, _, _, _ = orc.composite_fwd(sorted_z, None, occ, feats, t_thres, occ_mode=True)
     return of, od
+
+
+# --------------------------------------------------------------------------
+# float32-accumulating and float64 evaluations of the same network (the
+# tolerance references of the tensor-core kernel)
+# --------------------------------------------------------------------------
+def _fc_acc(x16, params, off, n_in, n_out, dtype):
+    W = np.asarray(params[off:off + n_in * n_out], F16).reshape(n_out, n_in).astype(F64)
+    b = np.asarray(params[off + n_in * n_out:off + n_in * n_out + n_out], F16).astype(F64)
+    acc = x16.astype(F64) @ W.T
+    if dtype == F32:  # products summed in float32 precision, then the bias in float32
+        return (acc.astype(F32) + b.astype(F32)).astype(F32)
+    return acc + b
+
+
+def _mlp_acc(x, params, off, layers, last_relu, dtype):
+    for k, (n_in, n_out) in enumerate(layers):
+        y = _fc_acc(x, params, off, n_in, n_out, dtype)
+        off += n_in * n_out + n_out
+        if dtype == F32:
+            y = y.astype(F16)  # layer outputs rounded to float16 as the reference rounds them
+        if last_relu or k + 1 < len(layers):
+            y = np.maximum(y, 0).astype(y.dtype)
+        x = y
+    return x
+
+
+def infer_density_acc(points_z, points_tpsdf, feats_geo, params, batch_size, num_points, num_views, dtype=F32):
+    """infer_density with each layer's products summed at once instead of
+    through a float16 __hfma chain.  dtype float32: layer sums in float32,
+    layer outputs rounded to float16 where the reference rounds them (the
+    arithmetic of a float32-accumulating implementation, up to the order of
+    its float32 additions); float64: no rounding after the float16 inputs
+    and weights (the network's exact value).  Returns (densities [B, 1, N],
+    geometry features [B, V, N, 8]) as float64."""
+    B, V, N = batch_size, num_views, num_points
+    params = np.asarray(params, F16)
+    x = np.concatenate([np.asarray(points_z, F32).reshape(-1, 1), np.asarray(points_tpsdf, F32).reshape(-1, 1),
+                        np.asarray(feats_geo, F32).reshape(-1, 16)], axis=1).astype(F16)
+    dens = _mlp_acc(x, params, 0, FEAT_LAYERS, True, dtype)
+    geo = _mlp_acc(x, params, GEO_OFFSET, GEO_LAYERS, True, dtype)
+    pv = dens.astype(F64 if dtype == F64 else F32).reshape(B, V, N, 64)
+    if dtype == F32:
+        acc = np.zeros((B, N, 64), F32)
+        for v in range(V):
+            acc = (acc + pv[:, v]).astype(F32)
+        mean = (acc * F32(1.0 / V)).astype(F32).reshape(-1, 64).astype(F16)
+    else:
+        mean = pv.mean(1).reshape(-1, 64)
+    h = _mlp_acc(mean, params, SIGMA_OFFSET, SIGMA_LAYERS[:2], True, dtype)
+    w3 = params[SIGMA_OFFSET + 8320:SIGMA_OFFSET + 8384].astype(F64)
+    b3 = F64(params[SIGMA_OFFSET + 8384])
+    pre = h.astype(F64) @ w3 + b3
+    if dtype == F32:
+        pre = pre.astype(F32).astype(F16).astype(F64)
+        d = (F32(1) / (F32(1) + np.exp(-pre).astype(F32))).astype(F16).astype(F64)
+    else:
+        d = 1.0 / (1.0 + np.exp(-pre))
+    return d.reshape(B, 1, N), geo.astype(F64).reshape(B, V, N, 8)

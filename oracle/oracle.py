@@ -10,7 +10,7 @@ import numpy as np
 
 from . import build as _build
 
-FLAG_TIE, FLAG_ALIAS, FLAG_OVERFLOW = 1, 2, 4
+FLAG_TIE, FLAG_ALIAS, FLAG_OVERFLOW, FLAG_TRUNC = 1, 2, 4, 8
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
@@ -57,6 +57,14 @@ def lib():
         L.orc_node_geometry.argtypes = [f, i, _f32p, _i32p, _f32p, _f32p]
         L.orc_project_xyz.argtypes = [i, i, i, i, _f32p, _f32p, _f32p, _i32p, _f32p, _f32p, i, i, _vp, i,
                                       _f32p, _f32p]
+        L.orc_octree_build.argtypes = [i, i, i, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p]
+        L.orc_octree_build.restype = i
+        L.orc_octree_traversal.argtypes = ([i, i, i, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p,
+                                            _f32p, _f32p, i, _f32p, _f32p, i, i, i, i, i]
+                                           + [_i32p, _f32p, _f32p, _i32p] * 2 + [_f32p, _i32p, _i32p])
+        L.orc_octree_traversal.restype = i
+        L.orc_sample_fine.argtypes = [i, i, i, _i32p, _i32p, _i32p, i, i, i, _i32p, _f32p, _f32p, _f32p,
+                                      _f32p, i, _f32p, _i32p, _f32p, _i32p]
         L.orc_num_threads.restype = i
         L.orc_set_threads.argtypes = [i]
         _lib = L
@@ -573,3 +581,114 @@ def trilinear_cells(pts, bbox_min, voxel_size, batch=None):
         w[:, cr] = ((f[:, 0] if dx else 1 - f[:, 0]) * (f[:, 1] if dy else 1 - f[:, 1])
                     * (f[:, 2] if dz else 1 - f[:, 2]))
     return i0.astype(np.int64), w
+
+
+# --------------------------------------------------------------------------
+# multi-level tree, depth-first traversal, fine sampler (octree_oracle.c)
+# --------------------------------------------------------------------------
+def merge_levels(occ0, counts0, rate, L):
+    """build_multi_res_volumes (octree_kernel.cu:367-411) for L levels:
+    volumes [level 0 (given), 1, .., L-1] and occupied counts [B, 1] each."""
+    vols, cnts = [_i(occ0).copy()], [np.asarray(counts0, np.int32).reshape(-1, 1)]
+    for _ in range(L - 1):
+        c, n = merge(vols[-1], rate)
+        vols.append(c)
+        cnts.append(n)
+    return vols, cnts
+
+
+def build_octree(vols, rate, caps=None):
+    """Multi-level tree over volumes [level 0 .. L-1] (rewrites copies).
+    Node ids: base[l] = sum of the lower levels' occupied voxel counts
+    (octree_nodes_index), capacities = the levels' occupied counts."""
+    L = len(vols)
+    B = vols[0].shape[0]
+    dims = np.array([v.shape[1] for v in vols], np.int32)
+    occ = [int((np.asarray(v) > -1).sum()) for v in vols]
+    cap = np.array(occ if caps is None else caps, np.int32)
+    base = np.concatenate([[0], np.cumsum(occ)[:-1]]).astype(np.int32)
+    vol = np.concatenate([_i(v).reshape(-1) for v in vols]).astype(np.int32)
+    n = max(int(cap.sum()), 1)
+    key = np.full(n, -1, np.int32)
+    parent = np.full(n, -1, np.int32)
+    cb = np.zeros(n, np.int32)
+    nc = np.zeros(n, np.int32)
+    counts = np.zeros(L, np.int32)
+    rc = lib().orc_octree_build(B, L, int(rate), dims, vol, base, cap, key, parent, cb, nc, counts)
+    if rc != 0:
+        raise RuntimeError("oracle octree build: capacity exceeded")
+    out_vols, off = [], 0
+    for v in vols:
+        m = v.size
+        out_vols.append(vol[off:off + m].reshape(v.shape).copy())
+        off += m
+    return dict(B=B, L=L, rate=int(rate), dims=dims, base=base, cap=cap, counts=counts, vols=out_vols,
+                vol=vol, key=key, parent=parent, child_base=cb, nchild=nc, n_nodes=int(sum(occ)))
+
+
+def octree_level_of(tree, ids):
+    ids = np.asarray(ids)
+    lv = np.full(ids.shape, -1, np.int64)
+    for l in range(tree["L"]):
+        m = (ids >= tree["base"][l]) & (ids < tree["base"][l] + tree["cap"][l])
+        lv[m] = l
+    return lv
+
+
+def octree_node_keys(tree, ids):
+    """Canonical (level, b, x, y, z) per node id of the multi-level tree."""
+    ids = np.asarray(ids)
+    out = np.full(ids.shape + (5,), -1, np.int64)
+    coff = np.concatenate([[0], np.cumsum(tree["cap"])[:-1]])
+    lv = octree_level_of(tree, ids)
+    for l in range(tree["L"]):
+        m = lv == l
+        if not m.any():
+            continue
+        D = int(tree["dims"][l])
+        key = tree["key"][coff[l] + ids[m] - tree["base"][l]].astype(np.int64)
+        out[m, 0] = l
+        out[m, 1] = key // D ** 3
+        r = key % D ** 3
+        out[m, 2], out[m, 3], out[m, 4] = r // (D * D), (r // D) % D, r % D
+    return out
+
+
+def octree_traversal(tree, ori, dirs, voxel_size, vol_bbox, start_level=0, Wc=256, Wf=1024, th_early_stop=-1,
+                     opt_num=-1):
+    B, N = ori.shape[0], ori.shape[1]
+    R = B * N
+    out = dict(idx_c=np.full((B, N, Wc), -1, np.int32), t0_c=np.full((B, N, Wc), -1, np.float32),
+               t1_c=np.full((B, N, Wc), -1, np.float32), cnt_c=np.zeros((B, N), np.int32),
+               idx=np.full((B, N, Wf), -1, np.int32), t0=np.full((B, N, Wf), -1, np.float32),
+               t1=np.full((B, N, Wf), -1, np.float32), cnt=np.zeros((B, N), np.int32),
+               valid_len=np.zeros((B, N), np.float32), flags=np.zeros((B, N), np.int32),
+               need=np.zeros((B, N), np.int32))
+    mx = lib().orc_octree_traversal(
+        tree["B"], tree["L"], tree["rate"], tree["dims"], tree["vol"], tree["base"], tree["cap"], tree["counts"],
+        tree["key"], tree["child_base"], tree["nchild"], _f(voxel_size).reshape(-1), _f(vol_bbox).reshape(-1), N,
+        _f(ori).reshape(-1), _f(dirs).reshape(-1), int(start_level), Wc, Wf, int(th_early_stop), int(opt_num),
+        out["idx_c"].reshape(-1), out["t0_c"].reshape(-1), out["t1_c"].reshape(-1), out["cnt_c"].reshape(-1),
+        out["idx"].reshape(-1), out["t0"].reshape(-1), out["t1"].reshape(-1), out["cnt"].reshape(-1),
+        out["valid_len"].reshape(-1), out["flags"].reshape(-1), out["need"].reshape(-1))
+    del R
+    out["max_fine"] = int(mx)
+    out["max_coarse"] = int(out["cnt_c"].max()) if out["cnt_c"].size else 0
+    out["valid_len"] = out["valid_len"][..., None]
+    return out
+
+
+def sample_fine(tree, idx, t0, t1, valid_len, rands, voxel_size, S, start_level=0):
+    """ray_voxels_points_sampling over fine rows: (sampled_idx, sampled_z,
+    flags) with FLAG_TIE near count / midpoint ties and FLAG_TRUNC where the
+    entries ask for more than S samples."""
+    idx, t0, t1 = _i(idx), _f(t0), _f(t1)
+    B, N, W = idx.shape
+    sidx = np.full((B, N, S), -1, np.int32)
+    sz = np.full((B, N, S), -1, np.float32)
+    flags = np.zeros((B, N), np.int32)
+    lib().orc_sample_fine(tree["B"], tree["L"], tree["rate"], tree["dims"], tree["base"], tree["cap"], N, W, S,
+                          idx.reshape(-1), t0.reshape(-1), t1.reshape(-1), _f(valid_len).reshape(-1),
+                          _f(rands).reshape(-1), int(start_level), _f(voxel_size).reshape(-1), sidx.reshape(-1),
+                          sz.reshape(-1), flags.reshape(-1))
+    return sidx, sz, flags

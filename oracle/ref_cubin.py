@@ -8,7 +8,10 @@ as device memory:
 
   integrate               fusion_kernel.cu:600-727
   build_multi_res_volumes octree_kernel.cu:367-411
-  init_octree/build_octree octree_kernel.cu:569-697 (two levels)
+  init_octree/build_octree octree_kernel.cu:569-697 (two levels; OctreeML:
+                          any depth, gen_root + gen_higher_octree_nodes)
+  octree_traversal        intersection_kernel.cu:441-643, 722-826 (OctreeML)
+  ray_voxels_points_sampling sampling_kernel.cu:911-1068, 1178-1248 (OctreeML)
   voxel_traversal         intersection_kernel.cu:828-895
   ray_voxels_points_sampling_coarse sampling_kernel.cu:1251-1304
   sort_samplings          sampling_kernel.cu:1308-1329 (torch.sort)
@@ -24,7 +27,11 @@ local id for occupied bricks that were not made nodes (no occupied
 neighbour), and writes hit lists without a bound.  ``voxel_traversal`` below
 refuses inputs where such a read could leave the node array, and the caller
 sizes the hit rows to the largest count the grid allows, so every access of
-the reference kernels stays in bounds.
+the reference kernels stays in bounds.  ``OctreeML`` runs only on trees
+where every occupied voxel became a node (no such reads), and its caller
+runs the descent only where the oracle shows that every coarse node's
+stack and list fit the reference's 8 entries (N_STACK_MAX_NODES), with
+rows as wide as the DDA's step bound allows.
 """
 import ctypes as C
 import os
@@ -53,6 +60,10 @@ _NAMES = {
     "rays_inverse": ("sampling_kernel", "14inverse_mat3x3IfE"),
     "rays": ("sampling_kernel", "23rays_calculating_kernelIfE"),
     "project": ("sampling_kernel", "11project_xyz"),
+    "gen_higher": ("octree_kernel", "23gen_higher_octree_nodes"),
+    "octree_traversal": ("intersection_kernel", "20ray_octree_traversal"),
+    "sampling_fine": ("sampling_kernel", "26ray_voxels_sampling_kernel"),
+    "sampling_further": ("sampling_kernel", "34ray_voxels_further_sampling_kernel"),
 }
 
 
@@ -288,6 +299,137 @@ class Octree:
         r = _dev(rands, torch.float32)
         d.launch("sampling", B * N, [self.nodes, idx, t0, t1, r, vl, si, sd, i32(B), i32(N), i32(W), i32(S),
                                      i32(self.max_hits), i32(start_level), i32(2), self.voxel_size])
+        torch.cuda.synchronize()
+        return si, sd
+
+
+def merge_levels(occ0, rate, L):
+    """build_multi_res_volumes for L levels (octree_kernel.cu:367-411):
+    merge_non_empty_nodes level by level."""
+    d = driver()
+    B = occ0.shape[0]
+    vols, cnts = [occ0], []
+    for _ in range(L - 1):
+        Dn = vols[-1].shape[1]
+        Dc = Dn // rate
+        occ = torch.full((B, Dc, Dc, Dc), -1, dtype=torch.int32, device="cuda")
+        cnt = torch.zeros((B, 1), dtype=torch.int32, device="cuda")
+        d.launch("merge", B * Dc ** 3, [occ, cnt, vols[-1], i32(Dc), i32(Dn), i32(B)])
+        vols.append(occ)
+        cnts.append(cnt)
+    torch.cuda.synchronize()
+    return vols, cnts
+
+
+class OctreeML:
+    """MultiLayerOctree of any depth (octree_kernel.cu:654-697): node slots
+    of level l at octree_nodes_index[l] = the lower levels' occupied counts;
+    gen_root_octree_nodes makes the top two levels, gen_higher_octree_nodes
+    each level below.  vols [level 0 .. L-1] are rewritten to node ids."""
+
+    def __init__(self, vols, voxel_size, vol_bbox, rate):
+        d = driver()
+        assert rate ** 3 <= 64, "reference node layout supports rate <= 4 only"
+        self.L = L = len(vols)
+        self.B = vols[0].shape[0]
+        self.dims = [int(v.shape[1]) for v in vols]
+        self.rate = rate
+        self.totals = [int((v > -1).sum()) for v in vols]
+        self.index = [sum(self.totals[:l]) for l in range(L)]
+        self.n_nodes = sum(self.totals)
+        self.vols = vols
+        self.voxel_size, self.vol_bbox = voxel_size, vol_bbox
+        self.nodes = torch.zeros(max(self.n_nodes, 1) * OCTREE_BYTES, dtype=torch.uint8, device="cuda")
+        self.queue = torch.zeros(L, dtype=torch.int32, device="cuda")
+        base = self.nodes.data_ptr()
+        T = L - 1
+        d.launch("gen_root", self.B * self.dims[T] ** 3,
+                 [vols[T], vols[T - 1], C.c_void_p(base + self.index[T] * OCTREE_BYTES),
+                  C.c_void_p(base + self.index[T - 1] * OCTREE_BYTES), i32(self.index[T]), i32(self.index[T - 1]),
+                  self.queue, voxel_size, vol_bbox, i32(self.dims[T]), i32(self.dims[0]), i32(rate), i32(self.B)])
+        for k in range(L - 2, 0, -1):
+            d.launch("gen_higher", self.totals[k],
+                     [vols[k - 1], C.c_void_p(base + self.index[k] * OCTREE_BYTES),
+                      C.c_void_p(base + self.index[k - 1] * OCTREE_BYTES), i32(self.index[k - 1]),
+                      i32(self.totals[k]), vol_bbox, C.c_void_p(self.queue.data_ptr() + 4 * (L - k)), i32(rate)])
+        torch.cuda.synchronize()
+        # queue_control[i] counts the nodes of level L-1-i
+        self.built = self.queue.cpu().numpy()[::-1].copy()
+        self.complete = bool(np.array_equal(self.built, np.array(self.totals)))
+
+    def node_table(self):
+        raw = self.nodes.cpu().numpy().reshape(-1, OCTREE_BYTES)
+
+        def col(off, dt, n=1):
+            return np.frombuffer(raw[:, off:off + 4 * n].tobytes(), dtype=dt).reshape(-1, n)
+        return dict(valid=np.frombuffer(raw[:, 0:2].tobytes(), np.uint16).copy(), vol_dim=col(24, np.int32)[:, 0],
+                    batch=col(28, np.int32)[:, 0], voxel_size=col(32, np.float32)[:, 0],
+                    xyz=col(36, np.int32, 3), nleaves=col(16, np.int32)[:, 0])
+
+    def canonical(self, ids, table=None):
+        """(level, b, x, y, z) per node id; -1 rows for -1 ids."""
+        table = self.node_table() if table is None else table
+        ids = np.asarray(ids)
+        out = np.full(ids.shape + (5,), -1, np.int32)
+        m = ids >= 0
+        g = ids[m]
+        lvl = np.full(g.shape, -2, np.int32)
+        for l, D in enumerate(self.dims):
+            lvl[table["vol_dim"][g] == D] = l
+        lvl[table["valid"][g] != 1] = -2
+        out[m, 0] = lvl
+        out[m, 1] = table["batch"][g]
+        out[m, 2:] = table["xyz"][g]
+        return out
+
+    def octree_traversal(self, ori, dirs, start_level, Wc, Wf):
+        """octree_traversal (intersection_kernel.cu:722-826) with
+        th_early_stop = opt_num = -1."""
+        assert self.complete, "every occupied voxel must be a node"
+        d = driver()
+        s = self.L - 1 - start_level
+        assert Wc >= 4 * self.dims[s] and Wf >= 8 * Wc, "rows narrower than the reference's bounds"
+        B, N = ori.shape[0], ori.shape[1]
+        o, dr = _dev(ori, torch.float32), _dev(dirs, torch.float32)
+        vl = torch.zeros((B, N, 1), device="cuda")
+        qc = torch.zeros((B, N, 1), dtype=torch.int32, device="cuda")
+        idx_c = torch.full((B, N, Wc), -1, dtype=torch.int32, device="cuda")
+        t0c = torch.full((B, N, Wc), -1.0, device="cuda")
+        t1c = torch.full((B, N, Wc), -1.0, device="cuda")
+        q = torch.zeros((B, N, 1), dtype=torch.int32, device="cuda")
+        idx = torch.full((B, N, Wf), -1, dtype=torch.int32, device="cuda")
+        t0 = torch.full((B, N, Wf), -1.0, device="cuda")
+        t1 = torch.full((B, N, Wf), -1.0, device="cuda")
+        mc = torch.zeros(1, dtype=torch.int32, device="cuda")
+        mf = torch.zeros(1, dtype=torch.int32, device="cuda")
+        d.launch("traversal", B * N, [self.vols[s], self.nodes, i32(self.index[s]), o, dr, idx_c, t0c, t1c, qc, vl,
+                                      self.vol_bbox, self.voxel_size, i32(N), i32(Wc), i32(self.totals[s]),
+                                      i32(self.dims[0]), i32(self.dims[s]), i32(B), mc, i32(-1), i32(-1), cb(False),
+                                      cb(False)])
+        torch.cuda.synchronize()
+        ncoarse = int(mc.item())
+        if ncoarse > 0:
+            d.launch("octree_traversal", B * N * ncoarse,
+                     [self.nodes, o, dr, idx_c, t0c, t1c, idx, t0, t1, q, vl, i32(N), i32(Wc), i32(Wf), mf,
+                      i32(ncoarse), i32(B), i32(self.rate)])
+            torch.cuda.synchronize()
+        self.max_fine = int(mf.item())
+        return dict(idx_c=idx_c, t0_c=t0c, t1_c=t1c, idx=idx, t0=t0, t1=t1, valid_len=vl, cnt=q)
+
+    def sample_fine(self, idx, t0, t1, vl, rands, S, start_level):
+        """ray_voxels_points_sampling (sampling_kernel.cu:1178-1248)."""
+        d = driver()
+        B, N, W = idx.shape
+        si = torch.full((B, N, S), -1, dtype=torch.int32, device="cuda")
+        sd = torch.full((B, N, S), -1.0, device="cuda")
+        sq = torch.zeros((B, N, 1), dtype=torch.int32, device="cuda")
+        if self.max_fine == 0:
+            return si, sd
+        r = _dev(rands, torch.float32)
+        d.launch("sampling_fine", B * N * self.max_fine,
+                 [self.nodes, idx, t0, t1, r, vl, si, sq, sd, i32(B), i32(N), i32(W), i32(S), i32(self.max_fine),
+                  i32(start_level), i32(self.L), self.voxel_size])
+        d.launch("sampling_further", B * N, [self.nodes, idx, t0, t1, r, si, sq, sd, i32(B), i32(N), i32(W), i32(S)])
         torch.cuda.synchronize()
         return si, sd
 

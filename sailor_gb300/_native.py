@@ -26,7 +26,8 @@ EXPORTS = (
     "sg_render_segments_bwd", "sg_render_segments_train",
     "sg_camera_params", "sg_rays_from_cameras", "sg_segment_rays", "sg_zero_near_nodes",
     "sg_project_sampled_xyz", "sg_project_gather", "sg_train_det_workspace_bytes", "sg_render_segments_train_det",
-    "sg_sort_pairs_scratch_bytes", "sg_sort_pairs",
+    "sg_sort_pairs_scratch_bytes", "sg_sort_pairs", "sg_octree_scratch_bytes", "sg_octree_build",
+    "sg_octree_nodes", "sg_octree_traversal", "sg_sample_fine", "sg_nerf_param_count", "sg_nerf_density",
 )
 
 
@@ -35,6 +36,17 @@ class SgTree(C.Structure):
                 ("base_top", C.c_int), ("base_bot", C.c_int), ("cap_top", C.c_int), ("cap_bot", C.c_int),
                 ("brick_node", C.c_void_p), ("brick_mask", C.c_void_p), ("top_key", C.c_void_p),
                 ("top_child_base", C.c_void_p), ("bot_key", C.c_void_p), ("bot_parent", C.c_void_p),
+                ("counts", C.c_void_p), ("voxel_size", C.c_void_p), ("vol_bbox", C.c_void_p)]
+
+
+SG_MAX_LEVELS = 12
+_LV = C.c_int * SG_MAX_LEVELS
+_LP = C.c_void_p * SG_MAX_LEVELS
+
+
+class SgOctree(C.Structure):
+    _fields_ = [("B", C.c_int), ("L", C.c_int), ("rate", C.c_int), ("dim", _LV), ("base", _LV), ("cap", _LV),
+                ("vol", _LP), ("key", _LP), ("parent", _LP), ("child_base", _LP), ("nchild", _LP),
                 ("counts", C.c_void_p), ("voxel_size", C.c_void_p), ("vol_bbox", C.c_void_p)]
 
 
@@ -126,6 +138,16 @@ def _load():
     lib.sg_project_gather.argtypes = [C.POINTER(SgProjGather), p]
     lib.sg_tune_set.argtypes = [i, i]
     lib.sg_tune_get.argtypes = [i]
+    O = C.POINTER(SgOctree)
+    lib.sg_octree_scratch_bytes.argtypes = [O]
+    lib.sg_octree_scratch_bytes.restype = sz
+    lib.sg_octree_build.argtypes = [O, p, sz, p, p]
+    lib.sg_octree_nodes.argtypes = [O, i, p, p]
+    lib.sg_octree_traversal.argtypes = [O, p, p, i, i, i, i, i, i, p, p, p, p, p, p, p, p, p, p, p]
+    lib.sg_sample_fine.argtypes = [O, p, p, p, i, i, p, p, i, i, p, p, p]
+    lib.sg_nerf_param_count.argtypes = []
+    lib.sg_nerf_param_count.restype = sz
+    lib.sg_nerf_density.argtypes = [p, p, p, p, i, i, i, p, p, p, p]
     lib.sg_trilerp_nodes_fwd.argtypes = [C.POINTER(SgTree), p, p, p, p, p, i, i, i, p, p]
     lib.sg_trilerp_nodes_bwd.argtypes = [C.POINTER(SgTree), p, p, p, p, p, i, i, i, p, p]
     return lib

@@ -192,6 +192,10 @@ int tune(int knob);
 // are multiples of it.
 int num_sms();
 
+// -1 padding of hit-row tails [count[r], W) of R rows (a warp per row, 16-byte
+// stores where the row is aligned); defined in intersect.cu
+void launch_pad_rows(long R, int W, const int *count, int *idx, float *t0, float *t1, sg_stream_t stream);
+
 // ---------------------------------------------------------------------------
 // ray generation (rays_calculating_kernel, sampling_kernel.cu:411-486)
 // ---------------------------------------------------------------------------

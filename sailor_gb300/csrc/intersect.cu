@@ -469,6 +469,13 @@ __global__ void pad_rows_kernel(long R, int W, const int *__restrict__ count, in
   }
 }
 
+void launch_pad_rows(long R, int W, const int *count, int *idx, float *t0, float *t1, sg_stream_t stream) {
+  if (R <= 0 || W <= 0) return;
+  int g = ceil_div(R * 32, 256);
+  if (g > num_sms() * 64) g = num_sms() * 64;
+  pad_rows_kernel<<<g, 256, 0, stream>>>(R, W, count, idx, t0, t1);
+}
+
 }  // namespace sg
 
 using namespace sg;
@@ -492,11 +499,7 @@ extern "C" int sg_intersect(const SgTree *tree, const float *ori, const float *d
     const int blk = tune(SG_TUNE_ISECT_BLOCK);
     intersect_kernel<<<ceil_div(R, blk), blk, 0, stream>>>(p);
   }
-  if (padded) {
-    int g = ceil_div(R * 32, 256);
-    if (g > num_sms() * 64) g = num_sms() * 64;
-    pad_rows_kernel<<<g, 256, 0, stream>>>(R, W, hit_count, hit_idx, hit_t0, hit_t1);
-  }
+  if (padded) launch_pad_rows(R, W, hit_count, hit_idx, hit_t0, hit_t1, stream);
   SG_LAUNCH_CHECK();
   return SG_OK;
 }

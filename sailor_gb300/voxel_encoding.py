@@ -242,7 +242,11 @@ def volume_rendering_occ_forward(sampled_depth, occs, feats, device, t_thresh):
 # intersection_kernel.cu:828-895, sampling_kernel.cu:1251-1462)
 # --------------------------------------------------------------------------
 class MultiLayerOctree:
-    """Two-level brick tree with the reference class's methods."""
+    """Brick tree with the reference class's methods.  Two levels (the
+    shipped octree_level=2) build the two-level tree that the coarse
+    traversal, sampling, trilinear and projection calls use; every depth
+    from 2 to SG_MAX_LEVELS also builds the multi-level node tables that
+    octree_traversal, ray_voxels_points_sampling and the node queries use."""
 
     def __init__(self, num_levels, batch_size, rate, device):
         self.num_levels = int(num_levels)
@@ -250,57 +254,113 @@ class MultiLayerOctree:
         self.rate = int(rate)
         self.device = torch.device("cuda", int(device))
         self._tree = None
+        self._oct = None
         self._status = None  # SgStatus block, allocated by init_octree
+        self._ostatus = None  # SgOctreeStatus block
         self.num_octree_nodes = 0
 
     # -- build -------------------------------------------------------------
     def init_octree(self, dense_volumes, total_num_occupied_voxels, num_occ_voxels_batches, octree_nodes_index,
                     vol_size, vol_bbox):
-        if len(dense_volumes) != 2:
-            raise RuntimeError("MultiLayerOctree: only two-level trees are supported (octree_level=2)")
+        L = len(dense_volumes)
+        if L < 2 or L > N.SG_MAX_LEVELS:
+            raise RuntimeError(f"MultiLayerOctree: {L} levels (2 to {N.SG_MAX_LEVELS} are supported)")
+        if self.rate not in (2, 4, 8):
+            raise RuntimeError(f"MultiLayerOctree: rate {self.rate} (2, 4 or 8 are supported)")
         with torch.cuda.device(self.device):
             self._vols = [_inplace(v, "volume", torch.int32) for v in dense_volumes]
             self._cnts = list(num_occ_voxels_batches)
-            self.num_levels = len(dense_volumes)
+            self.num_levels = L
             self.batch_size = self._vols[0].shape[0]
             self._totals = [int(x) for x in total_num_occupied_voxels]
             self._index = [int(x) for x in octree_nodes_index]
             self.num_octree_nodes = sum(self._totals)
             self.voxel_size = _in(vol_size, "voxel_size").view(-1)
             self.volume_bbox = _in(vol_bbox, "vol_bbox")
-            B, Db, Dt = self.batch_size, self._vols[0].shape[1], self._vols[1].shape[1]
-            if Db != Dt * self.rate:
-                raise RuntimeError(f"volume dims {Db}/{Dt} do not match rate {self.rate}")
-            mw = N.mask_words(self.rate)
+            dims = [int(v.shape[1]) for v in self._vols]
+            for l in range(1, L):
+                if dims[l - 1] != dims[l] * self.rate:
+                    raise RuntimeError(f"volume dims {dims[l - 1]}/{dims[l]} do not match rate {self.rate}")
             dev = self.device
             i32 = dict(dtype=torch.int32, device=dev)
-            cap_top, cap_bot = max(self._totals[1], 1), max(self._totals[0], 1)
-            self._bufs = dict(
-                brick_node=torch.empty(B * Dt ** 3, **i32),
-                brick_mask=torch.empty(B * Dt ** 3 * mw, **i32),
-                top_key=torch.empty(cap_top, **i32), top_child_base=torch.empty(cap_top, **i32),
-                bot_key=torch.empty(cap_bot, **i32), bot_parent=torch.empty(cap_bot, **i32),
-                counts=torch.zeros(2, **i32),
-                scratch=torch.empty(int(N.lib.sg_tree_scratch_bytes(B, Dt)), dtype=torch.uint8, device=dev))
-            b = self._bufs
-            self._tree = N.SgTree(B, Dt, Db, self.rate, self._index[1], self._index[0], cap_top, cap_bot,
-                                  b["brick_node"].data_ptr(), b["brick_mask"].data_ptr(), b["top_key"].data_ptr(),
-                                  b["top_child_base"].data_ptr(), b["bot_key"].data_ptr(),
-                                  b["bot_parent"].data_ptr(), b["counts"].data_ptr(), self.voxel_size.data_ptr(),
-                                  self.volume_bbox.data_ptr())
-            self._status = torch.zeros(4, dtype=torch.int32, device=dev)
+            self._status = torch.zeros(4, **i32)
+            self._ostatus = torch.zeros(4, **i32)
+            self._tree = None
+            if L == 2:
+                B, Db, Dt = self.batch_size, dims[0], dims[1]
+                mw = N.mask_words(self.rate)
+                cap_top, cap_bot = max(self._totals[1], 1), max(self._totals[0], 1)
+                self._bufs = dict(
+                    brick_node=torch.empty(B * Dt ** 3, **i32),
+                    brick_mask=torch.empty(B * Dt ** 3 * mw, **i32),
+                    top_key=torch.empty(cap_top, **i32), top_child_base=torch.empty(cap_top, **i32),
+                    bot_key=torch.empty(cap_bot, **i32), bot_parent=torch.empty(cap_bot, **i32),
+                    counts=torch.zeros(2, **i32),
+                    scratch=torch.empty(int(N.lib.sg_tree_scratch_bytes(B, Dt)), dtype=torch.uint8, device=dev))
+                b = self._bufs
+                self._tree = N.SgTree(B, Dt, Db, self.rate, self._index[1], self._index[0], cap_top, cap_bot,
+                                      b["brick_node"].data_ptr(), b["brick_mask"].data_ptr(),
+                                      b["top_key"].data_ptr(), b["top_child_base"].data_ptr(),
+                                      b["bot_key"].data_ptr(), b["bot_parent"].data_ptr(), b["counts"].data_ptr(),
+                                      self.voxel_size.data_ptr(), self.volume_bbox.data_ptr())
+            # multi-level node tables: one run per level, capacity = its occupied count
+            caps = [max(c, 0) for c in self._totals]
+            ob = dict(counts=torch.zeros(L, **i32))
+            for name in ("key", "parent", "child_base", "nchild"):
+                ob[name] = [torch.empty(max(c, 1), **i32) for c in caps]
+            o = N.SgOctree()
+            o.B, o.L, o.rate = self.batch_size, L, self.rate
+            for l in range(L):
+                o.dim[l], o.base[l], o.cap[l] = dims[l], self._index[l], caps[l]
+                o.vol[l] = self._vols[l].data_ptr()
+                for name in ("key", "parent", "child_base", "nchild"):
+                    getattr(o, name)[l] = ob[name][l].data_ptr()
+            o.counts = ob["counts"].data_ptr()
+            o.voxel_size = self.voxel_size.data_ptr()
+            o.vol_bbox = self.volume_bbox.data_ptr()
+            ob["scratch"] = torch.empty(max(int(N.lib.sg_octree_scratch_bytes(C.byref(o))), 16), dtype=torch.uint8,
+                                        device=dev)
+            self._oct, self._obufs = o, ob
+            self._oct_stale = True
 
     def build_octree(self):
-        if self._tree is None:
+        if self._oct is None:
             raise RuntimeError("build_octree before init_octree")
         with torch.cuda.device(self.device):
-            s = self._bufs["scratch"]
-            N.check(N.lib.sg_tree_build(C.byref(self._tree), N.ptr(self._vols[1]), N.ptr(self._vols[0]),
-                                        N.ptr(s), s.numel(), N.ptr(self._status), N.stream()), "tree_build")
+            if self._tree is not None:
+                s = self._bufs["scratch"]
+                N.check(N.lib.sg_tree_build(C.byref(self._tree), N.ptr(self._vols[1]), N.ptr(self._vols[0]),
+                                            N.ptr(s), s.numel(), N.ptr(self._status), N.stream()), "tree_build")
+                self._oct_stale = True  # multi-level tables built on first use
+            else:
+                self._build_levels()
+
+    def _build_levels(self):
+        """The multi-level node tables.  Over a two-level tree already built
+        they get the same ids (the volumes hold them; occupancy is still
+        value > -1) and the build writes them again."""
+        with torch.cuda.device(self.device):
+            self._ostatus.zero_()
+            s = self._obufs["scratch"]
+            N.check(N.lib.sg_octree_build(C.byref(self._oct), N.ptr(s), s.numel(), N.ptr(self._ostatus),
+                                          N.stream()), "octree_build")
+        self._oct_stale = False
+
+    def _levels(self):
+        if self._oct is None:
+            raise RuntimeError("multi-level query before init_octree")
+        if getattr(self, "_oct_stale", True):
+            self._build_levels()
+
+    def _two_level(self, what):
+        if self._tree is None:
+            raise RuntimeError(f"{what}: supported on two-level trees (octree_level=2); this tree has "
+                               f"{self.num_levels} levels")
 
     # -- queries -----------------------------------------------------------
     def voxel_traversal(self, ray_ori, ray_dir, n_max_hits_coarse, start_level, th_early_stop, is_training,
                         opt_num_intersected_voxels):
+        self._two_level("voxel_traversal")
         if int(start_level) != 0:
             raise RuntimeError("voxel_traversal: only start_level 0 (the top level) is supported")
         with torch.cuda.device(self.device):
@@ -323,6 +383,7 @@ class MultiLayerOctree:
 
     def ray_voxels_points_sampling_coarse(self, hits_idxs, min_depths, max_depths, uniform_rand_values,
                                           rays_valid_len, start_level, num_sampled):
+        self._two_level("ray_voxels_points_sampling_coarse")
         with torch.cuda.device(self.device):
             st = self._status.tolist()  # the reference reads its max-hit counter here too
             if st[0] & N.SG_FLAG_HIT_OVERFLOW:
@@ -354,6 +415,7 @@ class MultiLayerOctree:
             return srt, idx
 
     def trilinear_aggregate_features(self, ray_ori, ray_dir, sampled_z, sampled_idx, input_feats):
+        self._two_level("trilinear_aggregate_features")
         with torch.cuda.device(self.device):
             f = _in(input_feats, "input_feats")
             B, Cf, Nr, S, _ = f.shape
@@ -366,6 +428,7 @@ class MultiLayerOctree:
 
     def trilinear_aggregate_features_backward(self, ray_ori, ray_dir, sampled_z, sampled_idx, input_feats,
                                               grad_output):
+        self._two_level("trilinear_aggregate_features_backward")
         with torch.cuda.device(self.device):
             g = _in(grad_output, "grad_output")
             B, Cf, Nr, S = g.shape
@@ -382,8 +445,10 @@ class MultiLayerOctree:
         projected into every view: (proj_xy [B,V,N,S,9,2] or [B,V,N,S,2]
         normalised to [-1, 1], proj_z [B,V,N,S,9,1] or [B,V,N,S,1] camera z);
         -1 where the sample has no node (sampling_kernel.cu:1333-1381)."""
-        if record_corners and self._tree is None:
+        if record_corners and self._oct is None:
             raise RuntimeError("project_sampled_xyz with record_corners before init_octree")
+        if record_corners:
+            self._two_level("project_sampled_xyz with record_corners")
         with torch.cuda.device(self.device):
             z = _in(sampled_z, "sampled_z")
             idx = _in(sampled_idx, "sampled_idx", torch.int32)
@@ -407,16 +472,25 @@ class MultiLayerOctree:
     def get_nodes_tensor(self):
         with torch.cuda.device(self.device):
             out = torch.empty((self.num_octree_nodes, 6), device=self.device)
-            N.check(N.lib.sg_tree_nodes(C.byref(self._tree), self.num_octree_nodes, N.ptr(out), N.stream()),
-                    "tree_nodes")
+            if self._tree is not None:
+                N.check(N.lib.sg_tree_nodes(C.byref(self._tree), self.num_octree_nodes, N.ptr(out), N.stream()),
+                        "tree_nodes")
+            else:
+                self._levels()
+                N.check(N.lib.sg_octree_nodes(C.byref(self._oct), self.num_octree_nodes, N.ptr(out),
+                                              N.stream()), "octree_nodes")
             return out
 
     def get_num_nodes(self):
         return self.num_octree_nodes
 
     def get_num_nodes_valid(self):
-        """[#top nodes, #bottom nodes] (the reference's queue_control)."""
-        return self._bufs["counts"].tolist()
+        """Nodes built per level, top level first (the reference's
+        queue_control: [#top nodes, #next level, ...])."""
+        if self._tree is not None:
+            return self._bufs["counts"].tolist()
+        self._levels()
+        return self._obufs["counts"].tolist()[::-1]
 
     def get_num_levels(self):
         return self.num_levels
@@ -431,10 +505,70 @@ class MultiLayerOctree:
         """Device node tables (brick map, masks, keys) for inspection."""
         return dict(self._bufs)
 
-    def octree_traversal(self, *a, **k):
-        raise NotImplementedError("multi-level DFS traversal (octree_traversal) is not part of this build; "
-                                  "SRONet calls voxel_traversal (only_voxel_traversal=True)")
+    def octree_traversal(self, ray_ori, ray_dir, n_max_hits_coarse, n_max_hits, start_level, th_early_stop,
+                         opt_num_intersected_voxels):
+        """(idx, min_depths, max_depths, valid_len [B,N,1], idx_c, min_depths_c,
+        max_depths_c): the coarse DDA over level L-1-start_level, then the
+        depth-first descent of each coarse node (intersection_kernel.cu:
+        441-643, 722-826).  Fine rows hold each coarse node's entries
+        together, in descent order; the reference's atomic appends leave the
+        same entries in a run-dependent order."""
+        if self._oct is None:
+            raise RuntimeError("octree_traversal before init_octree")
+        self._levels()
+        start_level = int(start_level)
+        if not 0 <= start_level < self.num_levels:
+            raise RuntimeError(f"octree_traversal: start_level {start_level} outside [0, {self.num_levels})")
+        with torch.cuda.device(self.device):
+            ori = _in(ray_ori, "ray_ori")
+            dr = _in(ray_dir, "ray_dir")
+            Nr = ori.shape[1]
+            B, Wc, Wf = self.batch_size, int(n_max_hits_coarse), int(n_max_hits)
+            dev = self.device
+            idx_c = torch.empty((B, Nr, Wc), dtype=torch.int32, device=dev)
+            t0_c = torch.empty((B, Nr, Wc), device=dev)
+            t1_c = torch.empty((B, Nr, Wc), device=dev)
+            idx = torch.empty((B, Nr, Wf), dtype=torch.int32, device=dev)
+            t0 = torch.empty((B, Nr, Wf), device=dev)
+            t1 = torch.empty((B, Nr, Wf), device=dev)
+            vl = torch.empty((B, Nr, 1), device=dev)
+            cnt_c = torch.empty((B, Nr), dtype=torch.int32, device=dev)
+            cnt = torch.empty((B, Nr), dtype=torch.int32, device=dev)
+            self._ostatus.zero_()
+            N.check(N.lib.sg_octree_traversal(C.byref(self._oct), N.ptr(ori), N.ptr(dr), Nr, start_level, Wc, Wf,
+                                              int(th_early_stop), int(opt_num_intersected_voxels), N.ptr(idx_c),
+                                              N.ptr(t0_c), N.ptr(t1_c), N.ptr(cnt_c), N.ptr(idx), N.ptr(t0),
+                                              N.ptr(t1), N.ptr(cnt), N.ptr(vl), N.ptr(self._ostatus), N.stream()),
+                    "octree_traversal")
+            self._last_fine = (Wc, Wf)
+            return idx, t0, t1, vl, idx_c, t0_c, t1_c
 
-    def ray_voxels_points_sampling(self, *a, **k):
-        raise NotImplementedError("the fine adaptive sampler pairs with octree_traversal and is not part of this "
-                                  "build; use ray_voxels_points_sampling_coarse")
+    def ray_voxels_points_sampling(self, hits_idxs, min_depths, max_depths, rays_valid_len, uniform_rand_values,
+                                   start_level, num_sampled):
+        """(sampled_idx, sampled_depths) [B,N,S] over fine rows
+        (sampling_kernel.cu:911-1068, 1178-1248); unsorted, as the
+        reference returns them."""
+        if self._oct is None:
+            raise RuntimeError("ray_voxels_points_sampling before init_octree")
+        self._levels()
+        with torch.cuda.device(self.device):
+            st = self._ostatus.tolist()  # the reference reads its fine max-hit counter here too
+            if st[0] & N.SG_FLAG_HIT_OVERFLOW:
+                Wc, Wf = getattr(self, "_last_fine", (0, 0))
+                raise RuntimeError(f"octree row overflow: a ray has {st[1]} coarse / {st[2]} fine entries, "
+                                   f"rows hold {Wc} / {Wf}")
+            hi = _in(hits_idxs, "hits_idxs", torch.int32)
+            B, Nr, W = hi.shape
+            t0 = _in(min_depths, "min_depths")
+            t1 = _in(max_depths, "max_depths")
+            vl = _in(rays_valid_len, "rays_valid_len")
+            rd = _in(uniform_rand_values, "uniform_rand_values")
+            S = int(num_sampled)
+            if rd.numel() != B * Nr * S:
+                raise RuntimeError(f"uniform_rand_values must hold [{B}, {Nr}, {S}] values")
+            si = torch.empty((B, Nr, S), dtype=torch.int32, device=self.device)
+            sz = torch.empty((B, Nr, S), device=self.device)
+            N.check(N.lib.sg_sample_fine(C.byref(self._oct), N.ptr(hi), N.ptr(t0), N.ptr(t1), Nr, W, N.ptr(vl),
+                                         N.ptr(rd), S, int(start_level), N.ptr(si), N.ptr(sz), N.stream()),
+                    "sample_fine")
+            return si, sz

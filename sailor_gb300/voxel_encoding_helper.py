@@ -255,15 +255,25 @@ class OcTreeOptions(nn.Module):
     @torch.no_grad()
     def _ray_intersection(self, _ray_ori, _ray_dir, _instersect_start_level=1, th_early_stop=-1,
                           only_voxel_traversal=True, is_training=False, opt_num_intersected_voxels=-1):
-        if not only_voxel_traversal:
-            return self._octree.octree_traversal()
-        self._n_max_hits_coarse = 1024
-        return self._octree.voxel_traversal(_ray_ori, _ray_dir, self._n_max_hits_coarse, _instersect_start_level,
-                                            th_early_stop, is_training, opt_num_intersected_voxels)
+        # coarse rows: three cells per coarse-grid edge (voxel_encoding_helper.py:573)
+        self._n_max_hits_coarse = self._vol_dim[0] * 3 // self._rate ** (self._levels - _instersect_start_level - 1)
+        if only_voxel_traversal:
+            self._n_max_hits_coarse = 1024
+            return self._octree.voxel_traversal(_ray_ori, _ray_dir, self._n_max_hits_coarse,
+                                                _instersect_start_level, th_early_stop, is_training,
+                                                opt_num_intersected_voxels)
+        return self._octree.octree_traversal(_ray_ori, _ray_dir, self._n_max_hits_coarse, self._n_max_hits,
+                                             _instersect_start_level, th_early_stop, opt_num_intersected_voxels)
 
     @torch.no_grad()
     def _sort_sampling(self, sampled_depths):
         return self._octree.sort_samplings(sampled_depths)
+
+    @torch.no_grad()
+    def _ray_voxels_sampling_points(self, _idx, _min_depths, _max_depths, _ray_total_valid_len, _uniform_noise,
+                                    _instersect_start_level, _n_sampled_points):
+        return self._octree.ray_voxels_points_sampling(_idx, _min_depths, _max_depths, _ray_total_valid_len,
+                                                       _uniform_noise, _instersect_start_level, _n_sampled_points)
 
     @torch.no_grad()
     def _ray_voxels_points_sampling_coarse(self, _idx, _min_depths, _max_depths, _uniform_noise,
@@ -279,6 +289,11 @@ class OcTreeOptions(nn.Module):
                          only_voxel_traversal=True, is_training=False, opt_num_intersected_voxels=-1):
         return self._ray_intersection(ray_ori, ray_dir, instersect_start_level, th_early_stop,
                                       only_voxel_traversal, is_training, opt_num_intersected_voxels)
+
+    def ray_voxels_sampling_points(self, idx, min_depths, max_depths, ray_total_valid_len, uniform_noise,
+                                   instersect_start_level=1, n_sampled_points=128):
+        return self._ray_voxels_sampling_points(idx, min_depths, max_depths, ray_total_valid_len, uniform_noise,
+                                                instersect_start_level, n_sampled_points)
 
     def ray_voxels_points_sampling_coarse(self, idx, min_depths, max_depths, uniform_noise, ray_total_valid_len,
                                           instersect_start_level=1, n_sampled_points=128):

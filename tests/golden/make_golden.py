@@ -8,7 +8,9 @@ they lie; this script only loads the cubins):
 
 It writes ``ref_chain_explicit.npz``, ``ref_chain_auto.npz``,
 ``ref_composite.npz``, ``ref_rays.npz`` and ``ref_project.npz`` (``--only rays`` or
-``--only project``: that one alone; ``--only density_mlp`` writes
+``--only project``: that one alone; ``--only octree`` writes
+``ref_octree.npz`` from the multi-level tree, its depth-first traversal
+and the fine sampler; ``--only density_mlp`` writes
 ``ref_density_mlp.npz`` from FastNerf's occupancy MLP, whose cubin
 ``oracle/build.py --fastnerf`` builds).  Each holds the seeded inputs
 and the reference outputs of fusion, coarse occupancy, the two-level tree
@@ -199,14 +201,89 @@ def density_mlp(out_dir):
     print("density_mlp done", flush=True)
 
 
+def octree(out_dir):
+    """Rate-2 trees over a 64^3 fine grid -- two levels traversed from the
+    top (start level 0) and three levels traversed from the middle (start
+    level 1) -- their octree_traversal and ray_voxels_points_sampling with
+    rands 0.5 -> ref_octree.npz.  Both descents go one level below the
+    coarse node: deeper ones overflow the reference's 8-entry stack.  The
+    scene seed is the first whose top grid has no isolated occupied voxel in
+    either tree (so the reference's traversal reads only real nodes) and
+    whose descents fit the 8-entry stack and list with a margin (checked on
+    the oracle before any reference launch)."""
+    from oracle import oracle as orc
+    rate, Dm, tres = 2, 64, 40
+    configs = ((2, 0, 32), (3, 1, 48))  # (levels, start level, samples)
+    for seed in range(31, 60):
+        scene = syn.make_scene(seed=seed, n_views=VIEWS, res=RES, n_prims=PRIMS, D=Dm, trunc=0.03)
+        f = rc.integrate(scene["K"], scene["RT"], scene["colors"], scene["depths"], Dm, 1.0, 0.025,
+                         scene["trunc_weight"], 13.5, 13.5, vol_bbox=scene["vol_bbox"],
+                         voxel_size=scene["voxel_size"])
+        ori, dirs = syn.target_rays(seed=seed, res=tres)
+        vs, bb = scene["voxel_size"].reshape(-1), scene["vol_bbox"]
+        good = True
+        for L, st, _ in configs:
+            vols, _ = rc.merge_levels(f["occ"], rate, L)
+            occ_in = [v.cpu().numpy() for v in vols]
+            t = orc.build_octree(occ_in, rate)
+            s_ = L - 1 - st
+            good = good and np.array_equal(t["counts"], [int((v > -1).sum()) for v in occ_in])
+            good = good and orc.octree_traversal(t, ori, dirs, vs, bb, st, 4 * int(t["dims"][s_]),
+                                                 32 * int(t["dims"][s_]))["need"].max() <= 7
+        if good:
+            break
+    else:
+        raise RuntimeError("no seed gives complete trees with bounded descents")
+    out = dict(rate=np.array(rate), seed=np.array(seed), ori=ori, dirs=dirs, n_configs=np.array(len(configs)),
+               voxel_size=f["voxel_size"].cpu().numpy(), vol_bbox=f["vol_bbox"].cpu().numpy())
+    for c, (L, st, S) in enumerate(configs):
+        k = f"c{c}_"
+        vols, _ = rc.merge_levels(f["occ"].clone(), rate, L)
+        occ_in = [v.cpu().numpy() for v in vols]
+        tree = rc.OctreeML(vols, f["voxel_size"], f["vol_bbox"], rate)
+        assert tree.complete
+        table = tree.node_table()
+        out[k + "L"], out[k + "start"], out[k + "S"] = np.array(L), np.array(st), np.array(S)
+        for l in range(L):
+            out[k + f"occ_in_{l}"] = occ_in[l]
+            ids = np.arange(tree.index[l], tree.index[l] + tree.totals[l])
+            out[k + f"nodes_{l}"] = tree.canonical(ids, table)[:, 1:].astype(np.int16)
+        s_ = L - 1 - st
+        Wc = 4 * tree.dims[s_]
+        Wf = 8 * Wc
+        r = tree.octree_traversal(ori, dirs, st, Wc, Wf)
+        cnt = r["cnt"].cpu().numpy()[..., 0]
+        wf = max(int(cnt.max()), 1)
+        wc = max(int((r["idx_c"] >= 0).sum(-1).max().item()), 1)
+        out[k + "Wc"], out[k + "Wf"] = np.array(wc), np.array(wf)
+        out[k + "coarse_keys"] = tree.canonical(r["idx_c"][..., :wc].cpu().numpy(), table).astype(np.int16)
+        out[k + "t0_c"] = r["t0_c"][..., :wc].cpu().numpy()
+        out[k + "t1_c"] = r["t1_c"][..., :wc].cpu().numpy()
+        out[k + "fine_keys"] = tree.canonical(r["idx"][..., :wf].cpu().numpy(), table).astype(np.int16)
+        out[k + "t0"] = r["t0"][..., :wf].cpu().numpy()
+        out[k + "t1"] = r["t1"][..., :wf].cpu().numpy()
+        out[k + "valid_len"] = r["valid_len"].cpu().numpy()
+        rands = np.full((1, ori.shape[1], S), 0.5, np.float32)
+        si, sd = tree.sample_fine(r["idx"], r["t0"], r["t1"], r["valid_len"], rands, S, st)
+        out[k + "sample_keys"] = tree.canonical(si.cpu().numpy(), table).astype(np.int16)
+        out[k + "sample_z"] = sd.cpu().numpy()
+        print("octree", L, "levels, start", st, "coarse", wc, "fine", wf, flush=True)
+    np.savez_compressed(os.path.join(out_dir, "ref_octree.npz"), **out)
+    print("octree done, seed", seed, flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
-    ap.add_argument("--only", choices=["rays", "project", "density_mlp"])
+    ap.add_argument("--only", choices=["rays", "project", "density_mlp", "octree"])
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
     if args.only == "density_mlp":
         density_mlp(args.out)
+        return
+    if args.only == "octree":
+        assert rc.available(), "reference cubins or GPU missing"
+        octree(args.out)
         return
     assert rc.available(), "reference cubins or GPU missing"
     if args.only == "project":

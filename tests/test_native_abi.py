@@ -66,13 +66,26 @@ def test_cpu_tensors_rejected():
         VE.build_multi_res_volumes([torch.zeros(1, 8, 8, 8, dtype=torch.int32)], [torch.zeros(1, 1)], 2, 4, 0)
 
 
-def test_unsupported_tree_levels():
+def test_unsupported_tree_shapes():
+    """Depths outside [2, SG_MAX_LEVELS] and rates other than 2, 4, 8 are
+    refused on the host before anything reaches the device; the traversal
+    and fine sampling refuse to run before init_octree."""
+    from sailor_gb300 import _native as N
     from sailor_gb300.dist import VoxelEncoding as VE
-    o = VE.MultiLayerOctree(3, 1, 2, 0)
-    with pytest.raises(RuntimeError, match="two-level"):
+    o = VE.MultiLayerOctree(1, 1, 2, 0)
+    with pytest.raises(RuntimeError, match="levels"):
+        o.init_octree([None], [0], [None], [0], None, None)
+    o = VE.MultiLayerOctree(N.SG_MAX_LEVELS + 1, 1, 2, 0)
+    with pytest.raises(RuntimeError, match="levels"):
+        o.init_octree([None] * (N.SG_MAX_LEVELS + 1), [0] * 13, [None] * 13, [0] * 13, None, None)
+    o = VE.MultiLayerOctree(3, 1, 3, 0)
+    with pytest.raises(RuntimeError, match="rate"):
         o.init_octree([None] * 3, [0, 0, 0], [None] * 3, [0, 0, 0], None, None)
-    with pytest.raises(NotImplementedError):
-        o.octree_traversal()
+    o = VE.MultiLayerOctree(3, 1, 2, 0)
+    with pytest.raises(RuntimeError, match="before init_octree"):
+        o.octree_traversal(None, None, 8, 8, 0, -1, -1)
+    with pytest.raises(RuntimeError, match="before init_octree"):
+        o.ray_voxels_points_sampling(None, None, None, None, None, 0, 8)
 
 
 def test_struct_layouts_match_header(tmp_path):
@@ -84,7 +97,7 @@ def test_struct_layouts_match_header(tmp_path):
     if shutil.which("gcc") is None:
         pytest.skip("gcc not available")
     structs = {name: getattr(N, name) for name in ("SgTree", "SgViews", "SgRaySegments", "SgRenderArgs",
-                                                   "SgFeatureMap", "SgProjGather")}
+                                                   "SgFeatureMap", "SgProjGather", "SgOctree")}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "sailor_gb300.h"', "int main(void) {"]
     for name, cls in structs.items():
         lines.append(f'  printf("{name} size %zu\\n", sizeof({name}));')
