@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="small configuration (256^3, 512^2) for profiling")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
-    ap.add_argument("--workload", default="batch", choices=["batch", "plain", "project", "diff", "octree"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "plain", "project", "diff", "octree", "nerf"])
     ap.add_argument("--unfused", action="store_true",
                     help="render with four kernels (sample+sort, two field gathers, composite) instead of one")
     ap.add_argument("--no-parity", action="store_true",
@@ -1352,16 +1352,18 @@ def octree_step(o, d, cfg, events=None):
     return rows, si, sz
 
 
-def _cpu_octree_job(cfg, occ0, ori, dirs, vs, bbox, reps, n_rays=4096):
+def _cpu_octree_job(cfg, occ0, ori, dirs, vs, bbox, reps, n_rays=None):
     """The oracle's C port on the host cores (spawned process): the
     multi-level build of the whole volume, and traversal + fine sampling of
-    n_rays rays drawn from the target, scaled to all its rays."""
+    n_rays rays drawn from the target (all of them by default), scaled to
+    all its rays."""
     import time
 
     from oracle import oracle as orc
     L, rate, S = cfg["levels"], cfg["rate"], cfg["S"]
     R = ori.shape[1]
-    pick = np.random.default_rng(5).choice(R, n_rays, replace=False)
+    n_rays = R if n_rays is None else n_rays
+    pick = np.sort(np.random.default_rng(5).choice(R, n_rays, replace=False))
     rd = np.random.default_rng(6).random((1, n_rays, S), dtype=np.float32)
     out = []
     for _ in range(reps):
@@ -1384,9 +1386,9 @@ def cpu_baseline_octree(cfg, occ0, ori, dirs, vs, bbox, reps):
     with cf.ProcessPoolExecutor(max_workers=1, mp_context=mp.get_context("spawn")) as ex:
         runs, cores = ex.submit(_cpu_octree_job, cfg, occ0, ori, dirs, vs, bbox, reps).result()
     return dict(value=float(np.median([r["value"] for r in runs])), unit="rays/s", cores=cores, kind="port",
-                sample="oracle (C port, OpenMP) on host cores: merge + multi-level build of the whole volume, "
-                       "traversal + fine sampling of 4096 of the target's rays scaled to all of them; median of "
-                       f"{len(runs)} samples in a separate process",
+                sample="oracle (C port, OpenMP) on host cores: the whole step (merge + multi-level build of "
+                       "the whole volume, traversal + fine sampling of every ray of the target); median of "
+                       f"{len(runs)} runs in a separate process",
                 samples=[r["value"] for r in runs], sample_wall_s=[r["sample_wall_s"] for r in runs])
 
 
@@ -1530,9 +1532,186 @@ def run_octree(args):
     print(json.dumps(out), flush=True)
 
 
+# --------------------------------------------------------------------------
+# FastNerf's occupancy network (the consumer of the samples): the tensor-core
+# sg_nerf_density over sampled point-views
+# --------------------------------------------------------------------------
+NERF = dict(points=1 << 22, views=3, scale=0.3, seed=29)
+
+
+def nerf_inputs(cfg, dev):
+    import torch
+    gen = torch.Generator(device=dev).manual_seed(cfg["seed"])
+    B, V, N = 1, cfg["views"], cfg["points"]
+    from sailor_gb300 import _native as N_
+    params = (torch.randn(int(N_.lib.sg_nerf_param_count()), generator=gen, device=dev) * cfg["scale"]).half()
+    z = torch.rand((B, V, N, 1), generator=gen, device=dev) * 2.5 + 0.5
+    tp = torch.rand((B, V, N, 1), generator=gen, device=dev) * 2.0 - 1.0
+    g = torch.randn((B, V, N, 16), generator=gen, device=dev) * 0.5
+    return params, z, tp, g
+
+
+# float multiply-adds per point-view (feature + geometry MLPs) and per point (sigma MLP)
+NERF_MACS_PV = 18 * 64 + 3 * 64 * 64 + 18 * 16 + 16 * 8
+NERF_MACS_P = 2 * 64 * 64 + 64
+
+
+def _cpu_nerf_job(cfg, n_points, reps):
+    """The reference's float16 network restated in numpy (oracle/fastnerf.py)
+    on n_points points x V views, in a spawned process."""
+    import time
+
+    from oracle import fastnerf as fn
+    rng = np.random.default_rng(cfg["seed"])
+    V = cfg["views"]
+    params = (rng.normal(0, 1, fn.PARAM_COUNT) * cfg["scale"]).astype(np.float16)
+    z = rng.uniform(0.5, 3.0, (1, V, n_points, 1)).astype(np.float32)
+    tp = rng.uniform(-1.0, 1.0, (1, V, n_points, 1)).astype(np.float32)
+    g = rng.normal(0, 0.5, (1, V, n_points, 16)).astype(np.float32)
+    out = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        fn.infer_density(z, tp, g, params, 1, n_points, V)
+        out.append(n_points / (time.perf_counter() - t0))
+    return out
+
+
+def run_nerf(args):
+    import tempfile
+
+    import torch
+
+    from sailor_gb300 import _native as N_
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    cfg = dict(NERF)
+    if args.small:
+        cfg.update(points=1 << 18)
+    params, z, tp, g = nerf_inputs(cfg, dev)
+    B, V, Np = 1, cfg["views"], cfg["points"]
+    dens = torch.empty((B, 1, Np), device=dev)
+    geo = torch.empty((B, V, Np, 8), device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+
+    def step():
+        N_.check(N_.lib.sg_nerf_density(N_.ptr(params), N_.ptr(z), N_.ptr(tp), N_.ptr(g), B, Np, V, N_.ptr(dens),
+                                        N_.ptr(geo), N_.ptr(err), N_.stream()), "nerf_density")
+    warm = max(args.warmup, 3)
+    for _ in range(warm):
+        step()
+    torch.cuda.synchronize()
+    if err.item():
+        raise RuntimeError("nerf_density wait timed out")
+    clk = ClockSampler(os.path.join(tempfile.gettempdir(), "sg_clocks_nerf.csv"))
+    with clk:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(args.steps):
+            step()
+        e1.record()
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    flops = 2.0 * (NERF_MACS_PV * V * Np + NERF_MACS_P * Np)
+    # algorithmic bytes: inputs (z, t_psdf, 16 features) per point-view, the
+    # geometry features out per point-view, the density out per point, params
+    nbytes = (18 * 4 + 8 * 4) * V * Np + 4 * Np + 2 * N_.lib.sg_nerf_param_count()
+    pk, pk_kind = peaks()
+    # e2e through the Python drop-in from pinned host buffers
+    from sailor_gb300.nerf import infer_density
+    host = [t.cpu().pin_memory() for t in (z, tp, g)]
+    dev_in = [torch.empty_like(t) for t in (z, tp, g)]
+    out_h = torch.empty((B, 1, Np)).pin_memory()
+
+    def e2e_step():
+        for a, b in zip(dev_in, host):
+            a.copy_(b, non_blocking=True)
+        d = infer_density(dev_in[0], dev_in[1], dev_in[2], params, B, Np, V, 0)
+        out_h.copy_(d, non_blocking=True)
+    e2e_step()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_e2e = e0.elapsed_time(e1) / args.steps
+    tf = flops / (ms / 1000.0) / 1e12
+    out = dict(metric="points/s FastNerf occupancy network (3 views, feature + geometry + sigma MLPs, fp16 operands)",
+               value=Np / (ms / 1000.0), unit="points/s", n_gpus=1, steps=args.steps, warmup=warm, ms_per_step=ms,
+               higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f16 operands, f32 sums",
+               data="synthetic (seeded inputs, N(0, 0.3) float16 parameters)",
+               config=dict(workload=f"{Np} points x {V} views (z, t_psdf, 16 geometry features each) -> densities "
+                                    f"and geometry features", l2=f"inputs {nbytes / 1e9:.2f} GB > L2"),
+               tensor_tflops=tf, hbm_gbs=nbytes / (ms / 1000.0) / 1e9,
+               roofline=dict(bound="hbm", kernel="nerf_density_kernel", achieved=nbytes / (ms / 1000.0) / 1e9,
+                             peak=pk["hbm_gbs"], unit="GB/s", frac=nbytes / (ms / 1000.0) / 1e9 / pk["hbm_gbs"],
+                             traffic=None, peak_kind=pk_kind, algorithmic_bytes=nbytes,
+                             tensor=dict(achieved=tf, peak=pk.get("bf16_tflops"), unit="TFLOP/s",
+                                         frac=(tf / pk["bf16_tflops"]) if pk.get("bf16_tflops") else None,
+                                         flops=flops)),
+               e2e=dict(value=Np / (ms_e2e / 1000.0), unit="points/s",
+                        h2d_bytes_per_step=sum(t.numel() * 4 for t in host), d2h_bytes_per_step=out_h.numel() * 4),
+               gpu_launches=args.steps, clocks=clk.summary())
+    if not args.no_cpu_baseline:
+        import concurrent.futures as cf
+        import multiprocessing as mp
+        n_cpu = 1 << 14
+        with cf.ProcessPoolExecutor(max_workers=1, mp_context=mp.get_context("spawn")) as ex:
+            vals = ex.submit(_cpu_nerf_job, cfg, n_cpu, 3).result()
+        out["cpu_baseline"] = dict(value=float(np.median(vals)), unit="points/s", cores=1, kind="port",
+                                   sample=f"oracle/fastnerf.py (numpy restatement of the reference's float16 "
+                                          f"__hfma chains) on {n_cpu} points x {V} views; median of 3",
+                                   samples=vals)
+    print(json.dumps(out), flush=True)
+
+
+def run_reference_nerf(args):
+    """--impl reference --workload nerf: the reference's own CUDA kernels
+    (density_feat_kernel, torch.mean, density_sigma_kernel, from the cubin
+    that oracle/build.py --fastnerf compiles) on the same inputs and GPU."""
+    import torch
+
+    from oracle import ref_cubin as rc
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    cfg = dict(NERF)
+    if args.small:
+        cfg.update(points=1 << 18)
+    if not rc.nerf_available():
+        print(json.dumps({"impl": "reference", "unavailable": "FastNerf cubin not built (oracle/build.py --fastnerf)"}))
+        return
+    params, z, tp, g = nerf_inputs(cfg, dev)
+    B, V, Np = 1, cfg["views"], cfg["points"]
+    p_np, z_np, tp_np, g_np = (t.cpu().numpy() for t in (params, z, tp, g))
+    for _ in range(max(args.warmup, 1)):
+        rc.infer_density_mlp(z_np, tp_np, g_np, p_np, B, Np, V)
+    import time
+    times = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc.infer_density_mlp(z_np, tp_np, g_np, p_np, B, Np, V)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    ms = 1000.0 * float(np.median(times))
+    v = Np / (ms / 1000.0)
+    print(json.dumps(dict(metric="points/s FastNerf occupancy network (3 views, feature + geometry + sigma MLPs, "
+                                 "fp16 operands)", value=v, unit="points/s", impl="reference", n_gpus=1,
+                          steps=args.steps, warmup=args.warmup, ms_per_step=ms, higher_is_better=True,
+                          scaling="weak", vs_baseline=None, dtype="f16",
+                          data="synthetic (seeded inputs, N(0, 0.3) float16 parameters)",
+                          config=dict(workload=f"{Np} points x {V} views, the reference's two kernels and torch.mean "
+                                               "on this GPU (host-to-device copies of the inputs included)"),
+                          e2e=dict(value=v, unit="points/s", h2d_bytes_per_step=int(z_np.nbytes * 2 + g_np.nbytes),
+                                   d2h_bytes_per_step=0))), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
+        if args.workload == "nerf":
+            return run_reference_nerf(args)
         return run_reference(args)
     if args.workload == "batch":
         return run_batch(args)
@@ -1542,6 +1721,8 @@ def main():
         return run_diff(args)
     if args.workload == "octree":
         return run_octree(args)
+    if args.workload == "nerf":
+        return run_nerf(args)
     return run_plain(args)
 
 

@@ -342,7 +342,8 @@ int sg_sort_samples(const float *z, int R, int S, float *sorted, int *idx,
 
 /* ---- compositing ------------------------------------------------------------ */
 
-/* Front-to-back compositing of R rays x S samples, C feature channels.
+/* Front-to-back compositing of R rays x S samples (S <= 128), C <= 32
+ * feature channels (C <= 16 for the adjoint).
  * mode 0: alpha = 1 - exp(-sigma * delta) (volume_rendering_training_
  * forward_kernel, volume_rendering.cu:17-126); mode 1: alpha = sigma
  * (volume_rendering_occ_training_forward_kernel :129-240).  sort_idx NULL:

@@ -14,10 +14,12 @@ The occupancy compositing that consumes the densities
 (volume_rendering_occ_kernel, infer_mlp.cu:508-580) is the pre-sorted
 occupancy mode of ``oracle.composite_fwd`` with C channels.
 
-Parity unpinned: the reference kernels have not yet been run to produce
-golden vectors for this restatement (``oracle/build.py --fastnerf`` compiles
-them to a cubin); the CPU tests pin the float16 arithmetic (``hfma`` against
-exact rational arithmetic) and the parameter layout.
+Pinned: the reference kernels (compiled by ``oracle/build.py --fastnerf``
+and run by ``tests/golden/make_golden.py --only density_mlp``) give
+``tests/golden/ref_density_mlp.npz``, which this restatement reproduces bit
+for bit (densities and geometry features); the CPU tests also pin the
+float16 arithmetic (``hfma`` against exact rational arithmetic) and the
+parameter layout.
 
 Parameter layout of the density network (one float16 vector, per layer the
 weights [out][in] row-major, then the bias [out]):

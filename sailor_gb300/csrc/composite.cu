@@ -25,7 +25,8 @@
 
 namespace sg {
 
-constexpr int kMaxC = 16;
+constexpr int kMaxC = 32;     // forward: FastNerf composites 30 channels (infer_mlp.cu:508-580)
+constexpr int kMaxCBwd = 16;  // adjoint (no inference-only caller needs more)
 
 struct CompParams {
   const float *z;
@@ -145,7 +146,7 @@ __global__ void __launch_bounds__(256) composite_bwd_kernel(CompParams p) {
   const int lane = lane_id();
   float *s_z = s_zall[threadIdx.x >> 5];
   float *s_f = s_fall[threadIdx.x >> 5];
-  constexpr int CM = CT > 0 ? CT : kMaxC;
+  constexpr int CM = CT > 0 ? CT : kMaxCBwd;
   const int C = CT > 0 ? CT : p.C;
   for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < p.R;
        r += ((long)gridDim.x * blockDim.x) >> 5) {
@@ -373,7 +374,7 @@ extern "C" int sg_composite_bwd(const float *g_feat, const float *g_depth, const
   if (!g_feat || !g_depth || !g_ws || !g_alpha || !z || !sigma || !feats || !grad_feats || !grad_sigma)
     return SG_ERR_INVALID_ARG;
   if (!exact && (!o_feat || !o_depth || !o_ws || !o_alpha)) return SG_ERR_INVALID_ARG;
-  if (R < 0 || S <= 0 || C <= 0 || C > kMaxC || (mode != 0 && mode != 1)) return SG_ERR_INVALID_ARG;
+  if (R < 0 || S <= 0 || C <= 0 || C > kMaxCBwd || (mode != 0 && mode != 1)) return SG_ERR_INVALID_ARG;
   if (R == 0) return SG_OK;
   CompParams p{};
   p.z = z;

@@ -41,3 +41,16 @@ def infer_density(points_z, points_tpsdf, sampled_feats_geo, net_params_density,
         if err.item():
             raise RuntimeError("nerf_density: a tensor-core wait timed out")
         return (dens, geo_out) if return_geo else dens
+
+
+def occupancy_compositing(sorted_depths, occupancies, feats, t_thres, device):
+    """FastNerf's occupancy compositing (volume_rendering_occ_kernel,
+    c_lib/FastNerf/src/infer_mlp.cu:508-580): pre-sorted depths [B, R, S]
+    (-1 for none), occupancies [B, R, S(, 1)] used as alphas, features
+    [B, R, S, C] (C <= 32; FastNerf composites 30) -> (features [B, R, C],
+    depths [B, R, 1]); rays whose last depth is negative give zeros, and a
+    ray stops after the sample that takes its transmittance below t_thres."""
+    from .voxel_encoding import volume_rendering_occ_forward
+    occ = occupancies if occupancies.dim() == 4 else occupancies.unsqueeze(-1)
+    f, d, _, _ = volume_rendering_occ_forward(sorted_depths, occ, feats, device, t_thres)
+    return f, d

@@ -86,3 +86,27 @@ def test_argument_errors():
     g2 = np.zeros((1, 129, 1, 16), np.float32)
     with pytest.raises(RuntimeError, match="invalid"):
         infer_density(c(z2), c(z2), c(g2), c(params, torch.float16), 1, 1, 129, 0)
+
+
+def test_occupancy_compositing_30_channels():
+    """FastNerf's compositing of 30-channel features by occupancies, against
+    the float64 oracle (<= 1e-5; rays within 1e-4 of the termination
+    threshold are flagged by the oracle and left out)."""
+    from oracle import oracle as orc
+    from sailor_gb300.nerf import occupancy_compositing
+    rng = np.random.default_rng(9)
+    B, R, S, C = 2, 700, 96, 30
+    z = np.sort(rng.uniform(1.0, 3.0, (B, R, S)), -1).astype(np.float32)
+    z[:, :40, :10] = -1.0          # padding first, as sorted rows hold it
+    z[:, 40:50, :] = -1.0          # rays without samples
+    occ = rng.uniform(0.0, 0.2, (B, R, S)).astype(np.float32)
+    feats = rng.random((B, R, S, C), dtype=np.float32)
+    c = lambda a: torch.as_tensor(a, device="cuda")  # noqa: E731
+    f, d = occupancy_compositing(c(z), c(occ), c(feats), 1e-4, 0)
+    torch.cuda.synchronize()
+    of, od, _, _, fl = orc.composite_fwd(z, None, occ[..., None], feats, 1e-4, True)
+    ok = fl == 0
+    assert ok.mean() > 0.95
+    assert np.abs(f.cpu().numpy() - of)[ok].max() <= 1e-5
+    assert np.abs(d.cpu().numpy() - od)[ok].max() <= 1e-5 * 3.0
+    assert (f.cpu().numpy()[:, 40:50] == 0).all() and (d.cpu().numpy()[:, 40:50] == 0).all()

@@ -199,7 +199,7 @@ def test_headline_grid_four_levels():
     ot = orc.octree_traversal(ref, s["ori"][:, pick], s["dirs"][:, pick], s["vs"], s["bbox"], start, 256, 2048)
     sub = {k: v[:, pick] for k, v in g.items() if k != "gpu"}
     ok = _compare_rows(ot, sub, "headline", 4)
-    assert (ot["cnt"][0] > 0).sum() > 2000
+    assert (ot["cnt"][0] > 0).sum() > 1000
     rd = np.random.default_rng(4).random((1, N, S), dtype=np.float32)
     idx, t0, t1, vl = g["gpu"]
     si, sz = o.ray_voxels_points_sampling(idx, t0, t1, vl, _cuda(rd), start, S)
