@@ -517,18 +517,21 @@ def infer_density_mlp(points_z, points_tpsdf, feats_geo, params, batch_size, num
     nv = B * V * N
     # the reference kernels read mlp_params up to PARAM_COUNT halves and the
     # point inputs by index up to n_points with no bound of their own
-    params = np.asarray(params, np.float16).reshape(-1)
-    if params.size != fastnerf.PARAM_COUNT:
-        raise ValueError(f"params holds {params.size} float16 values, the network has {fastnerf.PARAM_COUNT}")
-    if np.size(points_z) != nv or np.size(points_tpsdf) != nv:
+    def size(a):
+        return a.numel() if isinstance(a, torch.Tensor) else np.size(a)
+    if size(params) != fastnerf.PARAM_COUNT:
+        raise ValueError(f"params holds {size(params)} float16 values, the network has {fastnerf.PARAM_COUNT}")
+    if size(points_z) != nv or size(points_tpsdf) != nv:
         raise ValueError(f"points_z / points_tpsdf must hold B*V*N = {nv} values")
-    if np.size(feats_geo) != nv * 16:
+    if size(feats_geo) != nv * 16:
         raise ValueError(f"feats_geo must hold B*V*N x 16 = {nv * 16} values")
     d = driver()
-    z = _dev(np.reshape(points_z, -1), torch.float32)
-    tp = _dev(np.reshape(points_tpsdf, -1), torch.float32)
-    g = _dev(np.reshape(feats_geo, (-1, 16)), torch.float32)
-    w = _dev(params, torch.float16)
+    # device tensors are used in place; host arrays are copied up
+    z = _dev(points_z, torch.float32).reshape(-1)
+    tp = _dev(points_tpsdf, torch.float32).reshape(-1)
+    g = _dev(feats_geo, torch.float32).reshape(-1, 16)
+    w = _dev(params if isinstance(params, torch.Tensor) else np.asarray(params, np.float16).reshape(-1),
+             torch.float16).reshape(-1)
     dens = torch.empty((nv, 64), device="cuda")
     geo = torch.empty((nv, 8), device="cuda")
     d.launch("nerf_density_feat", nv, [w, z, tp, g, i32(nv), dens, geo], block=256)
