@@ -67,6 +67,12 @@ typedef struct SgTree {
   int *counts;            /* [2] {#top nodes, #bottom nodes}             */
   const float *voxel_size;/* [B]                                         */
   const float *vol_bbox;  /* [B,3,2] (min,max) per axis                  */
+  int *brick_box;         /* [B*6] or NULL: per frame the bounds of its  */
+                          /* kept bricks (lo x,y,z, hi x,y,z), written by */
+                          /* the build; the intersection then stops a ray */
+                          /* once its DDA has passed them on some axis    */
+                          /* (no node can follow), which leaves every     */
+                          /* output unchanged                             */
 } SgTree;
 
 /* 32-bit words per brick in SgTree.brick_mask: max(1, rate^3 / 32). */

@@ -36,7 +36,8 @@ class SgTree(C.Structure):
                 ("base_top", C.c_int), ("base_bot", C.c_int), ("cap_top", C.c_int), ("cap_bot", C.c_int),
                 ("brick_node", C.c_void_p), ("brick_mask", C.c_void_p), ("top_key", C.c_void_p),
                 ("top_child_base", C.c_void_p), ("bot_key", C.c_void_p), ("bot_parent", C.c_void_p),
-                ("counts", C.c_void_p), ("voxel_size", C.c_void_p), ("vol_bbox", C.c_void_p)]
+                ("counts", C.c_void_p), ("voxel_size", C.c_void_p), ("vol_bbox", C.c_void_p),
+                ("brick_box", C.c_void_p)]
 
 
 SG_MAX_LEVELS = 12

@@ -135,12 +135,13 @@ class BatchPipeline:
         self.bot_key = torch.empty(Vol, **i32)
         self.bot_parent = torch.empty(Vol, **i32)
         self.counts = torch.zeros(2, **i32)
+        self.brick_box = torch.empty(6 * B, **i32)
         self.scratch = torch.empty(int(N.lib.sg_tree_scratch_bytes(B, self.Dt)), dtype=torch.uint8, device=dev)
         self.status = torch.zeros(4, **i32)
         self.tree = N.SgTree(B, self.Dt, D, rate, Vol, 0, Vt, Vol, N.ptr(self.brick_node), N.ptr(self.brick_mask),
                              N.ptr(self.top_key), N.ptr(self.top_child_base), N.ptr(self.bot_key),
                              N.ptr(self.bot_parent), N.ptr(self.counts), N.ptr(self.voxel_size),
-                             N.ptr(self.vol_bbox))
+                             N.ptr(self.vol_bbox), N.ptr(self.brick_box))
         # rays and segments.  Targets are laid out grouped by the sample
         # capacity their S needs (32, 64 or 128 samples per ray), so each
         # group is one launch of the training kernel sized for it;

@@ -19,6 +19,10 @@
 // ray's row; the reference's -1 padding of the row tail is written by a
 // second, warp-per-row kernel with coalesced 16-byte stores.
 //
+// With the tree's kept-brick bounds (SgTree.brick_box) the walk stops once
+// it has passed them on an axis -- every later cell is empty, so the rows,
+// counts and valid lengths are those of the full walk.
+//
 // Isolated occupied bricks (no occupied neighbour, hence not nodes) are
 // treated as empty.  The reference instead looks up node index == the
 // brick's local id there, i.e. an unrelated node.
@@ -89,10 +93,27 @@ __global__ void __launch_bounds__(512) intersect_kernel(IsectParams p) {
       const int J = 4 * t.Dt;
       bool pre_empty = false, has_valid = false;
       int nsucc = 0, nint = 0;
+      // the frame's kept-brick bounds: cells outside hold no node, and once
+      // the walk has passed them on an axis no node can follow
+      int blo[3] = {0, 0, 0}, bhi[3] = {t.Dt - 1, t.Dt - 1, t.Dt - 1};
+      if (t.brick_box) {
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+          blo[a] = __ldg(t.brick_box + 6 * b + a);
+          bhi[a] = __ldg(t.brick_box + 6 * b + 3 + a);
+        }
+      }
       for (int j = 0; j < J; j++) {
         int rid = -1;
+        bool inside = true, past = false;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+          inside = inside && st[a] >= blo[a] && st[a] <= bhi[a];
+          past = past || (step[a] > 0 ? st[a] > bhi[a] : st[a] < blo[a]);
+        }
+        if (past) break;
         long brick = (long)b * vt + ((long)st[0] * t.Dt + st[1]) * t.Dt + st[2];
-        int k = t.brick_node[brick];
+        int k = inside ? t.brick_node[brick] : -1;
         if (k >= 0) {
           float p0, p1;
           if (slab(o, inv, node_coord(gt, bmin[0], st[0]), node_coord(gt, bmin[1], st[1]),

@@ -197,6 +197,8 @@ __global__ void tree_tile_scan_kernel(TreeScratch s, int ntiles, SgTree t, SgSta
     if (threadIdx.x == blockDim.x - 1) carry = make_int2(ex + v.x, ey + v.y);
     __syncthreads();
   }
+  if (t.brick_box)  // empty bounds (lo > hi) before the kept bricks widen them
+    for (int i = threadIdx.x; i < 6 * t.B; i += blockDim.x) t.brick_box[i] = (i % 6) < 3 ? t.Dt : -1;
   if (threadIdx.x == 0) {
     int nt = carry.x, nbt = carry.y;
     bool over = nt > t.cap_top || nbt > t.cap_bot;
@@ -246,6 +248,18 @@ __global__ void __launch_bounds__(256) tree_emit_top_kernel(SgTree t, int *occ_t
       t.top_key[k] = (int)i;
       t.top_child_base[k] = c;
       occ_top[i] = t.base_top + k;
+      if (t.brick_box) {
+        const int b = (int)(i / vt);
+        const long l = i - (long)b * vt;
+        const int x = (int)(l / ((long)t.Dt * t.Dt)), y = (int)((l / t.Dt) % t.Dt), z = (int)(l % t.Dt);
+        int *bx = t.brick_box + 6 * b;
+        atomicMin(bx + 0, x);
+        atomicMin(bx + 1, y);
+        atomicMin(bx + 2, z);
+        atomicMax(bx + 3, x);
+        atomicMax(bx + 4, y);
+        atomicMax(bx + 5, z);
+      }
     } else {
       t.brick_node[i] = -1;
     }
@@ -253,7 +267,6 @@ __global__ void __launch_bounds__(256) tree_emit_top_kernel(SgTree t, int *occ_t
     k += kk[j];
     c += cc[j];
   }
-  (void)vt;
 }
 
 // (4) warp per kept brick: bottom nodes in lexicographic child order

@@ -50,6 +50,7 @@ class FramePipeline:
         self.bot_key = torch.empty(V, **i32)
         self.bot_parent = torch.empty(V, **i32)
         self.counts = torch.zeros(2, **i32)
+        self.brick_box = torch.empty(6 * B, **i32)
         self.scratch = torch.empty(int(N.lib.sg_tree_scratch_bytes(B, self.Dt)), dtype=torch.uint8, device=dev)
         self.status = torch.zeros(4, **i32)
         R = B * n_rays
@@ -74,7 +75,8 @@ class FramePipeline:
         return N.SgTree(B, self.Dt, D, self.rate, B * D ** 3, 0, B * self.Dt ** 3, B * D ** 3,
                         self.brick_node.data_ptr(), self.brick_mask.data_ptr(), self.top_key.data_ptr(),
                         self.top_child_base.data_ptr(), self.bot_key.data_ptr(), self.bot_parent.data_ptr(),
-                        self.counts.data_ptr(), voxel_size.data_ptr(), vol_bbox.data_ptr())
+                        self.counts.data_ptr(), voxel_size.data_ptr(), vol_bbox.data_ptr(),
+                        self.brick_box.data_ptr())
 
     def _mark(self, name):
         if self.events is not None:

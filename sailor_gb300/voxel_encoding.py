@@ -295,14 +295,15 @@ class MultiLayerOctree:
                     brick_mask=torch.empty(B * Dt ** 3 * mw, **i32),
                     top_key=torch.empty(cap_top, **i32), top_child_base=torch.empty(cap_top, **i32),
                     bot_key=torch.empty(cap_bot, **i32), bot_parent=torch.empty(cap_bot, **i32),
-                    counts=torch.zeros(2, **i32),
+                    counts=torch.zeros(2, **i32), brick_box=torch.empty(6 * B, **i32),
                     scratch=torch.empty(int(N.lib.sg_tree_scratch_bytes(B, Dt)), dtype=torch.uint8, device=dev))
                 b = self._bufs
                 self._tree = N.SgTree(B, Dt, Db, self.rate, self._index[1], self._index[0], cap_top, cap_bot,
                                       b["brick_node"].data_ptr(), b["brick_mask"].data_ptr(),
                                       b["top_key"].data_ptr(), b["top_child_base"].data_ptr(),
                                       b["bot_key"].data_ptr(), b["bot_parent"].data_ptr(), b["counts"].data_ptr(),
-                                      self.voxel_size.data_ptr(), self.volume_bbox.data_ptr())
+                                      self.voxel_size.data_ptr(), self.volume_bbox.data_ptr(),
+                                      b["brick_box"].data_ptr())
             # multi-level node tables: one run per level, capacity = its occupied count
             caps = [max(c, 0) for c in self._totals]
             ob = dict(counts=torch.zeros(L, **i32))

@@ -191,6 +191,42 @@ def test_intersection_variants_identical(case, mode):
     assert (outs[0][0] >= 0).sum().item() > 100
 
 
+@pytest.mark.parametrize("mode", ["inference", "training", "early_stop", "opt_num"])
+def test_brick_box_exit_identical(case, mode):
+    """The walk that stops once it has passed the frame's kept-brick bounds
+    (SgTree.brick_box) gives the full walk's rows, counts, t-intervals,
+    valid lengths and status bit for bit; the bounds are the kept bricks'
+    coordinate extremes."""
+    g = case["g"]
+    octree = g["octree"]
+    args = dict(inference=(-1, False, -1), training=(-1, True, -1), early_stop=(2, False, -1),
+                opt_num=(-1, False, 3))[mode]
+    box = octree.tree_arrays()["brick_box"].cpu().numpy().reshape(-1, 6)
+    t = octree._tree
+    Dt = t.Dt
+    nt = octree.get_num_nodes_valid()[0]
+    keys = octree.tree_arrays()["top_key"][:nt].cpu().numpy().astype(np.int64)
+    fb, lin = keys // Dt ** 3, keys % Dt ** 3
+    xyz = np.stack([lin // (Dt * Dt), (lin // Dt) % Dt, lin % Dt], 1)
+    for b in range(box.shape[0]):
+        m = fb == b
+        assert np.array_equal(box[b, :3], xyz[m].min(0)) and np.array_equal(box[b, 3:], xyz[m].max(0))
+    outs = []
+    saved = t.brick_box
+    try:
+        for ptr in (saved, None):
+            t.brick_box = ptr
+            idx, t0, t1, vl = octree.voxel_traversal(_t(case["ori"]), _t(case["dirs"]), case["W"], 0, args[0],
+                                                     args[1], args[2])
+            torch.cuda.synchronize()
+            outs.append((idx.clone(), t0.clone(), t1.clone(), vl.clone(), octree._status.clone()))
+    finally:
+        t.brick_box = saved
+    for x, y in zip(*outs):
+        assert torch.equal(x, y)
+    assert (outs[0][0] >= 0).sum().item() > 100
+
+
 def test_rays_starting_inside(case):
     """Rays whose origin lies inside the volume (the whole-grid slab test
     clamps the entry to t = 0, so the walk starts in the origin's brick):
