@@ -60,6 +60,8 @@ _NAMES = {
     "rays_inverse": ("sampling_kernel", "14inverse_mat3x3IfE"),
     "rays": ("sampling_kernel", "23rays_calculating_kernelIfE"),
     "project": ("sampling_kernel", "11project_xyz"),
+    "trilerp_fwd": ("sampling_kernel", "35trilinear_aggregate_features_kernel"),
+    "trilerp_bwd": ("sampling_kernel", "44trilinear_aggregate_features_backward_kernel"),
     "gen_higher": ("octree_kernel", "23gen_higher_octree_nodes"),
     "octree_traversal": ("intersection_kernel", "20ray_octree_traversal"),
     "sampling_fine": ("sampling_kernel", "26ray_voxels_sampling_kernel"),
@@ -301,6 +303,31 @@ class Octree:
                                      i32(self.max_hits), i32(start_level), i32(2), self.voxel_size])
         torch.cuda.synchronize()
         return si, sd
+
+
+def trilerp_nodes(tree, ori, dirs, z, idx, feats, gout):
+    """trilinear_aggregate_features and its backward (sampling_kernel.cu:
+    162-327, host :1384-1462) on the tree's nodes.  Both kernels step
+    through the per-sample corner values with the stride MAX_LEAVES = 64
+    (octree.h:13) although the host hands them [B, C, N, S, 8] tensors;
+    here the values sit in the first 8 entries of [B, C, N, S, 64] blocks, so
+    every access stays inside the buffers.  feats [B, C, N, S, 8], gout
+    [B, C, N, S] -> (out [B, C, N, S], grad [B, C, N, S, 8])."""
+    d = driver()
+    o, dr = _dev(ori, torch.float32), _dev(dirs, torch.float32)
+    zt, it = _dev(z, torch.float32), _dev(idx, torch.int32)
+    f8 = _dev(feats, torch.float32)
+    B, C, N, S, _ = f8.shape
+    f64 = torch.zeros((B, C, N, S, 64), device="cuda")
+    f64[..., :8] = f8
+    go = _dev(gout, torch.float32)
+    out = torch.zeros((B, C, N, S), device="cuda")
+    gd = torch.zeros((B, C, N, S, 64), device="cuda")
+    n = B * N * S * C
+    d.launch("trilerp_fwd", n, [tree.nodes, o, dr, it, zt, f64, out, i32(B), i32(N), i32(S), i32(C)])
+    d.launch("trilerp_bwd", n, [tree.nodes, o, dr, it, zt, go, gd, i32(B), i32(N), i32(S), i32(C)])
+    torch.cuda.synchronize()
+    return out, gd[..., :8].contiguous()
 
 
 def merge_levels(occ0, rate, L):

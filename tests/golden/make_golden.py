@@ -10,16 +10,19 @@ It writes ``ref_chain_explicit.npz``, ``ref_chain_auto.npz``,
 ``ref_composite.npz``, ``ref_rays.npz`` and ``ref_project.npz`` (``--only rays`` or
 ``--only project``: that one alone; ``--only octree`` writes
 ``ref_octree.npz`` from the multi-level tree, its depth-first traversal
-and the fine sampler; ``--only density_mlp`` writes
+and the fine sampler; ``--only trilerp`` writes ``ref_trilerp.npz`` from the
+node-corner trilinear gather and its adjoint (run with inputs laid out at
+the kernels' own per-sample stride, so that they stay in bounds); ``--only density_mlp`` writes
 ``ref_density_mlp.npz`` from FastNerf's occupancy MLP, whose cubin
 ``oracle/build.py --fastnerf`` builds).  Each holds the seeded inputs
 and the reference outputs of fusion, coarse occupancy, the two-level tree
 (as canonical node keys, since the reference's node ids depend on atomic
 ordering), the voxel traversal, the coarse sampling, the sort, compositing
-forward/backward.  The reference's trilinear_aggregate_features kernels are
-not run: they step through their [B,C,N,S,8] input and gradient tensors
-with a per-sample stride of MAX_LEAVES = 64 (sampling_kernel.cu:210-213,
-272-275; octree.h:13) and so read and write past those tensors.  The committed
+forward/backward.  The reference's trilinear_aggregate_features kernels step
+through their [B,C,N,S,8] input and gradient tensors with a per-sample
+stride of MAX_LEAVES = 64 (sampling_kernel.cu:210-213, 272-275; octree.h:13),
+past the end of those tensors; ``--only trilerp`` runs them on [B,C,N,S,64]
+buffers holding the 8 values at the start of each block.  The committed
 copies under tests/golden/ pin the CPU oracle in the CPU test suite.
 """
 import argparse
@@ -272,10 +275,44 @@ def octree(out_dir):
     print("octree done, seed", seed, flush=True)
 
 
+def trilerp(out_dir):
+    """The node-corner trilinear gather and its adjoint (trilinear_aggregate_
+    features(_backward)) on the reference's own two-level tree and coarse
+    samples (64^3, rate 4), 128 rays with hits, 2 channels -> ref_trilerp.npz
+    with each sample's node corners from the reference's node array."""
+    scene = syn.make_scene(seed=11, n_views=VIEWS, res=RES, n_prims=PRIMS, D=D, trunc=0.03)
+    ori, dirs = syn.target_rays(seed=11, res=TRES)
+    f = rc.integrate(scene["K"], scene["RT"], scene["colors"], scene["depths"], D, 1.0, 0.025,
+                     scene["trunc_weight"], 13.5, 13.5, vol_bbox=scene["vol_bbox"], voxel_size=scene["voxel_size"])
+    occ1, cnt1 = rc.build_multi_res_volumes(f["occ"], f["count"], RATE)
+    tree = rc.Octree(f["occ"], occ1, f["count"], cnt1, f["voxel_size"], f["vol_bbox"], RATE)
+    W = 4 * tree.Dt * (RATE ** 3 + 1)
+    idx, t0, t1, vl, q = tree.voxel_traversal(ori, dirs, W)
+    rands = np.full((1, ori.shape[1], S), 0.5, np.float32)
+    si, sd = tree.sample_coarse(idx, t0, t1, rands, vl, S)
+    hit = np.flatnonzero((si.cpu().numpy()[0] >= 0).sum(1) >= S // 2)
+    pick = np.random.default_rng(3).choice(hit, 128, replace=False)
+    pick.sort()
+    o, dr = ori[:, pick], dirs[:, pick]
+    z, ix = sd[:, pick].contiguous(), si[:, pick].contiguous()
+    rng = np.random.default_rng(4)
+    C = 2
+    feats = rng.normal(size=(1, C, 128, S, 8)).astype(np.float32)
+    gout = rng.normal(size=(1, C, 128, S)).astype(np.float32)
+    out, grad = rc.trilerp_nodes(tree, o, dr, z, ix, feats, gout)
+    table = tree.node_table()
+    ixn = ix.cpu().numpy()
+    corners = table["corners"][np.where(ixn >= 0, ixn, 0)]
+    np.savez_compressed(os.path.join(out_dir, "ref_trilerp.npz"), ori=o, dirs=dr, sampled_z=z.cpu().numpy(),
+                        valid=(ixn >= 0).astype(np.int8), corners=corners.astype(np.float32), feats=feats, gout=gout,
+                        out=out.cpu().numpy(), grad=grad.cpu().numpy())
+    print("trilerp done", flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
-    ap.add_argument("--only", choices=["rays", "project", "density_mlp", "octree"])
+    ap.add_argument("--only", choices=["rays", "project", "density_mlp", "octree", "trilerp"])
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
     if args.only == "density_mlp":
@@ -284,6 +321,10 @@ def main():
     if args.only == "octree":
         assert rc.available(), "reference cubins or GPU missing"
         octree(args.out)
+        return
+    if args.only == "trilerp":
+        assert rc.available(), "reference cubins or GPU missing"
+        trilerp(args.out)
         return
     assert rc.available(), "reference cubins or GPU missing"
     if args.only == "project":

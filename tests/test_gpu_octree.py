@@ -31,11 +31,11 @@ def _cuda(a, dt=torch.float32):
     return torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device="cuda")
 
 
-def _scene(D, res, n_views, tres, seed):
-    sc = syn.make_scene(seed=seed, n_views=n_views, res=res, n_prims=10, D=D, trunc=0.03)
+def _scene(D, res, n_views, tres, seed, batch=1):
+    sc = syn.make_scene(seed=seed, n_views=n_views, res=res, n_prims=10, D=D, trunc=0.03, batch=batch)
     fz = orc.integrate(sc["K"], sc["RT"], sc["colors"], sc["depths"], D, sc["vol_bbox"], sc["voxel_size"], 1.0,
                        sc["trunc_weight"], 13.5, 13.5)
-    ori, dirs = syn.target_rays(seed=seed, res=tres)
+    ori, dirs = syn.target_rays(seed=seed, res=tres, batch=batch)
     return dict(sc=sc, occ=fz["occ"], ori=ori, dirs=dirs, vs=sc["voxel_size"].reshape(-1).astype(np.float32),
                 bbox=sc["vol_bbox"].astype(np.float32))
 
@@ -207,3 +207,30 @@ def test_headline_grid_four_levels():
                                 start)
     assert np.array_equal(si.cpu().numpy()[:, pick], ri) and np.array_equal(sz.cpu().numpy()[:, pick], rz)
     del ok
+
+
+def test_two_frames():
+    """Two frames in one tree (node keys carry the frame): build, traversal
+    from the top and from the middle level, and fine sampling against the
+    oracle."""
+    s = _scene(64, 128, 4, 48, 9, batch=2)
+    o, gv, ref = _trees(s, 2, 3)
+    for l in range(3):
+        assert np.array_equal(gv[l].cpu().numpy(), ref["vols"][l])
+    for start in (0, 1):
+        sl = 2 - start
+        Wc = 4 * int(ref["dims"][sl])
+        g = _gpu_rows(o, s, start, Wc, 2048)
+        ot = orc.octree_traversal(ref, s["ori"], s["dirs"], s["vs"], s["bbox"], start, Wc, 2048)
+        for b in range(2):
+            sub_g = {k: v[b:b + 1] for k, v in g.items() if k != "gpu"}
+            sub_o = dict(ot, **{k: ot[k][b:b + 1] for k in ("idx", "t0", "t1", "idx_c", "t0_c", "t1_c", "valid_len",
+                                                             "flags", "cnt")})
+            _compare_rows(sub_o, sub_g, ("two frames", start, b), 2 ** sl)
+        idx, t0, t1, vl = g["gpu"]
+        S = 48
+        rd = np.random.default_rng(3).random((2, s["ori"].shape[1], S), dtype=np.float32)
+        si, sz = o.ray_voxels_points_sampling(idx, t0, t1, vl, _cuda(rd), start, S)
+        ri, rz, _ = orc.sample_fine(ref, g["idx"], g["t0"], g["t1"], g["valid_len"], rd, s["vs"], S, start)
+        assert np.array_equal(si.cpu().numpy(), ri) and np.array_equal(sz.cpu().numpy(), rz)
+        assert (g["idx"][1] >= 0).sum() > 100  # the second frame's rays hit its own tree

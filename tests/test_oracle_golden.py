@@ -8,11 +8,14 @@ keys.  The oracle uses a correctly rounded reciprocal where the reference
 uses __fdividef; rays the oracle flags as near-ties are excluded from the
 bit-exact hit comparisons, and t-intervals are compared within 1e-5.
 """
+import os
+
 import numpy as np
 import pytest
 
 from oracle import oracle as orc
 
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CHAINS = ["explicit", "auto"]
 
 
@@ -242,3 +245,35 @@ def test_grid_sample_restatement_vs_torch():
     ref = F.grid_sample(torch.tensor(img), torch.tensor(grid)[:, :, None, :], align_corners=True,
                         mode="bilinear")[..., 0].permute(0, 2, 1).numpy()
     assert np.abs(orc.grid_sample(img, grid) - ref).max() <= 1e-12
+
+
+def test_trilerp_nodes_against_reference_golden():
+    """Pin of the node-corner trilinear gather and its adjoint
+    (trilinear_aggregate_features(_backward), sampling_kernel.cu:162-327):
+    the reference's kernels, run on its own two-level tree and coarse samples
+    (tests/golden/ref_trilerp.npz, inputs at the kernels' per-sample stride
+    of 64 so that they stay in bounds), against the oracle's float64
+    restatement on the same node corners and sample points (the kernels'
+    fused multiply-add point): outputs and gradients within 2e-5 relative to
+    the values' scale (the reference forms its fractions in float32)."""
+    path = os.path.join(GOLDEN, "ref_trilerp.npz")
+    if not os.path.exists(path):
+        pytest.skip("ref_trilerp.npz not generated (tests/golden/make_golden.py --only trilerp)")
+    g = np.load(path)
+    B, C, R, S, _ = g["feats"].shape
+    pts = orc.sample_points(g["ori"][0], g["dirs"][0], g["sampled_z"][0]).reshape(-1, 3)
+    valid = g["valid"].reshape(-1).astype(np.int32)
+    assert valid.mean() > 0.5
+    corners = g["corners"].reshape(-1, 8, 3)
+    fo = g["feats"].transpose(1, 0, 2, 3, 4).reshape(C, -1, 8)
+    go = g["gout"].transpose(1, 0, 2, 3).reshape(C, -1)
+    ro, rg = orc.trilerp_nodes(pts, corners, valid, fo, go)
+    ro = ro.reshape(C, B, R, S).transpose(1, 0, 2, 3)
+    rg = rg.reshape(C, B, R, S, 8).transpose(1, 0, 2, 3, 4)
+    scale_o = np.abs(g["out"]).max()
+    scale_g = np.abs(g["grad"]).max()
+    assert np.abs(ro - g["out"]).max() <= 2e-5 * scale_o
+    assert np.abs(rg - g["grad"]).max() <= 2e-5 * scale_g
+    # samples without a node: zeros in both
+    inv = ~valid.astype(bool).reshape(B, R, S)
+    assert np.all(g["out"][:, :, inv[0]] == 0) and np.all(ro[:, :, inv[0]] == 0)
