@@ -594,11 +594,14 @@ def test_pipeline_matches_oracle():
     mine = np.where(node >= D ** 3, node - D ** 3 + t["base_top"], node)
     assert np.array_equal(np.sort(mine[ok], 1), np.sort(ref_nodes[ok], 1))
     # fields and compositing against the oracle on the same sorted samples
-    pts = (ori[0][:, None, :] + dirs[0][:, None, :] * np.maximum(z, 0)[..., None]).reshape(-1, 3)
+    # the sample points as the kernels form them (fused multiply-add)
+    pts = orc.sample_points(ori[0], dirs[0], np.maximum(z, 0)).reshape(-1, 3)
     tsdf = orc.grid_gather(pts, ref["fusion"]["tsdf"][..., None], sc["vol_bbox"][:, :, 0], sc["voxel_size"][:, 0])
     sig = 1.0 / (1.0 + np.exp(tsdf[:, 0] * trunc_m / 0.005)) / 0.005
     sig = np.where(z.reshape(-1) >= 0, sig, 0).reshape(R, S)
-    assert np.abs(pipe.sigma.cpu().numpy() - sig).max() <= 1e-3 * 200  # sigma <= 200, float gather
+    # sigma <= 200 and steep in the TSDF (slope up to 6 / 0.005^2 / 4 per unit
+    # TSDF): float32 gather and exp against float64
+    assert np.abs(pipe.sigma.cpu().numpy() - sig).max() <= 5e-3
     col = orc.grid_gather(pts, cgrid, cbb[:, :, 0], cvs[:, 0]).reshape(R, S, 3)
     col = np.where(z[..., None] >= 0, col, 0)
     assert np.abs(pipe.rgb.cpu().numpy() - col).max() <= 1e-5

@@ -254,8 +254,9 @@ def test_trilerp_nodes_against_reference_golden():
     (tests/golden/ref_trilerp.npz, inputs at the kernels' per-sample stride
     of 64 so that they stay in bounds), against the oracle's float64
     restatement on the same node corners and sample points (the kernels'
-    fused multiply-add point): outputs and gradients within 2e-5 relative to
-    the values' scale (the reference forms its fractions in float32)."""
+    fused multiply-add point): outputs and gradients within 1e-6 relative to
+    the values' scale (the reference forms its fractions in float32; the
+    measured gap is 1e-7 and 2e-7)."""
     path = os.path.join(GOLDEN, "ref_trilerp.npz")
     if not os.path.exists(path):
         pytest.skip("ref_trilerp.npz not generated (tests/golden/make_golden.py --only trilerp)")
@@ -272,8 +273,8 @@ def test_trilerp_nodes_against_reference_golden():
     rg = rg.reshape(C, B, R, S, 8).transpose(1, 0, 2, 3, 4)
     scale_o = np.abs(g["out"]).max()
     scale_g = np.abs(g["grad"]).max()
-    assert np.abs(ro - g["out"]).max() <= 2e-5 * scale_o
-    assert np.abs(rg - g["grad"]).max() <= 2e-5 * scale_g
+    assert np.abs(ro - g["out"]).max() <= 1e-6 * scale_o
+    assert np.abs(rg - g["grad"]).max() <= 1e-6 * scale_g
     # samples without a node: zeros in both
     inv = ~valid.astype(bool).reshape(B, R, S)
     assert np.all(g["out"][:, :, inv[0]] == 0) and np.all(ro[:, :, inv[0]] == 0)
