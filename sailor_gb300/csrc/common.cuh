@@ -192,6 +192,35 @@ int tune(int knob);
 // are multiples of it.
 int num_sms();
 
+// -1 padding of one hit row's tail [c, W) by the calling warp: scalar
+// stores up to a 4-element boundary, then 16-byte stores.  base = the row's
+// first element (row index x W).
+__device__ __forceinline__ void pad_row_tail(int *idx, float *t0, float *t1, size_t base, int c, int W, int lane) {
+  int head = c;
+  while (head < W && ((base + head) & 3)) {
+    if (lane == 0) {
+      idx[base + head] = -1;
+      t0[base + head] = -1.0f;
+      t1[base + head] = -1.0f;
+    }
+    head++;
+  }
+  const int nvec = (W - head) / 4;
+  const int4 mi = make_int4(-1, -1, -1, -1);
+  const float4 mf = make_float4(-1.f, -1.f, -1.f, -1.f);
+  for (int q = lane; q < nvec; q += 32) {
+    const size_t o = base + head + 4 * q;
+    *reinterpret_cast<int4 *>(idx + o) = mi;
+    *reinterpret_cast<float4 *>(t0 + o) = mf;
+    *reinterpret_cast<float4 *>(t1 + o) = mf;
+  }
+  for (int q = head + 4 * nvec + lane; q < W; q += 32) {
+    idx[base + q] = -1;
+    t0[base + q] = -1.0f;
+    t1[base + q] = -1.0f;
+  }
+}
+
 // -1 padding of hit-row tails [count[r], W) of R rows (a warp per row, 16-byte
 // stores where the row is aligned); defined in intersect.cu
 void launch_pad_rows(long R, int W, const int *count, int *idx, float *t0, float *t1, sg_stream_t stream);

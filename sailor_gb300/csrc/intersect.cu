@@ -461,32 +461,7 @@ __global__ void pad_rows_kernel(long R, int W, const int *__restrict__ count, in
   const int lane = lane_id();
   for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < R;
        r += ((long)gridDim.x * blockDim.x) >> 5) {
-    int c = min(count[r], W);
-    size_t base = (size_t)r * W;
-    // scalar head up to a 4-element boundary, then 16-byte stores
-    int head = c;
-    while (head < W && ((base + head) & 3)) {
-      if (lane == 0) {
-        idx[base + head] = -1;
-        t0[base + head] = -1.0f;
-        t1[base + head] = -1.0f;
-      }
-      head++;
-    }
-    int nvec = (W - head) / 4;
-    int4 mi = make_int4(-1, -1, -1, -1);
-    float4 mf = make_float4(-1.f, -1.f, -1.f, -1.f);
-    for (int q = lane; q < nvec; q += 32) {
-      size_t o = base + head + 4 * q;
-      *reinterpret_cast<int4 *>(idx + o) = mi;
-      *reinterpret_cast<float4 *>(t0 + o) = mf;
-      *reinterpret_cast<float4 *>(t1 + o) = mf;
-    }
-    for (int q = head + 4 * nvec + lane; q < W; q += 32) {
-      idx[base + q] = -1;
-      t0[base + q] = -1.0f;
-      t1[base + q] = -1.0f;
-    }
+    pad_row_tail(idx, t0, t1, (size_t)r * W, min(count[r], W), W, lane);
   }
 }
 

@@ -43,6 +43,8 @@ namespace sg {
 struct OctMeta {
   int L;
   int dim[SG_MAX_LEVELS], base[SG_MAX_LEVELS], cap[SG_MAX_LEVELS], count[SG_MAX_LEVELS];
+  int shift[SG_MAX_LEVELS];   // log2(dim) where dim is a power of two, else -1
+  float size[SG_MAX_LEVELS];  // fine voxels per node edge, dim[0] / dim[l]
   const int *vol[SG_MAX_LEVELS], *key[SG_MAX_LEVELS], *child_base[SG_MAX_LEVELS], *nchild[SG_MAX_LEVELS];
 };
 
@@ -59,6 +61,9 @@ __device__ __forceinline__ void load_meta(const SgOctree &t, OctMeta &m) {
       m.child_base[l] = t.child_base[l];
       m.nchild[l] = t.nchild[l];
       m.count[l] = (l < t.L && t.counts) ? min(t.counts[l], t.cap[l]) : 0;
+      const int D = t.dim[l];
+      m.shift[l] = (D > 0 && (D & (D - 1)) == 0) ? __ffs(D) - 1 : -1;
+      m.size[l] = D > 0 ? (float)(t.dim[0] / D) : 0.0f;
     }
   }
 }
@@ -69,13 +74,33 @@ __device__ __forceinline__ int meta_level_of(const OctMeta &m, int id) {
   return -1;
 }
 
-__device__ __forceinline__ void decode_key(long key, int D, int &b, int &x, int &y, int &z) {
-  const long v = (long)D * D * D;
-  b = (int)(key / v);
-  const long l = key - (long)b * v;
-  x = (int)(l / ((long)D * D));
-  y = (int)((l / D) % D);
-  z = (int)(l % D);
+// key = b * D^3 + (x * D + y) * D + z, 0 <= key < 2^31 (the volume sizes
+// are checked on the host): 32-bit unsigned arithmetic
+__device__ __forceinline__ void decode_key(int key, int D, int &b, int &x, int &y, int &z) {
+  const unsigned u = (unsigned)key, d = (unsigned)D, d2 = d * d;
+  const unsigned bu = u / (d2 * d);
+  const unsigned l = u - bu * d2 * d;
+  const unsigned xu = l / d2, rem = l - xu * d2;
+  const unsigned yu = rem / d;
+  b = (int)bu;
+  x = (int)xu;
+  y = (int)yu;
+  z = (int)(rem - yu * d);
+}
+
+// the same for a node of level lv: shifts and masks where the level's
+// edge is a power of two
+__device__ __forceinline__ void decode_node(const OctMeta &m, int lv, int key, int &x, int &y, int &z) {
+  const int sh = m.shift[lv];
+  if (sh >= 0) {
+    const unsigned u = (unsigned)key, mask = (1u << sh) - 1u;
+    z = (int)(u & mask);
+    y = (int)((u >> sh) & mask);
+    x = (int)((u >> (2 * sh)) & mask);
+  } else {
+    int b;
+    decode_key(key, m.dim[lv], b, x, y, z);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -217,173 +242,196 @@ struct OctTravParams {
 
 // node edge of level l in frame b's metres
 __device__ __forceinline__ float level_edge(const OctMeta &m, float vs, int l) {
-  return vs * (float)(m.dim[0] / m.dim[l > 0 ? l : 0]);
+  return vs * m.size[l > 0 ? l : 0];
 }
 
-__global__ void __launch_bounds__(128) octree_traverse_kernel(OctTravParams p) {
+constexpr int kTravThreads = 128;
+
+__global__ void __launch_bounds__(kTravThreads) octree_traverse_kernel(OctTravParams p) {
   __shared__ OctMeta m;
+  // the ray's frame's node geometry per level (edge, offset), one column
+  // per thread: set once per ray instead of once per tested node
+  __shared__ float g_vs[SG_MAX_LEVELS][kTravThreads], g_st[SG_MAX_LEVELS][kTravThreads];
   load_meta(p.t, m);
   __syncthreads();
   const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= p.R) return;
-  const SgOctree &t = p.t;
-  const int b = (int)(r / p.N);
+  const int tid = threadIdx.x;
   const int s = p.s;
-  const int Ds = m.dim[s];
-  const float *bb = t.vol_bbox + 6 * b;
-  const float bmin[3] = {bb[0], bb[2], bb[4]};
-  const float xc = (bb[0] + bb[1]) / 2.0f, yc = (bb[2] + bb[3]) / 2.0f, zc = (bb[4] + bb[5]) / 2.0f;
-  const float vs = t.voxel_size[b];
-  const float vs_top = vs * (float)(m.dim[0] / Ds);
-  const float bst[3] = {bb[0] - vs / 2.0f, bb[2] - vs / 2.0f, bb[4] - vs / 2.0f};
-  const float o[3] = {p.ori[r * 3 + 0], p.ori[r * 3 + 1], p.ori[r * 3 + 2]};
-  const float d[3] = {p.dir[r * 3 + 0], p.dir[r * 3 + 1], p.dir[r * 3 + 2]};
-  const float inv[3] = {__fdividef(1.0f, d[0]), __fdividef(1.0f, d[1]), __fdividef(1.0f, d[2])};
-  const LevelGeom gs = level_geom(vs, m.dim[0] / Ds);
-  const long vt = (long)Ds * Ds * Ds;
-  const int *vol_s = m.vol[s], *key_s = m.key[s];
-  int *oic = p.idx_c + (size_t)r * p.Wc;
-  float *o0c = p.t0_c + (size_t)r * p.Wc, *o1c = p.t1_c + (size_t)r * p.Wc;
-  int *oif = p.idx + (size_t)r * p.Wf;
-  float *o0f = p.t0 + (size_t)r * p.Wf, *o1f = p.t1 + (size_t)r * p.Wf;
   int cc = 0, fc = 0;
-  float vlen = 0.0f;
-  float T0, T1;
-  if (slab(o, inv, xc, yc, zc, vs_top * (float)Ds, T0, T1) && !(T0 < 0.0f || T1 < 0.0f)) {
-    float so[3];
-    int st[3];
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-      float sp = __fmaf_rn(T0, d[a], o[a]);
-      so[a] = sp - bst[a];
-      int q = (int)(so[a] / vs_top);
-      q = q < 0 ? 0 : q;
-      st[a] = q < Ds ? q : Ds - 1;
+  if (r < p.R) {
+    const SgOctree &t = p.t;
+    const int b = (int)(r / p.N);
+    const int Ds = m.dim[s];
+    const float *bb = t.vol_bbox + 6 * b;
+    const float bmin[3] = {bb[0], bb[2], bb[4]};
+    const float xc = (bb[0] + bb[1]) / 2.0f, yc = (bb[2] + bb[3]) / 2.0f, zc = (bb[4] + bb[5]) / 2.0f;
+    const float vs = t.voxel_size[b];
+    const float vs_top = vs * (float)(m.dim[0] / Ds);
+    const float bst[3] = {bb[0] - vs / 2.0f, bb[2] - vs / 2.0f, bb[4] - vs / 2.0f};
+    const float o[3] = {p.ori[r * 3 + 0], p.ori[r * 3 + 1], p.ori[r * 3 + 2]};
+    const float d[3] = {p.dir[r * 3 + 0], p.dir[r * 3 + 1], p.dir[r * 3 + 2]};
+    const float inv[3] = {__fdividef(1.0f, d[0]), __fdividef(1.0f, d[1]), __fdividef(1.0f, d[2])};
+    const LevelGeom gs = level_geom(vs, m.dim[0] / Ds);
+    for (int l = 0; l < s; l++) {
+      const LevelGeom g = level_geom(vs, m.dim[0] / m.dim[l]);
+      g_vs[l][tid] = g.vs;
+      g_st[l][tid] = g.start;
     }
-    float step[3], tm[3], td[3];
+    const long vt = (long)Ds * Ds * Ds;
+    const int *vol_s = m.vol[s], *key_s = m.key[s];
+    int *oic = p.idx_c + (size_t)r * p.Wc;
+    float *o0c = p.t0_c + (size_t)r * p.Wc, *o1c = p.t1_c + (size_t)r * p.Wc;
+    int *oif = p.idx + (size_t)r * p.Wf;
+    float *o0f = p.t0 + (size_t)r * p.Wf, *o1f = p.t1 + (size_t)r * p.Wf;
+    float vlen = 0.0f;
+    float T0, T1;
+    if (slab(o, inv, xc, yc, zc, vs_top * (float)Ds, T0, T1) && !(T0 < 0.0f || T1 < 0.0f)) {
+      float so[3];
+      int st[3];
 #pragma unroll
-    for (int a = 0; a < 3; a++) {
-      step[a] = (d[a] >= 0) ? 1.0f : -1.0f;
-      float nb = (step[a] > 0) ? ((float)st[a] + step[a]) * vs_top : (float)st[a] * vs_top;
-      tm[a] = (d[a] != 0) ? (nb - so[a]) / d[a] : 9999999.0f;
-      td[a] = (d[a] != 0) ? vs_top / d[a] * step[a] : 9999999.0f;
-    }
-    const int J = 4 * Ds;
-    bool pre_empty = false, has_valid = false;
-    int nsucc = 0, nint = 0;
-    int cbs[SG_MAX_LEVELS], cur[SG_MAX_LEVELS];
-    for (int j = 0; j < J; j++) {
-      int rid = -1;
-      const long cell = (long)b * vt + ((long)st[0] * Ds + st[1]) * Ds + st[2];
-      const int v = vol_s[cell];
-      const int k0 = v - m.base[s];
-      if (v > -1 && k0 >= 0 && k0 < m.count[s] && key_s[k0] == (int)cell) {
-        float p0, p1;
-        if (slab(o, inv, node_coord(gs, bmin[0], st[0]), node_coord(gs, bmin[1], st[1]),
-                 node_coord(gs, bmin[2], st[2]), gs.vs, p0, p1) &&
-            !(p0 < 0.0f || p1 < 0.0f)) {
-          rid = cc;
-          if (cc < p.Wc) {
-            oic[cc] = v;
-            o0c[cc] = p0;
-            o1c[cc] = p1;
-          }
-          cc++;
-          // descent from this coarse node
-          const int f0 = fc;
-          if (fc < p.Wf) {
-            oif[fc] = v;
-            o0f[fc] = p0;
-            o1f[fc] = p1;
-          }
-          fc++;
-          int depth = -1;
-          if (s > 0 && m.nchild[s][k0] > 0) {
-            depth = 0;
-            cbs[0] = m.child_base[s][k0];
-            cur[0] = m.nchild[s][k0] - 1;
-          }
-          while (depth >= 0) {
-            if (cur[depth] < 0) {
-              depth--;
-              continue;
+      for (int a = 0; a < 3; a++) {
+        float sp = __fmaf_rn(T0, d[a], o[a]);
+        so[a] = sp - bst[a];
+        int q = (int)(so[a] / vs_top);
+        q = q < 0 ? 0 : q;
+        st[a] = q < Ds ? q : Ds - 1;
+      }
+      float step[3], tm[3], td[3];
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        step[a] = (d[a] >= 0) ? 1.0f : -1.0f;
+        float nb = (step[a] > 0) ? ((float)st[a] + step[a]) * vs_top : (float)st[a] * vs_top;
+        tm[a] = (d[a] != 0) ? (nb - so[a]) / d[a] : 9999999.0f;
+        td[a] = (d[a] != 0) ? vs_top / d[a] * step[a] : 9999999.0f;
+      }
+      const int J = 4 * Ds;
+      bool pre_empty = false, has_valid = false;
+      int nsucc = 0, nint = 0;
+      int cbs[SG_MAX_LEVELS], cur[SG_MAX_LEVELS];
+      for (int j = 0; j < J; j++) {
+        int rid = -1;
+        const long cell = (long)b * vt + ((long)st[0] * Ds + st[1]) * Ds + st[2];
+        const int v = vol_s[cell];
+        const int k0 = v - m.base[s];
+        if (v > -1 && k0 >= 0 && k0 < m.count[s] && key_s[k0] == (int)cell) {
+          float p0, p1;
+          if (slab(o, inv, node_coord(gs, bmin[0], st[0]), node_coord(gs, bmin[1], st[1]),
+                   node_coord(gs, bmin[2], st[2]), gs.vs, p0, p1) &&
+              !(p0 < 0.0f || p1 < 0.0f)) {
+            rid = cc;
+            if (cc < p.Wc) {
+              oic[cc] = v;
+              o0c[cc] = p0;
+              o1c[cc] = p1;
             }
-            const int lv = s - 1 - depth;
-            const int kk = cbs[depth] + cur[depth];
-            cur[depth]--;
-            if (kk >= m.count[lv]) continue;  // a level past its capacity (flagged by the build)
-            int cb_, cx, cy, cz;
-            decode_key(m.key[lv][kk], m.dim[lv], cb_, cx, cy, cz);
-            const LevelGeom gl = level_geom(vs, m.dim[0] / m.dim[lv]);
-            float c0, c1;
-            if (!slab(o, inv, node_coord(gl, bmin[0], cx), node_coord(gl, bmin[1], cy), node_coord(gl, bmin[2], cz),
-                      gl.vs, c0, c1))
-              continue;
-            const int cid = m.base[lv] + kk;
-            bool found = false;
+            cc++;
+            // descent from this coarse node
+            const int f0 = fc;
+            if (fc < p.Wf) {
+              oif[fc] = v;
+              o0f[fc] = p0;
+              o1f[fc] = p1;
+            }
+            fc++;
+            int depth = -1;
+            if (s > 0 && m.nchild[s][k0] > 0) {
+              depth = 0;
+              cbs[0] = m.child_base[s][k0];
+              cur[0] = m.nchild[s][k0] - 1;
+            }
+            while (depth >= 0) {
+              if (cur[depth] < 0) {
+                depth--;
+                continue;
+              }
+              const int lv = s - 1 - depth;
+              const int kk = cbs[depth] + cur[depth];
+              cur[depth]--;
+              if (kk >= m.count[lv]) continue;  // a level past its capacity (flagged by the build)
+              int cx, cy, cz;
+              decode_node(m, lv, m.key[lv][kk], cx, cy, cz);
+              const LevelGeom gl{g_vs[lv][tid], g_st[lv][tid]};
+              float c0, c1;
+              if (!slab(o, inv, node_coord(gl, bmin[0], cx), node_coord(gl, bmin[1], cy),
+                        node_coord(gl, bmin[2], cz), gl.vs, c0, c1))
+                continue;
+              const int cid = m.base[lv] + kk;
+              bool found = false;
+              const int fe = min(fc, p.Wf);
+              for (int e = f0; e < fe; e++) {
+                if (o0f[e] == c0 && o1f[e] == c1) {
+                  const int pid = oif[e];
+                  if (level_edge(m, vs, meta_level_of(m, pid)) > gl.vs) oif[e] = cid;
+                  found = true;
+                  break;
+                }
+              }
+              if (!found) {
+                if (fc < p.Wf) {
+                  oif[fc] = cid;
+                  o0f[fc] = c0;
+                  o1f[fc] = c1;
+                }
+                fc++;
+              }
+              if (lv > 0) {
+                const int nc = m.nchild[lv][kk];
+                if (nc > 0) {
+                  depth++;
+                  cbs[depth] = m.child_base[lv][kk];
+                  cur[depth] = nc - 1;
+                }
+              }
+            }
             const int fe = min(fc, p.Wf);
             for (int e = f0; e < fe; e++) {
-              if (o0f[e] == c0 && o1f[e] == c1) {
-                const int pid = oif[e];
-                if (level_edge(m, vs, meta_level_of(m, pid)) > gl.vs) oif[e] = cid;
-                found = true;
-                break;
-              }
-            }
-            if (!found) {
-              if (fc < p.Wf) {
-                oif[fc] = cid;
-                o0f[fc] = c0;
-                o1f[fc] = c1;
-              }
-              fc++;
-            }
-            if (lv > 0) {
-              const int nc = m.nchild[lv][kk];
-              if (nc > 0) {
-                depth++;
-                cbs[depth] = m.child_base[lv][kk];
-                cur[depth] = nc - 1;
-              }
+              const float scale = gs.vs / level_edge(m, vs, meta_level_of(m, oif[e]));
+              vlen = vlen + (o1f[e] - o0f[e]) * scale;
             }
           }
-          const int fe = min(fc, p.Wf);
-          for (int e = f0; e < fe; e++) {
-            const float scale = gs.vs / level_edge(m, vs, meta_level_of(m, oif[e]));
-            vlen = vlen + (o1f[e] - o0f[e]) * scale;
+        }
+        if (p.th_early_stop > -1) {
+          if (rid == -1) {
+            if (pre_empty && has_valid) nsucc++;
+            pre_empty = true;
+          } else {
+            nsucc = 0;
+            pre_empty = false;
+            has_valid = true;
           }
+          if ((nsucc + 1) >= p.th_early_stop) break;
         }
-      }
-      if (p.th_early_stop > -1) {
-        if (rid == -1) {
-          if (pre_empty && has_valid) nsucc++;
-          pre_empty = true;
-        } else {
-          nsucc = 0;
-          pre_empty = false;
-          has_valid = true;
+        if (p.opt_num > -1) {
+          if (rid + 1 > 0) nint++;
+          if (nint >= p.opt_num) break;
         }
-        if ((nsucc + 1) >= p.th_early_stop) break;
+        int ax;
+        if (tm[0] < tm[1]) ax = (tm[0] < tm[2]) ? 0 : 2;
+        else ax = (tm[1] < tm[2]) ? 1 : 2;
+        st[ax] += (int)step[ax];
+        tm[ax] += td[ax];
+        if (st[0] < 0 || st[0] >= Ds || st[1] < 0 || st[1] >= Ds || st[2] < 0 || st[2] >= Ds) break;
       }
-      if (p.opt_num > -1) {
-        if (rid + 1 > 0) nint++;
-        if (nint >= p.opt_num) break;
-      }
-      int ax;
-      if (tm[0] < tm[1]) ax = (tm[0] < tm[2]) ? 0 : 2;
-      else ax = (tm[1] < tm[2]) ? 1 : 2;
-      st[ax] += (int)step[ax];
-      tm[ax] += td[ax];
-      if (st[0] < 0 || st[0] >= Ds || st[1] < 0 || st[1] >= Ds || st[2] < 0 || st[2] >= Ds) break;
+    }
+    p.vl[r] = vlen;
+    if (p.cnt_c) p.cnt_c[r] = cc;
+    if (p.cnt) p.cnt[r] = fc;
+    if (p.st) {
+      if (cc > 0) atomicMax(&p.st->max_coarse, cc);
+      if (fc > 0) atomicMax(&p.st->max_fine, fc);
+      if (cc > p.Wc || fc > p.Wf) atomicOr(&p.st->flags, SG_FLAG_HIT_OVERFLOW);
     }
   }
-  p.vl[r] = vlen;
-  if (p.cnt_c) p.cnt_c[r] = cc;
-  if (p.cnt) p.cnt[r] = fc;
-  if (p.st) {
-    if (cc > 0) atomicMax(&p.st->max_coarse, cc);
-    if (fc > 0) atomicMax(&p.st->max_fine, fc);
-    if (cc > p.Wc || fc > p.Wf) atomicOr(&p.st->flags, SG_FLAG_HIT_OVERFLOW);
+  // -1 padding of the warp's 32 rows, each by the whole warp (16-byte
+  // stores; the rays' own threads would write them one element at a time)
+  const int lane = lane_id();
+  const long r0 = r - lane;
+  for (int i = 0; i < 32; i++) {
+    const int ci = __shfl_sync(SG_FULL, cc, i), fi = __shfl_sync(SG_FULL, fc, i);
+    const long ri = r0 + i;
+    if (ri >= p.R) break;
+    pad_row_tail(p.idx_c, p.t0_c, p.t1_c, (size_t)ri * p.Wc, min(ci, p.Wc), p.Wc, lane);
+    pad_row_tail(p.idx, p.t0, p.t1, (size_t)ri * p.Wf, min(fi, p.Wf), p.Wf, lane);
   }
 }
 
@@ -611,9 +659,8 @@ extern "C" int sg_octree_traversal(const SgOctree *tree, const float *ori, const
   const long R = (long)tree->B * N;
   OctTravParams p{*tree, ori, dir, N, tree->L - 1 - start_level, Wc, Wf, th_early_stop, opt_num,
                   idx_c, t0_c, t1_c, cnt_c, idx, t0, t1, cnt, valid_len, status, R};
-  octree_traverse_kernel<<<ceil_div(R, 128), 128, 0, stream>>>(p);
-  launch_pad_rows(R, Wc, cnt_c, idx_c, t0_c, t1_c, stream);
-  launch_pad_rows(R, Wf, cnt, idx, t0, t1, stream);
+  // rows padded in the kernel
+  octree_traverse_kernel<<<ceil_div(R, kTravThreads), kTravThreads, 0, stream>>>(p);
   SG_LAUNCH_CHECK();
   return SG_OK;
 }
