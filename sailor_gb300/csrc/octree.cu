@@ -25,7 +25,12 @@
 // per level (no stack bound: a node's children are a contiguous run), in
 // the reference's per-node order (children last to first), and writes the
 // fine row in coarse order.  The comparison that merges a descendant into an
-// entry with bit-identical depths reads the entries already in the row.
+// entry with bit-identical depths reads the entries already in the row, and
+// only when a 64-bit filter of the coarse node's entry depths says a match
+// is possible.  Node keys decode with shifts where a level's edge is a power
+// of two, each level's node geometry is set once per ray, a node's key and
+// child run are loaded together, and each warp pads its 32 rows' tails
+// itself (16-byte stores) once its rays are done.
 //
 // Fine sampling: one warp per ray; per chunk of 32 entries a warp scan turns
 // the per-entry sample counts into slot ranges and the chunk's samples are
@@ -247,7 +252,12 @@ __device__ __forceinline__ float level_edge(const OctMeta &m, float vs, int l) {
 
 constexpr int kTravThreads = 128;
 
-__global__ void __launch_bounds__(kTravThreads) octree_traverse_kernel(OctTravParams p) {
+// one of 64 bits chosen by the bits of t (multiplicative hash)
+__device__ __forceinline__ unsigned long long t0_bit(float t) {
+  return 1ull << ((__float_as_uint(t + 0.0f) * 0x9E3779B1u) >> 26);
+}
+
+__global__ void __launch_bounds__(kTravThreads, 8) octree_traverse_kernel(OctTravParams p) {
   __shared__ OctMeta m;
   // the ray's frame's node geometry per level (edge, offset), one column
   // per thread: set once per ray instead of once per tested node
@@ -313,7 +323,18 @@ __global__ void __launch_bounds__(kTravThreads) octree_traverse_kernel(OctTravPa
         const long cell = (long)b * vt + ((long)st[0] * Ds + st[1]) * Ds + st[2];
         const int v = vol_s[cell];
         const int k0 = v - m.base[s];
-        if (v > -1 && k0 >= 0 && k0 < m.count[s] && key_s[k0] == (int)cell) {
+        bool node = v > -1 && k0 >= 0 && k0 < m.count[s];
+        int nc0 = 0, cb0 = 0;
+        if (node) {
+          // the node's key and child run, loaded together
+          const int kv = key_s[k0];
+          if (s > 0) {
+            nc0 = m.nchild[s][k0];
+            cb0 = m.child_base[s][k0];
+          }
+          node = kv == (int)cell;
+        }
+        if (node) {
           float p0, p1;
           if (slab(o, inv, node_coord(gs, bmin[0], st[0]), node_coord(gs, bmin[1], st[1]),
                    node_coord(gs, bmin[2], st[2]), gs.vs, p0, p1) &&
@@ -327,6 +348,10 @@ __global__ void __launch_bounds__(kTravThreads) octree_traverse_kernel(OctTravPa
             cc++;
             // descent from this coarse node
             const int f0 = fc;
+            // bit per hashed t0 of this coarse node's stored entries: a
+            // depth whose bit is clear matches no entry (equal depths hash
+            // alike; + 0.0f folds -0 into +0, which compare equal)
+            unsigned long long seen = fc < p.Wf ? t0_bit(p0) : 0ull;
             if (fc < p.Wf) {
               oif[fc] = v;
               o0f[fc] = p0;
@@ -334,10 +359,10 @@ __global__ void __launch_bounds__(kTravThreads) octree_traverse_kernel(OctTravPa
             }
             fc++;
             int depth = -1;
-            if (s > 0 && m.nchild[s][k0] > 0) {
+            if (nc0 > 0) {
               depth = 0;
-              cbs[0] = m.child_base[s][k0];
-              cur[0] = m.nchild[s][k0] - 1;
+              cbs[0] = cb0;
+              cur[0] = nc0 - 1;
             }
             while (depth >= 0) {
               if (cur[depth] < 0) {
@@ -348,8 +373,15 @@ __global__ void __launch_bounds__(kTravThreads) octree_traverse_kernel(OctTravPa
               const int kk = cbs[depth] + cur[depth];
               cur[depth]--;
               if (kk >= m.count[lv]) continue;  // a level past its capacity (flagged by the build)
+              // the node's key and child run, loaded together
+              const int key = m.key[lv][kk];
+              int nc = 0, cbn = 0;
+              if (lv > 0) {
+                nc = m.nchild[lv][kk];
+                cbn = m.child_base[lv][kk];
+              }
               int cx, cy, cz;
-              decode_node(m, lv, m.key[lv][kk], cx, cy, cz);
+              decode_node(m, lv, key, cx, cy, cz);
               const LevelGeom gl{g_vs[lv][tid], g_st[lv][tid]};
               float c0, c1;
               if (!slab(o, inv, node_coord(gl, bmin[0], cx), node_coord(gl, bmin[1], cy),
@@ -357,13 +389,16 @@ __global__ void __launch_bounds__(kTravThreads) octree_traverse_kernel(OctTravPa
                 continue;
               const int cid = m.base[lv] + kk;
               bool found = false;
-              const int fe = min(fc, p.Wf);
-              for (int e = f0; e < fe; e++) {
-                if (o0f[e] == c0 && o1f[e] == c1) {
-                  const int pid = oif[e];
-                  if (level_edge(m, vs, meta_level_of(m, pid)) > gl.vs) oif[e] = cid;
-                  found = true;
-                  break;
+              const unsigned long long hb = t0_bit(c0);
+              if (seen & hb) {
+                const int fe = min(fc, p.Wf);
+                for (int e = f0; e < fe; e++) {
+                  if (o0f[e] == c0 && o1f[e] == c1) {
+                    const int pid = oif[e];
+                    if (level_edge(m, vs, meta_level_of(m, pid)) > gl.vs) oif[e] = cid;
+                    found = true;
+                    break;
+                  }
                 }
               }
               if (!found) {
@@ -371,16 +406,14 @@ __global__ void __launch_bounds__(kTravThreads) octree_traverse_kernel(OctTravPa
                   oif[fc] = cid;
                   o0f[fc] = c0;
                   o1f[fc] = c1;
+                  seen |= hb;
                 }
                 fc++;
               }
-              if (lv > 0) {
-                const int nc = m.nchild[lv][kk];
-                if (nc > 0) {
-                  depth++;
-                  cbs[depth] = m.child_base[lv][kk];
-                  cur[depth] = nc - 1;
-                }
+              if (nc > 0) {
+                depth++;
+                cbs[depth] = cbn;
+                cur[depth] = nc - 1;
               }
             }
             const int fe = min(fc, p.Wf);
