@@ -9,12 +9,14 @@ to 1024^2, 7.4 M rays in all) with 32-128 adaptive samples per ray.  One
 step = fusion + tree build of all frames, intersection, forward render
 (density from the fused TSDF, colour = a linear head over a seeded
 256^3 x 16 feature grid per frame), the gradient of an L2 colour loss, and
-the backward (exact compositing adjoint, gradients scattered into the
-feature and TSDF grids) -- one launch per stage over all frames and targets,
-replayed from a CUDA graph.  value = rays of all targets / step time.  The
-plain per-frame forward-only launch sequence (the reference's call order
-through the drop-in API: integrate, build_multi_res_volumes, octree, and per
-target traversal with 128-wide padded hit rows, coarse sampling, sort, field
+the backward (exact compositing adjoint; one 32-byte record per used sample,
+then a segmented reduction over the sorted cell keys adds the feature and
+TSDF gradients into the grids without atomics, bit-identical run to run)
+-- one launch per stage over all frames and targets, replayed from a CUDA
+graph.  value = rays of all targets / step time.  The plain per-frame
+forward-only launch sequence (the reference's call order through the
+drop-in API: integrate, build_multi_res_volumes, octree, and per target
+traversal with 256-wide padded hit rows, coarse sampling, sort, field
 gathers, compositing) runs on the same inputs for the ratio.
 
 --workload plain: one frame of 4 views at 1024^2 fused into a 512^3 grid,
@@ -24,7 +26,12 @@ e2e = the same step through the public API from pinned host buffers (images,
 cameras, rays and target colours copied in; the rendered colours read
 back).  The per-step working set (> 10 GB) is far larger than L2.
 
-  python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--workload batch|plain]
+--workload diff | project | octree | nerf: the differentiation step, the
+sample projection + 2D feature gather, the multi-level tree path and
+FastNerf's occupancy network (each described at its run_* function).
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+                  [--workload batch|plain|diff|project|octree|nerf]
 """
 import argparse
 import json
