@@ -141,14 +141,37 @@ __global__ void det_unique_kernel(const uint32_t *__restrict__ key, const int *_
   }
 }
 
-// the records in sorted key order (one gathered 32-byte sector per record)
+// the records in sorted key order (one gathered 32-byte sector per record);
+// kGatherItems records a thread per step, their loads in flight together
+constexpr int kGatherItems = 4;
 __global__ void det_gather_kernel(const uint32_t *__restrict__ sorted_slot, const int *__restrict__ cnt,
                                   const GradRecord *__restrict__ rec, GradRecord *__restrict__ pay) {
   const long n = cnt[kDetValid];
-  for (long j = (long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x) {
-    const uint32_t slot = __ldg(sorted_slot + j);
-    pay[j].fw = __ldg(&rec[slot].fw);
-    pay[j].kt = __ldg(&rec[slot].kt);
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long j0 = (long)blockIdx.x * blockDim.x + threadIdx.x; j0 < n; j0 += stride * kGatherItems) {
+    uint32_t slot[kGatherItems];
+    float4 fw[kGatherItems];
+    int4 kt[kGatherItems];
+#pragma unroll
+    for (int q = 0; q < kGatherItems; q++) {
+      const long j = j0 + q * stride;
+      slot[q] = j < n ? __ldg(sorted_slot + j) : 0u;
+    }
+#pragma unroll
+    for (int q = 0; q < kGatherItems; q++) {
+      if (j0 + q * stride < n) {
+        fw[q] = __ldg(&rec[slot[q]].fw);
+        kt[q] = __ldg(&rec[slot[q]].kt);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kGatherItems; q++) {
+      const long j = j0 + q * stride;
+      if (j < n) {
+        pay[j].fw = fw[q];
+        pay[j].kt = kt[q];
+      }
+    }
   }
 }
 
@@ -165,7 +188,7 @@ __device__ __forceinline__ int lower_bound_u32(const uint32_t *a, int n, uint32_
 // Cells of parity class cls: warp per cell, its run summed in order, the
 // sums added into the 8 corner voxels of the feature grid (and TSDF grid).
 template <int C>
-__global__ void __launch_bounds__(256) det_class_kernel(DetReduceParams q, int cls) {
+__global__ void __launch_bounds__(256, 4) det_class_kernel(DetReduceParams q, int cls) {
   // per warp: the current chunk of up to 32 records of a run and the G rows
   // of their rays, loaded by all lanes at once and read back in run order
   __shared__ __align__(16) float4 s_g[8][32][4];
@@ -186,13 +209,36 @@ __global__ void __launch_bounds__(256) det_class_kernel(DetReduceParams q, int c
   const int ch = C == 16 ? 4 * (lane & 3) : (lane < 24 ? lane % 3 : 0);
   const bool fown = C == 16 || lane < 24;
   const long D = q.keys.D;
-  for (long u = lo + (((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5); u < hi;
-       u += ((long)gridDim.x * blockDim.x) >> 5) {
-    const int j0 = __ldg(q.ustart + u), j1 = __ldg(q.ustart + u + 1);
+  const long wstride = ((long)gridDim.x * blockDim.x) >> 5;
+  long u = lo + (((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  // the cell's run bounds and key, and its first 32 records, are loaded one
+  // cell ahead: while a cell is summed, the next one's loads are in flight
+  int j0 = 0, j1 = 0;
+  uint32_t ckey = 0;
+  if (u < hi) {
+    j0 = __ldg(q.ustart + u);
+    j1 = __ldg(q.ustart + u + 1);
+    ckey = __ldg(q.ukey + u);
+  }
+  float4 pf_fw = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  int4 pf_kt = make_int4(0, 0, 0, 0);
+  if (u < hi && j0 + lane < j1) {
+    pf_fw = __ldg(&q.pay[j0 + lane].fw);
+    pf_kt = __ldg(&q.pay[j0 + lane].kt);
+  }
+  for (; u < hi; u += wstride) {
+    const long un = u + wstride;
+    int nj0 = 0, nj1 = 0;
+    uint32_t nkey = 0;
+    if (un < hi) {
+      nj0 = __ldg(q.ustart + un);
+      nj1 = __ldg(q.ustart + un + 1);
+      nkey = __ldg(q.ukey + un);
+    }
     // the cell's corner values are read before its run is summed, so the
     // read of the grid overlaps the run
     int b, i0[3];
-    record_cell(q.keys, __ldg(q.ukey + u), b, i0);
+    record_cell(q.keys, ckey, b, i0);
     const int vx = i0[0] + ((cr >> 2) & 1), vy = i0[1] + ((cr >> 1) & 1), vz = i0[2] + (cr & 1);
     const bool fin = fown && vx >= 0 && vy >= 0 && vz >= 0 && vx < D && vy < D && vz < D;
     float *gp = fin ? q.grad_feat + ((((size_t)b * D + vx) * D + vy) * D + vz) * C + ch : nullptr;
@@ -211,8 +257,15 @@ __global__ void __launch_bounds__(256) det_class_kernel(DetReduceParams q, int c
       // lane jj stages the run's record c0 + jj (sorted: one coalesced load)
       // and its ray's G row; then the samples are summed in run order
       if (c0 + lane < j1) {
-        const float4 fw = __ldg(&q.pay[c0 + lane].fw);
-        const int4 kt = __ldg(&q.pay[c0 + lane].kt);
+        float4 fw;
+        int4 kt;
+        if (c0 == j0) {
+          fw = pf_fw;
+          kt = pf_kt;
+        } else {
+          fw = __ldg(&q.pay[c0 + lane].fw);
+          kt = __ldg(&q.pay[c0 + lane].kt);
+        }
         const float *g = q.ray_g + (size_t)kt.x * C;
         if (C == 16) {
 #pragma unroll
@@ -222,6 +275,11 @@ __global__ void __launch_bounds__(256) det_class_kernel(DetReduceParams q, int c
         }
         s_f[w8][lane] = fw;
         s_t[w8][lane] = __int_as_float(kt.y);
+      }
+      if (c0 == j0 && un < hi && nj0 + lane < nj1) {
+        // the next cell's first records
+        pf_fw = __ldg(&q.pay[nj0 + lane].fw);
+        pf_kt = __ldg(&q.pay[nj0 + lane].kt);
       }
       __syncwarp();
       const int m = min(32, j1 - c0);
@@ -251,6 +309,9 @@ __global__ void __launch_bounds__(256) det_class_kernel(DetReduceParams q, int c
         *gp = old.x + acc.x;
     }
     if (tin) *tp = told + acct;
+    j0 = nj0;
+    j1 = nj1;
+    ckey = nkey;
   }
 }
 

@@ -171,10 +171,16 @@ __global__ void __launch_bounds__(256) radix_hist_kernel(const uint32_t *__restr
     s_h[threadIdx.x] = 0;
     __syncthreads();
     const long base = (long)tile * kSortTile;
-#pragma unroll 4
+    uint32_t kk[kSortTile / 256];
+#pragma unroll
     for (int k = 0; k < kSortTile / 256; k++) {
       const long i = base + k * 256 + threadIdx.x;
-      if (i < n) atomicAdd(&s_h[(__ldg(keys + i) >> shift) & 0xff], 1);
+      kk[k] = i < n ? __ldg(keys + i) : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < kSortTile / 256; k++) {
+      const long i = base + k * 256 + threadIdx.x;
+      if (i < n) atomicAdd(&s_h[(kk[k] >> shift) & 0xff], 1);
     }
     __syncthreads();
     hist[(size_t)threadIdx.x * ntiles + tile] = s_h[threadIdx.x];  // digit-major, live tiles
@@ -186,7 +192,7 @@ __global__ void __launch_bounds__(256) radix_hist_kernel(const uint32_t *__restr
 // first placed in shared memory in their sorted order (digit runs in digit
 // order), then written out with consecutive threads on consecutive
 // destinations of each digit run.
-__global__ void __launch_bounds__(256) radix_scatter_kernel(const uint32_t *__restrict__ keys,
+__global__ void __launch_bounds__(256, 3) radix_scatter_kernel(const uint32_t *__restrict__ keys,
                                                             const uint32_t *__restrict__ vals,
                                                             const int *__restrict__ n_dev, int shift,
                                                             const int *__restrict__ meta,
@@ -209,12 +215,18 @@ __global__ void __launch_bounds__(256) radix_scatter_kernel(const uint32_t *__re
     const long wbase = tbase + (long)w * (R * 32);
     uint32_t k[R], v[R];
     int rank[R];
+    // all of the warp's loads first, so that they are in flight together
 #pragma unroll
     for (int q = 0; q < R; q++) {
       const long i = wbase + q * 32 + lane;
       const bool live = i < n;
       k[q] = live ? __ldg(keys + i) : 0u;
       v[q] = live ? (vals ? __ldg(vals + i) : (uint32_t)i) : 0u;
+    }
+#pragma unroll
+    for (int q = 0; q < R; q++) {
+      const long i = wbase + q * 32 + lane;
+      const bool live = i < n;
       // inactive lanes match each other on a digit value no live key has
       const unsigned dg = live ? ((k[q] >> shift) & 0xffu) : 0x100u;
       const unsigned peers = __match_any_sync(SG_FULL, dg);
