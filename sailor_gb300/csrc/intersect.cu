@@ -136,6 +136,12 @@ __global__ void __launch_bounds__(512) intersect_kernel(IsectParams p) {
               const float ivs = 1.0f / gb.vs;
               const float u0 = (o[0] - e0) * ivs, u1 = (o[1] - e1) * ivs, u2 = (o[2] - e2) * ivs;
               const float du0 = d[0] * ivs, du1 = d[1] * ivs, du2 = d[2] * ivs;
+              // the candidate ranges only need to contain the cells the
+              // ray reaches: a reciprocal's few-ulp error is far inside
+              // kMargin, and every candidate gets the exact slab test
+              // (slopes too small for a finite reciprocal keep the division)
+              const bool rcp = fabsf(du0) > 1e-20f;
+              const float idu0 = rcp ? 1.0f / du0 : 0.0f;
               const float tm_ = 1e-4f * (p1 - p0) + 1e-5f * fabsf(p1) + 1e-6f;
               const float tlo = p0 - tm_, thi = p1 + tm_;
               constexpr float kMargin = 0.02f;
@@ -143,7 +149,8 @@ __global__ void __launch_bounds__(512) intersect_kernel(IsectParams p) {
               for (int a = 0; a < r; a++) {
                 float ta, tb;
                 if (du0 != 0.0f) {
-                  float q1 = ((float)a - kMargin - u0) / du0, q2 = ((float)a + 1.0f + kMargin - u0) / du0;
+                  const float n1 = (float)a - kMargin - u0, n2 = (float)a + 1.0f + kMargin - u0;
+                  const float q1 = rcp ? n1 * idu0 : n1 / du0, q2 = rcp ? n2 * idu0 : n2 / du0;
                   ta = fminf(q1, q2);
                   tb = fmaxf(q1, q2);
                 } else {
