@@ -24,7 +24,10 @@ a 1024^2 target with up to 96 samples, forward only.
 
 e2e = the same step through the public API from pinned host buffers (images,
 cameras, rays and target colours copied in; the rendered colours read
-back).  The per-step working set (> 10 GB) is far larger than L2.
+back); the batched step's e2e goes through
+BatchPipeline.train_steps_from_host, which copies each step's inputs and
+outputs beside the neighbouring steps.  The per-step working set (> 10 GB)
+is far larger than L2.
 
 --workload diff | project | octree | nerf: the differentiation step, the
 sample projection + 2D feature gather, the multi-level tree path and
@@ -905,26 +908,18 @@ def run_batch(args):
                 tT=torch.as_tensor(np.stack([w["targets"][t]["T"] for t in bp.order])),
                 target_rgb=torch.as_tensor(target))
     host = {k: v.contiguous().pin_memory() for k, v in host.items()}
-    dst = dict(depth=bp.depth, color=bp.color, K=bp.K, RT=bp.RT, tK=bp.tK, tR=bp.tR, tT=bp.tT,
-               target_rgb=bp.target_rgb)
     out_host = torch.empty((R, 3), dtype=torch.float32).pin_memory()
     h2d = sum(v.numel() * v.element_size() for v in host.values())
     d2h = out_host.numel() * 4
-
-    def e2e_step():
-        for k in host:
-            dst[k].copy_(host[k], non_blocking=True)
-        graph.replay()
-        out_host.copy_(bp.out_rgb, non_blocking=True)
-
-    for _ in range(2):
-        e2e_step()
+    # BatchPipeline.train_steps_from_host: every step's inputs go up and its
+    # image comes back, the copies of neighbouring steps beside the step
+    feed = [(host, {"out_rgb": out_host})]
+    bp.train_steps_from_host(feed * 2, graph)
     barrier()
     f0 = torch.cuda.Event(enable_timing=True)
     f1 = torch.cuda.Event(enable_timing=True)
     f0.record()
-    for _ in range(args.steps):
-        e2e_step()
+    bp.train_steps_from_host(feed * args.steps, graph)
     f1.record()
     barrier()
     _, e2e_value = whole_job(f0.elapsed_time(f1) / args.steps, R, world, dev)

@@ -424,6 +424,95 @@ class BatchPipeline:
             self.train_step()
         return g
 
+    # step inputs a host may feed, and step outputs it may read back
+    HOST_INPUTS = ("depth", "color", "K", "RT", "tK", "tR", "tT", "ori", "dirs", "target_rgb")
+    HOST_OUTPUTS = ("out_rgb", "out_depth", "out_ws", "out_alpha", "out_loss")
+
+    def train_steps_from_host(self, batches, graph=None):
+        """Training steps fed from host memory, with the copies overlapped.
+
+        batches: iterable of (inputs, outputs) per step; inputs maps names of
+        HOST_INPUTS to pinned host tensors holding that step's values (the
+        shape and dtype of the pipeline's buffer of that name; tK / tR / tT in
+        the segment order, ``order``), outputs maps names of HOST_OUTPUTS to
+        pinned host tensors that receive the step's results.  graph: a
+        ``capture`` of this pipeline's train_step (else train_step runs).
+
+        Step i+1's inputs are copied into device staging buffers on a copy
+        stream while step i runs, then into the pipeline's buffers (a device
+        copy) when step i+1 starts; step i's outputs go to staging buffers
+        when it ends and reach the host while step i+1 runs.  Every step's
+        inputs and outputs cross the link; the steps' results equal those of
+        copy-in, train_step, copy-out in sequence.  Returns on the host at
+        once: the outputs are complete when the current stream reaches the
+        end of the enqueued work (synchronize before reading them)."""
+        main = torch.cuda.current_stream(self.dev)
+        if getattr(self, "_feed", None) is None:
+            self._feed = dict(stream=torch.cuda.Stream(device=self.dev), stage={},
+                              ev={k: torch.cuda.Event() for k in ("in_ready", "in_free", "out_ready", "out_free")})
+        f = self._feed
+        cps, ev, stage = f["stream"], f["ev"], f["stage"]
+
+        def checked(allowed, tensors):
+            for k, t in tensors.items():
+                if k not in allowed:
+                    raise ValueError(f"{k}: not one of {allowed}")
+                if k in (("ori", "dirs") if self.cameras else ("tK", "tR", "tT")):
+                    raise ValueError(f"{k}: not an input of this pipeline (its targets are "
+                                     f"{'cameras' if self.cameras else 'ray buffers'})")
+                buf = getattr(self, k, None)
+                if buf is None:
+                    raise ValueError(f"{k}: this pipeline has no such buffer")
+                if t.device.type != "cpu" or not t.is_pinned():
+                    raise ValueError(f"{k}: host tensors must be pinned CPU tensors")
+                if t.shape != buf.shape or t.dtype != buf.dtype or not t.is_contiguous():
+                    raise ValueError(f"{k}: expected a contiguous {tuple(buf.shape)} {buf.dtype} tensor")
+                if k not in stage:
+                    stage[k] = torch.empty_like(buf)
+            return tensors
+
+        def upload(inputs):
+            with torch.cuda.stream(cps):
+                cps.wait_event(ev["in_free"])  # the previous step has taken its inputs
+                for k, t in inputs.items():
+                    stage[k].copy_(t, non_blocking=True)
+                ev["in_ready"].record(cps)
+
+        it = iter(batches)
+        cur = next(it, None)
+        if cur is None:
+            return
+        checked(self.HOST_INPUTS, cur[0])
+        checked(self.HOST_OUTPUTS, cur[1])
+        cps.wait_stream(main)
+        upload(cur[0])
+        while cur is not None:
+            nxt = next(it, None)
+            if nxt is not None:
+                checked(self.HOST_INPUTS, nxt[0])
+                checked(self.HOST_OUTPUTS, nxt[1])
+            main.wait_event(ev["in_ready"])
+            for k in cur[0]:
+                getattr(self, k).copy_(stage[k], non_blocking=True)
+            ev["in_free"].record(main)
+            if nxt is not None:
+                upload(nxt[0])
+            if graph is not None:
+                graph.replay()
+            else:
+                self.train_step()
+            main.wait_event(ev["out_free"])  # the previous step's outputs have left
+            for k in cur[1]:
+                stage[k].copy_(getattr(self, k), non_blocking=True)
+            ev["out_ready"].record(main)
+            with torch.cuda.stream(cps):
+                cps.wait_event(ev["out_ready"])
+                for k, t in cur[1].items():
+                    t.copy_(stage[k], non_blocking=True)
+                ev["out_free"].record(cps)
+            cur = nxt
+        main.wait_stream(cps)
+
     def stage_times(self):
         torch.cuda.synchronize()
         out = {}

@@ -467,3 +467,50 @@ def test_parity_batch_against_oracle(work, seed):
     assert par["sample_mismatches"] == 0 and par["composite_rays_flagged"] < 0.01 * par["rays"]
     assert par["composite_within_atol"], par["composite_max_abs_err"]
     assert par["grad_fd"]["max_abs_fd"] > 0 and par["grad_fd"]["rel_err"] <= 1e-4, par["grad_fd"]
+
+
+def test_train_steps_from_host_matches_serial(work):
+    """BatchPipeline.train_steps_from_host (each step's inputs uploaded on a
+    copy stream beside the previous step, outputs read back beside the next)
+    gives, step by step, the outputs of copy-in -> train_step -> copy-out in
+    sequence bit for bit, eagerly and through a graph replay, with inputs
+    that differ from step to step; the gradient grids end as the last
+    step's.  Host tensors that are not pinned, of another shape, or not
+    inputs of this pipeline are refused."""
+    bp = _pipeline(work)
+    rng = np.random.default_rng(21)
+    base = dict(depth=bp.depth.cpu(), color=bp.color.cpu(), K=bp.K.cpu(), RT=bp.RT.cpu(), ori=bp.ori.cpu(),
+                dirs=bp.dirs.cpu())
+    steps = []
+    for q in range(4):
+        inp = {k: v.clone() for k, v in base.items()}
+        inp["depth"] *= 1.0 + 0.01 * q
+        inp["target_rgb"] = torch.as_tensor(rng.random((bp.R, 3), dtype=np.float32))
+        steps.append({k: v.contiguous().pin_memory() for k, v in inp.items()})
+    # serial reference
+    ref = []
+    for inp in steps:
+        for k, v in inp.items():
+            getattr(bp, k).copy_(v)
+        bp.train_step()
+        torch.cuda.synchronize()
+        ref.append((bp.out_rgb.cpu(), bp.out_loss.cpu(), bp.out_depth.cpu()))
+    ref_grad = bp.grad_feat.clone()
+    g = bp.capture()
+    for graph in (None, g):
+        outs = [dict(out_rgb=torch.empty((bp.R, 3)).pin_memory(), out_loss=torch.empty(bp.R).pin_memory(),
+                     out_depth=torch.empty(bp.R).pin_memory()) for _ in steps]
+        bp.train_steps_from_host(list(zip(steps, outs)), graph)
+        torch.cuda.synchronize()
+        for o, r in zip(outs, ref):
+            assert torch.equal(o["out_rgb"], r[0]) and torch.equal(o["out_loss"], r[1])
+            assert torch.equal(o["out_depth"], r[2])
+        assert torch.equal(bp.grad_feat, ref_grad)
+    assert not torch.equal(ref[0][1], ref[1][1])  # the steps did differ
+    out = dict(out_rgb=torch.empty((bp.R, 3)).pin_memory())
+    for bad, match in ((dict(depth=base["depth"]), "pinned"),
+                       (dict(depth=base["depth"][:-1].contiguous().pin_memory()), "expected"),
+                       (dict(tK=torch.zeros(len(work["targets"]), 3, 3).pin_memory()), "not an input"),
+                       (dict(weight=base["depth"].pin_memory()), "not one of")):
+        with pytest.raises(ValueError, match=match):
+            bp.train_steps_from_host([(bad, out)])
