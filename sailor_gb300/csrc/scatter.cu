@@ -189,10 +189,14 @@ __device__ __forceinline__ int lower_bound_u32(const uint32_t *a, int n, uint32_
 // sums added into the 8 corner voxels of the feature grid (and TSDF grid).
 template <int C>
 __global__ void __launch_bounds__(256, 4) det_class_kernel(DetReduceParams q, int cls) {
-  // per warp: the current chunk of up to 32 records of a run and the G rows
-  // of their rays, loaded by all lanes at once and read back in run order
+  // per warp: the current chunk of up to 32 records of a run -- per record
+  // its 8 corner weights times its compositing weight (s_a), its 8 corner
+  // weights (s_cw, for the TSDF gradient), its TSDF gradient (s_t) and its
+  // ray's G row (s_g) -- staged by all lanes at once (lane j: record j) and
+  // read back in run order
   __shared__ __align__(16) float4 s_g[8][32][4];
-  __shared__ __align__(16) float4 s_f[8][32];
+  __shared__ __align__(16) float s_a[8][32][8];
+  __shared__ __align__(16) float s_cw[8][32][8];
   __shared__ float s_t[8][32];
   __shared__ int s_rng[2];
   const int nu = q.cnt[kDetCells];
@@ -273,7 +277,19 @@ __global__ void __launch_bounds__(256, 4) det_class_kernel(DetReduceParams q, in
         } else {
           s_g[w8][lane][0] = make_float4(__ldg(g), __ldg(g + 1), __ldg(g + 2), 0.0f);
         }
-        s_f[w8][lane] = fw;
+        const float f[3] = {fw.x, fw.y, fw.z};
+        float cw[8], a[8];
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+          cw[c] = corner_weight(f, c);
+          a[c] = cw[c] * fw.w;
+        }
+        reinterpret_cast<float4 *>(s_a[w8][lane])[0] = make_float4(a[0], a[1], a[2], a[3]);
+        reinterpret_cast<float4 *>(s_a[w8][lane])[1] = make_float4(a[4], a[5], a[6], a[7]);
+        if (q.grad_tsdf) {
+          reinterpret_cast<float4 *>(s_cw[w8][lane])[0] = make_float4(cw[0], cw[1], cw[2], cw[3]);
+          reinterpret_cast<float4 *>(s_cw[w8][lane])[1] = make_float4(cw[4], cw[5], cw[6], cw[7]);
+        }
         s_t[w8][lane] = __int_as_float(kt.y);
       }
       if (c0 == j0 && un < hi && nj0 + lane < nj1) {
@@ -285,9 +301,7 @@ __global__ void __launch_bounds__(256, 4) det_class_kernel(DetReduceParams q, in
       const int m = min(32, j1 - c0);
 #pragma unroll 4
       for (int jj = 0; jj < m; jj++) {
-        const float4 fw = s_f[w8][jj];
-        const float f[3] = {fw.x, fw.y, fw.z};
-        const float a = corner_weight(f, cr) * fw.w;
+        const float a = s_a[w8][jj][cr];
         if (C == 16) {
           const float4 g = s_g[w8][jj][lane & 3];
           acc.x = __fmaf_rn(a, g.x, acc.x);
@@ -298,7 +312,7 @@ __global__ void __launch_bounds__(256, 4) det_class_kernel(DetReduceParams q, in
           const float4 g = s_g[w8][jj][0];
           acc.x = __fmaf_rn(a, ch == 0 ? g.x : (ch == 1 ? g.y : g.z), acc.x);
         }
-        if (q.grad_tsdf && lane < 8) acct = __fmaf_rn(corner_weight(f, lane), s_t[w8][jj], acct);
+        if (q.grad_tsdf && lane < 8) acct = __fmaf_rn(s_cw[w8][jj][lane], s_t[w8][jj], acct);
       }
       __syncwarp();
     }
