@@ -167,11 +167,17 @@ __global__ void __launch_bounds__(512) intersect_kernel(IsectParams p) {
                 int y1 = min(r - 1, (int)floorf(fmaxf(ya, yb) + kMargin));
                 int z0 = max(0, (int)floorf(fminf(za, zb) - kMargin));
                 int z1 = min(r - 1, (int)floorf(fmaxf(za, zb) + kMargin));
+                // occupied candidates only: row (a, y) of the mask is r
+                // bits inside one word; its set bits in [z0, z1] in order
+                const uint32_t zsel = ((2u << z1) - 1u) & ~((1u << z0) - 1u);
                 for (int y = y0; y <= y1; y++) {
-                  for (int z = z0; z <= z1; z++) {
-                    const int c = (a * r + y) * r + z;
-                    const uint32_t word = __ldg(mask + (c >> 5));
-                    if (!((word >> (c & 31)) & 1u)) continue;
+                  const int row = (a * r + y) * r;
+                  const uint32_t word = __ldg(mask + (row >> 5));
+                  uint32_t zbits = (word >> (row & 31)) & zsel;
+                  while (zbits) {
+                    const int z = __ffs(zbits) - 1;
+                    zbits &= zbits - 1u;
+                    const int c = row + z;
                     float c0, c1;
                     if (slab(o, inv, node_coord(gb, bmin[0], st[0] * r + a),
                              node_coord(gb, bmin[1], st[1] * r + y), node_coord(gb, bmin[2], st[2] * r + z),
