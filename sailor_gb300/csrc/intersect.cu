@@ -147,6 +147,11 @@ __global__ void __launch_bounds__(512) intersect_kernel(IsectParams p) {
               constexpr float kMargin = 0.02f;
               int rword = 0, rbase = 0;  // set bits of mask words [0, rword)
               for (int a = 0; a < r; a++) {
+                // an x-slab without occupied cells has no candidate
+                const int sb = a * r * r;
+                const uint32_t sw = r == 8 ? (__ldg(mask + 2 * a) | __ldg(mask + 2 * a + 1))
+                                           : ((__ldg(mask + (sb >> 5)) >> (sb & 31)) & ((1u << (r * r)) - 1u));
+                if (sw == 0u) continue;
                 float ta, tb;
                 if (du0 != 0.0f) {
                   const float n1 = (float)a - kMargin - u0, n2 = (float)a + 1.0f + kMargin - u0;
