@@ -12,7 +12,10 @@
 // slab-tested with geometry recomputed from its index (the reference copies
 // a ~1.1 KB node per test).  The default variant (intersect_kernel) tests
 // them in the ray's own thread, visiting only the children the ray can
-// reach; the warp-cooperative variant (intersect_warp_kernel, tune knob
+// reach: per x-slab of the brick (slabs without occupied cells skipped) the
+// reachable y/z ranges, and in each (x, y) row of the range the set bits of
+// the occupancy mask within the z range, in ascending order; the
+// warp-cooperative variant (intersect_warp_kernel, tune knob
 // SG_TUNE_ISECT_WARP) tests every occupied child of a hit brick with the
 // whole warp, one brick at a time -- the same rows, but measured about 8x
 // slower at 8^3 bricks, where the reach test leaves ~1/5 of the children.  Hits are appended to the
