@@ -856,6 +856,7 @@ def run_batch(args):
         barrier()
     ms_max, value = whole_job(e0.elapsed_time(e1) / args.steps, R, world, dev)
     ref_rgb = bp.out_rgb.cpu()  # the timed steps' image, for the e2e check below
+    red_sizes = bp.reduction_sizes()  # of the last timed step
 
     # per-stage times (eager pass with events on the launching stream)
     stage_sum = {}
@@ -957,7 +958,7 @@ def run_batch(args):
             plain_per_frame_fwd=dict(value=plain_value, unit=UNIT, ms_per_step=plain_ms,
                                      ratio_batched_fwd_bwd=value / plain_value),
             tsdf_gvox_s=bcfg["frames"] * bcfg["D"] ** 3 / (stages["fusion"] / 1000.0) / 1e9,
-            hits_per_ray=n_hits / R, peak_hbm_bytes=peak_mem, touched_voxels=n_touched,
+            hits_per_ray=n_hits / R, peak_hbm_bytes=peak_mem, touched_voxels=n_touched, reduction=red_sizes,
             roofline=dict(bound="hbm", kernel=dom, achieved=rl[dom], peak=pk["hbm_gbs"], unit="GB/s",
                           frac=rl[dom] / pk["hbm_gbs"], traffic=traffic, peak_kind=pk_kind,
                           algorithmic_bytes=ab[dom]),

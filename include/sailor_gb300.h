@@ -699,7 +699,13 @@ int sg_render_segments_train(const SgTree *tree, const SgRaySegments *seg,
 /* Bytes of the workspace of sg_render_segments_train_det for R rays, nseg
  * segments, C feature channels and `capacity` gradient-record slots (one
  * slot per sample of every ray with hits: sum over those rays of their S;
- * the sum over all rays always suffices). */
+ * the sum over all rays always suffices).  After a call the workspace
+ * begins with SG_DET_COUNTERS ints: [SG_DET_RAYS_WITH_HITS] the rays with
+ * hits, [SG_DET_SLOTS_NEEDED] the record slots they need, [SG_DET_SLOTS]
+ * the slots used (at most `capacity`), [SG_DET_CELLS] the distinct cells
+ * summed, [SG_DET_RECORDS] the records with a cell. */
+#define SG_DET_COUNTERS 8
+enum { SG_DET_RAYS_WITH_HITS = 0, SG_DET_SLOTS_NEEDED = 1, SG_DET_SLOTS = 2, SG_DET_CELLS = 3, SG_DET_RECORDS = 4 };
 size_t sg_train_det_workspace_bytes(long long R, int nseg, int C, long long capacity);
 
 /* The training step of sg_render_segments_train (same outputs and loss)

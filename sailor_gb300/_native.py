@@ -15,6 +15,9 @@ LIB_PATH = os.path.join(HERE, "libsailor_gb300.so")
 SG_FLAG_HIT_OVERFLOW = 1
 SG_FLAG_TREE_CAPACITY = 2
 SG_FLAG_RECORD_CAPACITY = 4
+# leading counters of the deterministic reduction's workspace
+SG_DET_COUNTERS = 8
+SG_DET_RAYS_WITH_HITS, SG_DET_SLOTS_NEEDED, SG_DET_SLOTS, SG_DET_CELLS, SG_DET_RECORDS = 0, 1, 2, 3, 4
 
 EXPORTS = (
     "sg_mask_words", "sg_status_string", "sg_version", "sg_auto_bbox", "sg_fuse_tsdf",

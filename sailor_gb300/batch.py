@@ -394,6 +394,16 @@ class BatchPipeline:
         self.grad_bricks.copy_(self.brick_node)
         self._mark("train")
 
+    def reduction_sizes(self):
+        """Sizes of the last deterministic gradient reduction (synchronizes):
+        rays with hits, record slots needed and used, records with a cell,
+        distinct cells summed."""
+        if self.det_ws is None:
+            raise RuntimeError("the pipeline reduces gradients with atomics (deterministic=False)")
+        c = self.det_ws[:4 * N.SG_DET_COUNTERS].view(torch.int32).tolist()
+        return dict(rays_with_hits=c[N.SG_DET_RAYS_WITH_HITS], slots_needed=c[N.SG_DET_SLOTS_NEEDED],
+                    slots=c[N.SG_DET_SLOTS], records=c[N.SG_DET_RECORDS], cells=c[N.SG_DET_CELLS])
+
     def zero_grads(self):
         """Clear the gradient grids entirely (after writing into them)."""
         self.grad_feat.zero_()

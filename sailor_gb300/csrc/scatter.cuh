@@ -63,8 +63,15 @@ __device__ __forceinline__ void record_cell(const RecordKeys &k, uint32_t key, i
 // ---------------------------------------------------------------------------
 // workspace and launches of the deterministic reduction (scatter.cu)
 // ---------------------------------------------------------------------------
-constexpr int kDetCounters = 8;
-enum { kDetHits = 0, kDetSlotsNeeded = 1, kDetSlots = 2, kDetCells = 3, kDetValid = 4 };
+// the workspace's leading counters (their indices are the header's SG_DET_*)
+constexpr int kDetCounters = SG_DET_COUNTERS;
+enum {
+  kDetHits = SG_DET_RAYS_WITH_HITS,
+  kDetSlotsNeeded = SG_DET_SLOTS_NEEDED,
+  kDetSlots = SG_DET_SLOTS,
+  kDetCells = SG_DET_CELLS,
+  kDetValid = SG_DET_RECORDS
+};
 
 struct DetWork {
   int *cnt;                 // counters: rays with hits, slots needed, slots used, distinct cells,

@@ -46,6 +46,27 @@ def test_status_strings_and_constants(lib):
     assert lib.sg_tree_scratch_bytes(1, 32) >= 2 * 4 * 32 ** 3
 
 
+def test_det_counter_indices_match_header(tmp_path):
+    """The Python mirror of the reduction workspace's counter indices has
+    the header's values (a probe compiled with gcc against the header)."""
+    import shutil
+    import subprocess
+    from sailor_gb300 import _native as N
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    names = ["SG_DET_COUNTERS", "SG_DET_RAYS_WITH_HITS", "SG_DET_SLOTS_NEEDED", "SG_DET_SLOTS", "SG_DET_CELLS",
+             "SG_DET_RECORDS", "SG_FLAG_HIT_OVERFLOW", "SG_FLAG_TREE_CAPACITY", "SG_FLAG_RECORD_CAPACITY"]
+    src = tmp_path / "probe.c"
+    src.write_text("\n".join(['#include <stdio.h>', '#include "sailor_gb300.h"', "int main(void) {"] +
+                             [f'  printf("{n} %d\\n", (int)({n}));' for n in names] + ["  return 0;", "}"]))
+    exe = tmp_path / "probe"
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    subprocess.check_call(["gcc", "-I", os.path.join(root, "include"), str(src), "-o", str(exe)])
+    for line in subprocess.check_output([str(exe)]).decode().splitlines():
+        n, v = line.split()
+        assert getattr(N, n) == int(v), n
+
+
 def test_null_arguments_rejected(lib):
     """Entry points validate pointers and sizes before launching."""
     from sailor_gb300 import _native as N
