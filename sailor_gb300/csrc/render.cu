@@ -61,9 +61,11 @@ struct RenderParams {
   float *out_loss;
   // gradient records instead of the scatter (deterministic reduction,
   // scatter.cu): the launch's rays are hit_ray[k], k in [*k_begin, *k_end);
-  // the sample at sorted position q of ray k goes to record slot
-  // hit_slot[k] + q (below rec_cap)
+  // ray k's used samples, in sorted position order, go to record slots
+  // hit_slot[k], hit_slot[k] + 1, ... (below rec_cap), their count to
+  // ray_nrec[k]
   const int *hit_ray, *hit_slot, *k_begin, *k_end;
+  int *ray_nrec;
   uint32_t *rec_key;
   GradRecord *rec;
   float *ray_g;  // [k][C]: head^T (colour gradient of ray k)
@@ -279,8 +281,10 @@ __device__ __forceinline__ void flush_tsdf(const RenderParams &p, int b, const C
 // the sample at sorted position i is w_i G with G = head^T g_c (g_c: the
 // gradient of the ray's colour, w_i its compositing weight): G goes to
 // ray_g[k] once per ray, and each used sample's record holds its cell (the
-// key), its cell fractions and w_i, the ray and its TSDF gradient.  Positions
-// without a contribution get the key no cell has.
+// key), its cell fractions and w_i, the ray and its TSDF gradient.  The
+// records of the samples with a cell are packed, in sorted position order,
+// at the front of the ray's slots (a warp scan over the positions); their
+// count goes to ray_nrec[k].
 template <int E, int C>
 __device__ __forceinline__ void emit_records(const RenderParams &p, long k, long r, int b, int S,
                                              const RayEval<E> &ev, const float (&w)[E], const float (&gsig)[E],
@@ -303,26 +307,35 @@ __device__ __forceinline__ void emit_records(const RenderParams &p, long k, long
   const float dr[3] = {__ldg(p.dir + r * 3), __ldg(p.dir + r * 3 + 1), __ldg(p.dir + r * 3 + 2)};
   const float dsdt_k = -p.dk * p.inv_s;
   const unsigned used = ev.proc & ev.valid;
+  const unsigned below = (1u << lane) - 1u;
+  int n = 0;  // records of the positions before this block
 #pragma unroll
   for (int e = 0; e < E; e++) {
     const int i = e * 32 + lane;
-    const long slot = base + i;
-    if (i >= S || slot >= p.rec_cap) continue;
     uint32_t key = p.keys.invalid;
-    if ((used >> e) & 1u) {
+    float f[3] = {0.0f, 0.0f, 0.0f};
+    if (i < S && ((used >> e) & 1u)) {
       const float pt[3] = {__fmaf_rn(dr[0], ev.z[e], o[0]), __fmaf_rn(dr[1], ev.z[e], o[1]),
                            __fmaf_rn(dr[2], ev.z[e], o[2])};
       int i0[3];
-      float f[3];
       tap_frac(fmin, fvs, inv_fvs, pt, i0, f);
       key = record_key(p.keys, b, i0);
-      if (key != p.keys.invalid) {
-        const float gt = p.grad_tsdf ? gsig[e] * (ev.s01[e] * (1.0f - ev.s01[e]) * dsdt_k) : 0.0f;
-        p.rec[slot].fw = make_float4(f[0], f[1], f[2], w[e]);
-        p.rec[slot].kt = make_int4((int)k, __float_as_int(gt), 0, 0);
-      }
     }
-    p.rec_key[slot] = key;
+    const bool has = key != p.keys.invalid;
+    const unsigned m = __ballot_sync(SG_FULL, has);
+    const long slot = base + n + __popc(m & below);
+    if (has && slot < p.rec_cap) {
+      const float gt = p.grad_tsdf ? gsig[e] * (ev.s01[e] * (1.0f - ev.s01[e]) * dsdt_k) : 0.0f;
+      p.rec[slot].fw = make_float4(f[0], f[1], f[2], w[e]);
+      p.rec[slot].kt = make_int4((int)k, __float_as_int(gt), 0, 0);
+      p.rec_key[slot] = key;
+    }
+    n += __popc(m);
+  }
+  if (lane == 0) {
+    // the ray's records within the slot capacity
+    const long room = p.rec_cap - base;
+    p.ray_nrec[k] = (int)(room <= 0 ? 0 : (n < room ? n : room));
   }
 }
 
@@ -376,12 +389,7 @@ __global__ void __launch_bounds__(256, kBwdMinBlocks<E, TRAIN, REC>) render_bwd_
     RayEval<E> ev;
     eval_ray<E, C, false>(p, r, b, S, sgm, sm, ev);
     if (ev.done == 0) {
-      if (REC) {
-        // no sample: the ray's record slots carry no cell
-        const long base = __ldg(p.hit_slot + it);
-        for (int i = lane; i < S; i += 32)
-          if (base + i < p.rec_cap) p.rec_key[base + i] = p.keys.invalid;
-      }
+      if (REC && lane == 0) p.ray_nrec[it] = 0;  // no sample: no record
       if (p.grad_sigma) {
         for (int i = lane; i < Smax; i += 32) {
           p.grad_sigma[(size_t)r * Smax + i] = 0.0f;
@@ -858,6 +866,7 @@ extern "C" int sg_render_segments_train_det(const SgTree *tree, const SgRaySegme
   p.grad_tsdf = grad_tsdf;
   p.hit_ray = w.hit_ray;
   p.hit_slot = w.hit_slot;
+  p.ray_nrec = w.ray_nrec;
   p.rec_key = w.rec_key;
   p.rec = w.rec;
   p.ray_g = w.ray_g;
@@ -875,5 +884,5 @@ extern "C" int sg_render_segments_train_det(const SgTree *tree, const SgRaySegme
     else rc = launch_render<16>(pg, 3, gsz, stream);
     if (rc != SG_OK) return rc;
   }
-  return launch_det_reduce(w, p.keys, (long)capacity, args->C, grad_feat, grad_tsdf, stream);
+  return launch_det_reduce(w, p.keys, R, (long)capacity, args->C, grad_feat, grad_tsdf, stream);
 }

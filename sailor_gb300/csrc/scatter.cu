@@ -9,8 +9,10 @@
 // corner, grouped by parity class), and a 32-byte record of its cell
 // fractions, its compositing weight, its ray and its TSDF gradient; the
 // ray's colour-head factor of the feature gradient goes to a per-ray table.
-// Then
-//   1. the records with a cell are compacted (slot order kept) and their
+// The pass packs each ray's records at the front of the ray's slots and
+// writes their count.  Then
+//   1. the records are compacted (slot order kept: a scan over the rays'
+//      record counts, a warp per ray moving its keys) and their
 //      keys sorted, stably, with the record slots as values (segsort.cu):
 //      records of one cell become one run, in slot order (ray order, then
 //      sorted sample order -- fixed by the ray layout); the records are
@@ -93,25 +95,22 @@ __global__ void det_seg_kernel(SgRaySegments seg, long R, const int *__restrict_
   }
 }
 
-// records with a cell (their keys are not the invalid key)
-__global__ void det_valid_flags_kernel(const uint32_t *__restrict__ key, const int *__restrict__ cnt,
-                                       uint32_t invalid, int *__restrict__ flag) {
-  const long n = cnt[kDetSlots];
-  for (long j = (long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x)
-    flag[j] = __ldg(key + j) != invalid ? 1 : 0;
-}
-
-// the records with a cell, compacted in slot order: key and slot
-__global__ void det_compact_kernel(const uint32_t *__restrict__ key, const int *__restrict__ cnt, uint32_t invalid,
-                                   const int *__restrict__ pos, uint32_t *__restrict__ ckey,
-                                   uint32_t *__restrict__ cslot) {
-  const long n = cnt[kDetSlots];
-  for (long j = (long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x) {
-    const uint32_t k = __ldg(key + j);
-    if (k != invalid) {
-      const int i = pos[j];
-      ckey[i] = k;
-      cslot[i] = (uint32_t)j;
+// the records, compacted in slot order (ray order, then sorted position
+// order: each ray's records lead its slots): key and slot, a warp per ray;
+// first = the rays' exclusive record counts
+__global__ void det_compact_kernel(const uint32_t *__restrict__ key, const int *__restrict__ cnt,
+                                   const int *__restrict__ first, const int *__restrict__ hit_slot,
+                                   uint32_t *__restrict__ ckey, uint32_t *__restrict__ cslot) {
+  const long n = cnt[kDetHits];
+  const int total = cnt[kDetValid];
+  const int lane = lane_id();
+  for (long k = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < n;
+       k += ((long)gridDim.x * blockDim.x) >> 5) {
+    const int a = __ldg(first + k), e = k + 1 < n ? __ldg(first + k + 1) : total;
+    const long base = __ldg(hit_slot + k);
+    for (int i = lane; i < e - a; i += 32) {
+      ckey[a + i] = __ldg(key + base + i);
+      cslot[a + i] = (uint32_t)(base + i);
     }
   }
 }
@@ -348,6 +347,7 @@ size_t det_layout(long R, int nseg, int C, long cap, char *base, DetWork *w) {
   d.hit_ray = (int *)take((size_t)R * 4);
   d.hit_slot = (int *)take((size_t)R * 4);
   d.seg_hit = (int *)take((size_t)(nseg + 1) * 4);
+  d.ray_nrec = (int *)take((size_t)R * 4);
   d.ray_g = (float *)take((size_t)R * C * 4);
   d.rec_key = (uint32_t *)take((size_t)cap * 4);
   d.rec = (GradRecord *)take((size_t)cap * sizeof(GradRecord));
@@ -383,16 +383,17 @@ int launch_det_prepare(const DetWork &w, const SgRaySegments &seg, int S_max, co
   return SG_OK;
 }
 
-int launch_det_reduce(const DetWork &w, const RecordKeys &keys, long cap, int C, float *grad_feat, float *grad_tsdf,
+int launch_det_reduce(const DetWork &w, const RecordKeys &keys, long R, long cap, int C, float *grad_feat,
+                      float *grad_tsdf,
                       sg_stream_t stream) {
   int key_bits = 1;
   while (key_bits < 32 && ((uint64_t)1 << key_bits) <= (uint64_t)keys.invalid) key_bits++;
   const int g = grid_for(cap, 16);
-  // the records with a cell, compacted into the b pair (slot order kept)
-  int *flag = (int *)w.ka;
-  det_valid_flags_kernel<<<g, 256, 0, stream>>>(w.rec_key, w.cnt, keys.invalid, flag);
-  launch_excl_scan_dev(flag, cap, w.cnt + kDetSlots, flag, w.scan_scratch, w.cnt + kDetValid, stream);
-  det_compact_kernel<<<g, 256, 0, stream>>>(w.rec_key, w.cnt, keys.invalid, flag, w.kb, w.vb);
+  // the records, compacted into the b pair (slot order kept): the rays'
+  // record counts scanned in place into their first positions
+  launch_excl_scan_dev(w.ray_nrec, R, w.cnt + kDetHits, w.ray_nrec, w.scan_scratch, w.cnt + kDetValid, stream);
+  det_compact_kernel<<<grid_for(R * 32, 16), 256, 0, stream>>>(w.rec_key, w.cnt, w.ray_nrec, w.hit_slot, w.kb,
+                                                                w.vb);
   const int passes = launch_radix_sort(w.kb, w.vb, w.cnt + kDetValid, cap, key_bits, w.ka, w.va, w.kb, w.vb,
                                        w.sort_scratch, stream);
   const uint32_t *skey = (passes & 1) ? w.ka : w.kb;

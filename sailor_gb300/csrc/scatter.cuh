@@ -79,6 +79,7 @@ struct DetWork {
   int *hitb, *slotb;        // [R]: per ray -> exclusive counts of rays with hits / record slots
   int *hit_ray, *hit_slot;  // [R]: compact list of rays with hits, first slot of each
   int *seg_hit;             // [segments + 1]: compact index of each segment's first ray
+  int *ray_nrec;            // [R]: per compact ray, its records (then their first position)
   float *ray_g;             // [R][C]: per compact ray, head^T (colour gradient)
   uint32_t *rec_key;        // [cap] cell key per slot (later: the distinct cells' keys)
   GradRecord *rec;          // [cap] record per slot
@@ -115,7 +116,8 @@ int launch_det_prepare(const DetWork &w, const SgRaySegments &seg, int S_max, co
 
 // Sort the records, find the distinct cells and add their gradients into
 // the grids (grad_tsdf may be null).
-int launch_det_reduce(const DetWork &w, const RecordKeys &keys, long cap, int C, float *grad_feat, float *grad_tsdf,
+int launch_det_reduce(const DetWork &w, const RecordKeys &keys, long R, long cap, int C, float *grad_feat,
+                      float *grad_tsdf,
                       sg_stream_t stream);
 
 }  // namespace sg
