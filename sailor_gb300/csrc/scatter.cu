@@ -186,7 +186,9 @@ __device__ __forceinline__ int lower_bound_u32(const uint32_t *a, int n, uint32_
 
 // Cells of parity class cls: warp per cell, its run summed in order, the
 // sums added into the 8 corner voxels of the feature grid (and TSDF grid).
-template <int C>
+// TSDF: the TSDF gradient is reduced too (q.grad_tsdf set); without it the
+// kernel holds no TSDF staging, which leaves more of the SM's L1 to the G rows
+template <int C, bool TSDF>
 __global__ void __launch_bounds__(256, 4) det_class_kernel(DetReduceParams q, int cls) {
   // per warp: the current chunk of up to 32 records of a run -- per record
   // its 8 corner weights times its compositing weight (s_a), its 8 corner
@@ -195,8 +197,8 @@ __global__ void __launch_bounds__(256, 4) det_class_kernel(DetReduceParams q, in
   // read back in run order
   __shared__ __align__(16) float4 s_g[8][32][4];
   __shared__ __align__(16) float s_a[8][32][8];
-  __shared__ __align__(16) float s_cw[8][32][8];
-  __shared__ float s_t[8][32];
+  __shared__ __align__(16) float s_cw[TSDF ? 8 : 1][32][8];
+  __shared__ float s_t[TSDF ? 8 : 1][32];
   __shared__ int s_rng[2];
   const int nu = q.cnt[kDetCells];
   if (threadIdx.x == 0) {
@@ -251,7 +253,7 @@ __global__ void __launch_bounds__(256, 4) det_class_kernel(DetReduceParams q, in
       else old.x = *gp;
     }
     const int tx = i0[0] + ((lane >> 2) & 1), ty = i0[1] + ((lane >> 1) & 1), tz = i0[2] + (lane & 1);
-    const bool tin = q.grad_tsdf && lane < 8 && tx >= 0 && ty >= 0 && tz >= 0 && tx < D && ty < D && tz < D;
+    const bool tin = TSDF && lane < 8 && tx >= 0 && ty >= 0 && tz >= 0 && tx < D && ty < D && tz < D;
     float *tp = tin ? q.grad_tsdf + (((size_t)b * D + tx) * D + ty) * D + tz : nullptr;
     const float told = tin ? *tp : 0.0f;
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -285,11 +287,11 @@ __global__ void __launch_bounds__(256, 4) det_class_kernel(DetReduceParams q, in
         }
         reinterpret_cast<float4 *>(s_a[w8][lane])[0] = make_float4(a[0], a[1], a[2], a[3]);
         reinterpret_cast<float4 *>(s_a[w8][lane])[1] = make_float4(a[4], a[5], a[6], a[7]);
-        if (q.grad_tsdf) {
+        if (TSDF) {
           reinterpret_cast<float4 *>(s_cw[w8][lane])[0] = make_float4(cw[0], cw[1], cw[2], cw[3]);
           reinterpret_cast<float4 *>(s_cw[w8][lane])[1] = make_float4(cw[4], cw[5], cw[6], cw[7]);
+          s_t[w8][lane] = __int_as_float(kt.y);
         }
-        s_t[w8][lane] = __int_as_float(kt.y);
       }
       if (c0 == j0 && un < hi && nj0 + lane < nj1) {
         // the next cell's first records
@@ -311,7 +313,7 @@ __global__ void __launch_bounds__(256, 4) det_class_kernel(DetReduceParams q, in
           const float4 g = s_g[w8][jj][0];
           acc.x = __fmaf_rn(a, ch == 0 ? g.x : (ch == 1 ? g.y : g.z), acc.x);
         }
-        if (q.grad_tsdf && lane < 8) acct = __fmaf_rn(s_cw[w8][jj][lane], s_t[w8][jj], acct);
+        if (TSDF && lane < 8) acct = __fmaf_rn(s_cw[w8][jj][lane], s_t[w8][jj], acct);
       }
       __syncwarp();
     }
@@ -410,8 +412,14 @@ int launch_det_reduce(const DetWork &w, const RecordKeys &keys, long R, long cap
   det_gather_kernel<<<g, 256, 0, stream>>>(sval, w.cnt, w.rec, w.pay);
   DetReduceParams q{keys, w.cnt, ukey, ustart, w.pay, w.ray_g, grad_feat, grad_tsdf};
   for (int cls = 0; cls < 8; cls++) {
-    if (C == 16) det_class_kernel<16><<<num_sms() * 8, 256, 0, stream>>>(q, cls);
-    else det_class_kernel<3><<<num_sms() * 8, 256, 0, stream>>>(q, cls);
+    const dim3 g(num_sms() * 8), blk(256);
+    if (C == 16) {
+      if (grad_tsdf) det_class_kernel<16, true><<<g, blk, 0, stream>>>(q, cls);
+      else det_class_kernel<16, false><<<g, blk, 0, stream>>>(q, cls);
+    } else {
+      if (grad_tsdf) det_class_kernel<3, true><<<g, blk, 0, stream>>>(q, cls);
+      else det_class_kernel<3, false><<<g, blk, 0, stream>>>(q, cls);
+    }
   }
   SG_LAUNCH_CHECK();
   return SG_OK;
