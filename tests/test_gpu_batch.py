@@ -335,6 +335,14 @@ def test_record_capacity_reported(work):
     torch.cuda.synchronize()
     assert bp.status[0].item() & N.SG_FLAG_RECORD_CAPACITY
     assert torch.equal(bp.out_rgb, full.out_rgb)
+    # the reduction's sizes: the same rays and slot needs; the capped
+    # pipeline keeps the records of its first 1000 slots only
+    a, c = full.reduction_sizes(), bp.reduction_sizes()
+    hits = int((full.hit_count > 0).sum().item())
+    assert a["rays_with_hits"] == c["rays_with_hits"] == hits
+    assert a["slots_needed"] == c["slots_needed"] == a["slots"] > 1000 == c["slots"]
+    assert 0 < a["cells"] <= a["records"] <= a["slots"] and a["cells"] > 100
+    assert 0 < c["cells"] <= c["records"] <= 1000
 
 
 @pytest.mark.parametrize("n,cap,bits", [(1, 16, 8), (5000, 8192, 12), (300000, 300000, 31), (70000, 100000, 20)])
