@@ -211,6 +211,7 @@ class BatchPipeline:
         self.events = None
         self.side_events = None
         self.side = torch.cuda.Stream(device=dev)  # zeroing of the gradient grids beside fusion
+        self._feed = None  # copy stream, staging buffers and events of train_steps_from_host
 
     # ------------------------------------------------------------------ inputs
     def load_views(self, frames, vol_bbox, voxel_size, trunc_weight):
@@ -457,7 +458,7 @@ class BatchPipeline:
         once: the outputs are complete when the current stream reaches the
         end of the enqueued work (synchronize before reading them)."""
         main = torch.cuda.current_stream(self.dev)
-        if getattr(self, "_feed", None) is None:
+        if self._feed is None:
             self._feed = dict(stream=torch.cuda.Stream(device=self.dev), stage={},
                               ev={k: torch.cuda.Event() for k in ("in_ready", "in_free", "out_ready", "out_free")})
         f = self._feed
